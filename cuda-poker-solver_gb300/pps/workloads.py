@@ -1,0 +1,208 @@
+"""Seeded synthetic spots for the solver's tests and benchmarks.
+
+Every random draw comes from one documented generator, splitmix64 (Steele,
+Lea, Flood 2014): state += 0x9E3779B97F4A7C15, then the two xor-shift-
+multiply rounds; a uniform double is (x >> 11) * 2**-53. Boards draw
+``next() % 52`` and reject repeats.
+
+Named spots (pot/stack in chips, bets as pot fractions, "a" = all-in):
+
+* ``river_c1``   river, both ranges all 1081 unblocked combos with weights
+  U(0,1); pot 100, stack 100; bets {0.5, 1.0, a}, raises {2.0}, max 2.
+* ``turn_c2``    turn, all 1128 combos U(0,1); pot 100, stack 200; turn bets
+  {0.33, 0.75, a}, river bets {0.5, 1.0, a}, raises {2.5}, max 3 bets per
+  street (per-street configs; ``turn_c2_uniform`` uses the turn config on
+  both streets, the only form the reference can express).
+* ``turn_c3``    turn, 60% of combos U(0.5,1) and the rest U(0,0.2); pot
+  100, stack 400; bets {0.25, 0.5, 1.0, 1.5, a}, raises {2.0}, max 4
+  (48,255 nodes).
+* ``turn_w52``   the reference's own "wide" bench spot (tools/quality/
+  bench_turn.sh:40-41): Qs9h2d7c, 300/1500, bets {0.25,0.5,0.75,1.25},
+  raises {2.5,3.0}, ranges "22+,A9s+,KTs+,QJs,JTs,T9s" vs the same plus
+  "AQo+" (51,903 nodes).
+* ``turn_api``   the reference's API test spot (python/test_pps.py:18-24).
+* ``turn_tiny``  the reference's known-answer spot (tools/tiny_check.cpp:
+  75-79, driven by tools/quality/gpu_postflop_parity.sh:139).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import List, Optional
+import math
+
+MASK64 = (1 << 64) - 1
+RANKS = "23456789TJQKA"
+SUITS = "cdhs"
+
+
+class SplitMix64:
+    def __init__(self, seed: int):
+        self.state = seed & MASK64
+
+    def next(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & MASK64
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK64
+        return z ^ (z >> 31)
+
+    def uniform(self) -> float:
+        return (self.next() >> 11) * (2.0 ** -53)
+
+
+def card_id(text: str) -> int:
+    return SUITS.index(text[1].lower()) * 13 + RANKS.index(text[0].upper())
+
+
+def card_text(cid: int) -> str:
+    return RANKS[cid % 13] + SUITS[cid // 13]
+
+
+def board_ids(text: str) -> List[int]:
+    return [card_id(text[i:i + 2]) for i in range(0, len(text), 2)]
+
+
+def draw_board(rng: SplitMix64, n: int) -> List[int]:
+    out: List[int] = []
+    while len(out) < n:
+        c = rng.next() % 52
+        if c not in out:
+            out.append(c)
+    return out
+
+
+@dataclass
+class BetCfg:
+    """pf::BetConfig (src/postflop_cfr.h:24-42)."""
+    bets: List[float] = field(default_factory=list)
+    raises: List[float] = field(default_factory=list)
+    allin: bool = False
+    geometric: bool = False
+    max_raises: int = 0
+    add_allin: float = 1.5
+    force_allin: float = 0.15
+    merging: float = 0.1
+
+    def bet_text(self) -> str:
+        toks = ["%g" % b for b in self.bets]
+        if self.allin:
+            toks.append("a")
+        if self.geometric:
+            toks.append("e")
+        return ",".join(toks)
+
+    def raise_text(self) -> str:
+        return ",".join("%g" % r for r in self.raises)
+
+
+@dataclass
+class Spot:
+    name: str
+    board: List[int]
+    oop: object            # 1326 weights (list) or a range string
+    ip: object
+    pot: int
+    stack: int
+    cfg: BetCfg
+    street_cfgs: Optional[List[BetCfg]] = None  # [flop, turn, river]
+    iterations: int = 1000
+
+    def board_text(self) -> str:
+        return "".join(card_text(c) for c in self.board)
+
+
+def uniform_weights(rng: SplitMix64) -> List[float]:
+    return [rng.uniform() for _ in range(1326)]
+
+
+def mixture_weights(rng: SplitMix64) -> List[float]:
+    out = []
+    for _ in range(1326):
+        if rng.uniform() < 0.6:
+            out.append(0.5 + 0.5 * rng.uniform())
+        else:
+            out.append(0.2 * rng.uniform())
+    return out
+
+
+def river_c1(seed: int = 101) -> Spot:
+    rng = SplitMix64(seed)
+    board = draw_board(rng, 5)
+    return Spot("river_c1", board, uniform_weights(rng), uniform_weights(rng),
+                100, 100, BetCfg([0.5, 1.0], [2.0], allin=True, max_raises=2),
+                iterations=1000)
+
+
+def turn_c2(seed: int = 202, uniform_config: bool = False) -> Spot:
+    rng = SplitMix64(seed)
+    board = draw_board(rng, 4)
+    turn = BetCfg([0.33, 0.75], [2.5], allin=True, max_raises=3)
+    river = BetCfg([0.5, 1.0], [2.5], allin=True, max_raises=3)
+    s = Spot("turn_c2", board, uniform_weights(rng), uniform_weights(rng),
+             100, 200, turn, [turn, turn, river], iterations=500)
+    if uniform_config:
+        s.name = "turn_c2_uniform"
+        s.street_cfgs = None
+    return s
+
+
+def turn_c3(seed: int = 303) -> Spot:
+    rng = SplitMix64(seed)
+    board = draw_board(rng, 4)
+    return Spot("turn_c3", board, mixture_weights(rng), mixture_weights(rng),
+                100, 400,
+                BetCfg([0.25, 0.5, 1.0, 1.5], [2.0], allin=True, max_raises=4),
+                iterations=1000)
+
+
+def turn_w52() -> Spot:
+    return Spot("turn_w52", board_ids("Qs9h2d7c"), "22+,A9s+,KTs+,QJs,JTs,T9s",
+                "22+,A9s+,KTs+,QJs,JTs,T9s,AQo+", 300, 1500,
+                BetCfg([0.25, 0.5, 0.75, 1.25], [2.5, 3.0]), iterations=2000)
+
+
+def turn_api() -> Spot:
+    return Spot("turn_api", board_ids("Qs9h2d7c"), "TT+,AKo", "AQ+,KQs", 200,
+                500, BetCfg([0.75], [2.5, 3.0], allin=True), iterations=300)
+
+
+def turn_tiny() -> Spot:
+    return Spot("turn_tiny", board_ids("Qs9h2d7c"), "TT+", "99+", 200, 3000,
+                BetCfg([0.5], []), iterations=0)
+
+
+def batched(count: int = 256, seed: int = 404) -> List[Spot]:
+    """The batched/served distribution: 70% river / 30% turn spots, weights
+    U(0,1), pot U(50,200), stack/pot log-uniform in [1, 8], 2-4 bet sizes
+    from {25,33,50,75,100,150}% plus all-in, raises {2.5}, max 3."""
+    rng = SplitMix64(seed)
+    sizes = [0.25, 0.33, 0.5, 0.75, 1.0, 1.5]
+    out = []
+    for k in range(count):
+        river = rng.uniform() < 0.7
+        board = draw_board(rng, 5 if river else 4)
+        pot = 50 + int(150 * rng.uniform())
+        spr = math.exp(math.log(8.0) * rng.uniform())
+        stack = max(1, int(round(pot * spr)))
+        n_sizes = 2 + int(3 * rng.uniform())
+        pool = list(sizes)
+        chosen = []
+        for _ in range(min(n_sizes, 4)):
+            chosen.append(pool.pop(rng.next() % len(pool)))
+        chosen.sort()
+        out.append(Spot("batch_%03d" % k, board, uniform_weights(rng),
+                        uniform_weights(rng), pot, stack,
+                        BetCfg(chosen, [2.5], allin=True, max_raises=3),
+                        iterations=1000))
+    return out
+
+
+NAMED = {
+    "river_c1": river_c1,
+    "turn_c2": turn_c2,
+    "turn_c2_uniform": lambda: turn_c2(uniform_config=True),
+    "turn_c3": turn_c3,
+    "turn_w52": turn_w52,
+    "turn_api": turn_api,
+    "turn_tiny": turn_tiny,
+}

@@ -1,0 +1,239 @@
+/* pps_gb.h - C ABI of the GB300-native postflop DCFR solver (libpps_gb.so).
+ *
+ * This is the drop-in boundary: every entry point mirrors one method of the
+ * reference's pps::gpu::GpuPostflopSolver (cuda/gpu_cfr.h:141-264), which
+ * the reference's own FFI (the pybind module, python/pps_native.cpp:514-551)
+ * binds. Plain pointers and sizes only; results go into caller buffers
+ * whose maximum sizes are fixed by PPS_GB_MAX_ACTIONS and PPS_GB_COMBOS.
+ *
+ * Every call returns PPS_GB_OK (0) or an error code; pps_gb_last_error()
+ * gives the calling thread's message for its last failed call. The library
+ * never exits the process. A handle is not thread-safe: drive one solver
+ * from one thread at a time (the reference has the same rule,
+ * python/pps_native.cpp:256-259).
+ */
+#ifndef PPS_GB_H
+#define PPS_GB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PPS_GB_ABI_VERSION 1
+#define PPS_GB_MAX_ACTIONS 32 /* reference kMaxNa, cuda/gpu_cfr.cu:41 */
+#define PPS_GB_COMBOS 1326    /* reference kCombos, src/range.h:14 */
+#define PPS_GB_MAX_SIZES 16
+
+enum {
+  PPS_GB_OK = 0,
+  PPS_GB_E_ARG = 1,         /* invalid argument (bad board, config, algo) */
+  PPS_GB_E_INDEX = 2,       /* node / action / player index out of range */
+  PPS_GB_E_STATE = 3,       /* call not valid in the current state */
+  PPS_GB_E_IO = 4,          /* file cannot be opened / written */
+  PPS_GB_E_FORMAT = 5,      /* corrupt, truncated or mismatched file */
+  PPS_GB_E_CUDA = 6,        /* CUDA runtime error (message has details) */
+  PPS_GB_E_MEMORY = 7,      /* host or device allocation failed */
+  PPS_GB_E_DEVICE = 8,      /* a kernel raised its device error flag */
+  PPS_GB_E_BUDGET = 9,      /* admission refused: over the HBM budget */
+  PPS_GB_E_TOO_WIDE = 10    /* more than PPS_GB_MAX_ACTIONS actions */
+};
+
+typedef struct pps_gb_solver pps_gb_solver;
+
+/* pf::BetConfig (src/postflop_cfr.h:24-42). */
+typedef struct {
+  double bet_fracs[PPS_GB_MAX_SIZES];
+  int n_bet_fracs;
+  double raise_mults[PPS_GB_MAX_SIZES];
+  int n_raise_mults;
+  int bet_allin;
+  int bet_geometric;
+  int max_raises;
+  double add_allin_threshold;
+  double force_allin_threshold;
+  double merging_threshold;
+} pps_gb_bet_config;
+
+/* gpu::PostflopSpot (cuda/gpu_cfr.h:35-42); card id = suit*13 + rank. */
+typedef struct {
+  uint8_t board[5];
+  int n_board; /* 3, 4 or 5 */
+  double oop[PPS_GB_COMBOS];
+  double ip[PPS_GB_COMBOS];
+  int64_t pot;
+  int64_t stack;
+} pps_gb_spot;
+
+/* gpu::ActionLabel (cuda/gpu_cfr.h:48-51); kind = pf::ActionKind value
+ * (0 fold, 1 check, 2 call, 3 bet, 4 raise, 5 all-in). */
+typedef struct {
+  int32_t kind;
+  int64_t amount;
+} pps_gb_action;
+
+/* pf::NodeStats (src/postflop_cfr.h:55-60). */
+typedef struct {
+  double ev0;
+  double ev1;
+  double expl;
+  int64_t pair_mass;
+} pps_gb_node_stats;
+
+/* Scalars of a compiled solver (numNodes/maxDepth/iterationsRun/... of
+ * cuda/gpu_cfr.h:176-241). */
+typedef struct {
+  int32_t num_nodes;
+  int32_t max_depth;
+  int32_t num_decide_nodes;
+  int32_t iterations_run;
+  int64_t total_iterations;
+  int32_t n_base[2];
+  int64_t row_total; /* regret (= strategy) row entries, reference regTotal */
+  int32_t empty;     /* 1 when a range compiled to no combos */
+  int32_t launches_per_iteration;
+  int64_t device_bytes;
+} pps_gb_info;
+
+/* gpu::DecideNodeInfo (cuda/gpu_cfr.h:54-62). */
+typedef struct {
+  int32_t node_id;
+  int32_t player;
+  int32_t depth;
+  int32_t n_board;
+  int32_t n_combos;
+  int32_t n_actions;
+  pps_gb_action actions[PPS_GB_MAX_ACTIONS];
+  int32_t children[PPS_GB_MAX_ACTIONS];
+} pps_gb_decide_info;
+
+const char* pps_gb_last_error(void);
+int pps_gb_abi_version(void);
+/* The bet config defaults of pf::BetConfig (src/postflop_cfr.h:24-42). */
+void pps_gb_bet_config_default(pps_gb_bet_config* cfg);
+
+/* GpuPostflopSolver(spot, cfg) - cuda/gpu_cfr.h:144. */
+int pps_gb_create(const pps_gb_spot* spot, const pps_gb_bet_config* cfg,
+                  pps_gb_solver** out);
+/* Extension: one bet config per street (cfgs[k] where the board has 3+k
+ * cards); no reference counterpart (the reference shares one config,
+ * cuda/gpu_cfr.cu:1254-1256). */
+int pps_gb_create_streets(const pps_gb_spot* spot,
+                          const pps_gb_bet_config cfgs[3],
+                          pps_gb_solver** out);
+/* GpuPostflopSolver(solutionPath) - cuda/gpu_cfr.h:149. */
+int pps_gb_load(const char* path, pps_gb_solver** out);
+/* ~GpuPostflopSolver - cuda/gpu_cfr.h:150. NULL is ignored. */
+void pps_gb_destroy(pps_gb_solver* h);
+
+/* solve(iterations, algo, target) - cuda/gpu_cfr.h:160. */
+int pps_gb_solve(pps_gb_solver* h, int iterations, const char* algo,
+                 double target);
+/* continueSolve(iterations, target) - cuda/gpu_cfr.h:168. */
+int pps_gb_continue(pps_gb_solver* h, int iterations, double target);
+/* reset() - cuda/gpu_cfr.h:172. */
+int pps_gb_reset(pps_gb_solver* h);
+/* numNodes/maxDepth/numDecideNodes/iterationsRun/totalIterations. */
+int pps_gb_get_info(pps_gb_solver* h, pps_gb_info* out);
+
+/* stats() - cuda/gpu_cfr.h:184 (FP64 walks on the device). */
+int pps_gb_stats(pps_gb_solver* h, pps_gb_node_stats* out);
+/* rootStrategy() - cuda/gpu_cfr.h:187; freq[PPS_GB_MAX_ACTIONS]. */
+int pps_gb_root_strategy(pps_gb_solver* h, double* freq, int* n_actions);
+/* nodeStrategy(i) - cuda/gpu_cfr.h:196; *n_actions = 0 where the reference
+ * returns {} (nodes past a chance node). */
+int pps_gb_node_strategy(pps_gb_solver* h, int decide_idx, double* freq,
+                         int* n_actions);
+/* decideNode(i) - cuda/gpu_cfr.h:201. */
+int pps_gb_decide_node(pps_gb_solver* h, int decide_idx,
+                       pps_gb_decide_info* out);
+/* comboStrategy(i) - cuda/gpu_cfr.h:208: actions[PPS_GB_MAX_ACTIONS],
+ * combos[PPS_GB_COMBOS], freqs[PPS_GB_MAX_ACTIONS * PPS_GB_COMBOS]
+ * (action-major, row stride = *n_combos). */
+int pps_gb_combo_strategy(pps_gb_solver* h, int decide_idx, int* n_actions,
+                          int* n_combos, pps_gb_action* actions,
+                          int* combos, double* freqs);
+/* rootEvPerCombo() - cuda/gpu_cfr.h:211, one player per call; combos, ev,
+ * mass hold PPS_GB_COMBOS entries. */
+int pps_gb_root_ev(pps_gb_solver* h, int player, int* n, int* combos,
+                   double* ev, double* mass);
+/* nodeEv(i) - cuda/gpu_cfr.h:216. Per side p (0, 1): n_combos[p],
+ * combos/ev/mass[p * PPS_GB_COMBOS + i], agg_ev[p]. Per action a:
+ * action_ev[a * PPS_GB_COMBOS + i] over the decider's combos and
+ * action_agg[a]. */
+int pps_gb_node_ev(pps_gb_solver* h, int decide_idx, int* decider,
+                   int* n_actions, pps_gb_action* actions, int* n_combos,
+                   int* combos, double* ev, double* mass, double* agg_ev,
+                   double* action_ev, double* action_agg);
+/* runoutSummary(i, a) - cuda/gpu_cfr.h:222. Per branch b (< 52):
+ * cards[b], next_decide[b], n_freq[b], freq[b * PPS_GB_MAX_ACTIONS + k],
+ * agg_ev[b * 2 + p]. */
+int pps_gb_runout_summary(pps_gb_solver* h, int decide_idx, int action_idx,
+                          int* decider, int* n_actions,
+                          pps_gb_action* actions, int* n_branches,
+                          int* cards, int* next_decide, int* n_freq,
+                          double* freq, double* agg_ev);
+/* playerCards(p) / numBaseCombos(p) - cuda/gpu_cfr.h:227-230:
+ * cards[2 * PPS_GB_COMBOS]. */
+int pps_gb_player_cards(pps_gb_solver* h, int player, uint8_t* cards, int* n);
+/* playerWeights(p) - cuda/gpu_cfr.h:234: w[PPS_GB_COMBOS]. */
+int pps_gb_player_weights(pps_gb_solver* h, int player, double* w, int* n);
+/* treeStructure() - cuda/gpu_cfr.h:238. Pass NULL arrays to get the sizes
+ * (*n_nodes, *n_children); then kinds[n_nodes], child_base[n_nodes],
+ * children[n_children], boards[5 * n_nodes]. */
+int pps_gb_tree_structure(pps_gb_solver* h, uint8_t* kinds, int* child_base,
+                          int* children, uint8_t* boards, int* n_nodes,
+                          int* n_children);
+/* save(path) - cuda/gpu_cfr.h:246 ("PPS1" file, cuda/gpu_cfr.cu:2686-2785). */
+int pps_gb_save(pps_gb_solver* h, const char* path);
+/* debugDump() - cuda/gpu_cfr.h:249. */
+int pps_gb_debug_dump(pps_gb_solver* h);
+
+/* Row access in the reference's dense layout (decide nodes in node order,
+ * each na x nC action-major at the reference regOff, cuda/gpu_cfr.cu:
+ * 1476-1481). which: 0 = cumulative regrets, 1 = cumulative strategy.
+ * Replaces the reference's debug hooks on the same rows (GPU_CFR_SEED_STRAT,
+ * cuda/gpu_cfr.cu:2066-2097, writes the strategy rows). */
+int pps_gb_read_rows(pps_gb_solver* h, int which, float* out, int64_t cap,
+                     int64_t* n);
+int pps_gb_write_rows(pps_gb_solver* h, int which, const float* in,
+                      int64_t n);
+/* One value walk (reference rootValue, cuda/gpu_cfr.cu:894-916): mode 0 =
+ * EV vs the average strategy, 1 = best response; FP64 on the device.
+ * root_cfv receives the traverser's root row (n_base[tr] entries) and
+ * *value the range-weighted root value in chips. */
+int pps_gb_walk(pps_gb_solver* h, int traverser, int mode, double* root_cfv,
+                double* value);
+/* Iteration engine choice for the CFR graph: 0 = depth-level kernels,
+ * 1 = fused leaf-street kernel where the tree allows it (default). */
+int pps_gb_set_engine(pps_gb_solver* h, int engine);
+
+/* Host-only compile (no device use): runs the tree compiler and reports
+ * every artifact in the reference's own layout (cuda/gpu_cfr.cu:1331-1827)
+ * through cb(user, name, dtype, data, count); dtype 'i' int32, 'q' int64,
+ * 'B' uint8, 'f' float32, 'd' float64. cfgs holds 1 config (all streets)
+ * or 3 (per street). */
+typedef void (*pps_gb_array_cb)(void* user, const char* name, char dtype,
+                                const void* data, int64_t count);
+int pps_gb_compile_export(const pps_gb_spot* spot,
+                          const pps_gb_bet_config* cfgs, int n_cfgs,
+                          pps_gb_array_cb cb, void* user);
+
+/* Evaluator entry (tests): strength keys of n 7-card hands (cards[7*i]). */
+int pps_gb_hand_keys(const uint8_t* cards, int n, uint64_t* keys);
+/* Bet abstraction entry (tests): pf::betActions (src/postflop_cfr.h:47-51);
+ * out[PPS_GB_MAX_ACTIONS]. */
+int pps_gb_bet_actions(int64_t pot_base, int64_t stack,
+                       const pps_gb_bet_config* cfg, int64_t sc0,
+                       int64_t sc1, int actor, int after_allin,
+                       int num_bets, int num_streets, pps_gb_action* out,
+                       int* n);
+/* Range parser entry (tests): parseRange (src/range.h:41). */
+int pps_gb_parse_range(const char* text, double* w /* PPS_GB_COMBOS */);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PPS_GB_H */

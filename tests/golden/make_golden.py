@@ -1,0 +1,208 @@
+"""Generates the golden fixtures in tests/golden/ from the REFERENCE itself.
+
+Run here (where the reference sources are mounted) after building the
+reference tools with ``sh oracle/ref/build_ref.sh``; the fixtures are then
+committed and the tests read only them (the reference does not exist where
+the GPU tests run).
+
+Fixtures:
+  ref_<spot>.npz      every integer artifact of the reference compiler
+                      (cuda/gpu_cfr.cu:1331-1827) for small spots
+  ref_hashes.json     sha256 per artifact for the large spots
+  tiny_check.json     known-answer EVs printed by tools/tiny_check.cpp
+  eval_keys.npz       reference strength keys of seeded 7-card hands
+  bet_actions.json    reference pf::betActions on seeded betting states
+  ranges.json         reference parseRange weights for range strings
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF_BIN = os.path.join(REPO, "oracle", "_ref")
+sys.path.insert(0, os.path.join(REPO, "cuda-poker-solver_gb300"))
+from pps import workloads as wl  # noqa: E402
+
+DT = {"i": np.int32, "q": np.int64, "B": np.uint8, "f": np.float32, "d": np.float64}
+
+
+def read_dump(path):
+    b = open(path, "rb").read()
+    assert b[:8] == b"PPSDUMP1"
+    n = struct.unpack_from("<I", b, 8)[0]
+    o = 12
+    out = {}
+    for _ in range(n):
+        ln = struct.unpack_from("<H", b, o)[0]
+        o += 2
+        name = b[o:o + ln].decode()
+        o += ln
+        t = chr(b[o])
+        o += 1
+        cnt = struct.unpack_from("<Q", b, o)[0]
+        o += 8
+        a = np.frombuffer(b, dtype=DT[t], count=cnt, offset=o).copy()
+        o += a.nbytes
+        out[name] = a
+    return out
+
+
+def range_arg(r, tmp, tag):
+    if isinstance(r, str):
+        return r
+    path = os.path.join(tmp, tag + ".w")
+    np.asarray(r, dtype="<f8").tofile(path)
+    return "@" + path
+
+
+def capture(spot: wl.Spot):
+    assert spot.street_cfgs is None, "the reference has one config for all streets"
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "dump.bin")
+        cmd = [os.path.join(REF_BIN, "ref_capture"), out, spot.board_text(),
+               range_arg(spot.oop, tmp, "oop"), range_arg(spot.ip, tmp, "ip"),
+               str(spot.pot), str(spot.stack), spot.cfg.bet_text(),
+               spot.cfg.raise_text(), str(spot.cfg.max_raises)]
+        subprocess.run(cmd, check=True)
+        return read_dump(out)
+
+
+def edge_spots():
+    s = []
+    api = wl.turn_api()
+    s.append(wl.Spot("turn_short", api.board, api.oop, api.ip, 500, 150,
+                     wl.BetCfg([0.5, 0.75], [2.5, 3.0])))
+    s.append(wl.Spot("flop_short", wl.board_ids("Qs9h2d"), "AA,KK", "QQ,JJ,AKs",
+                     100, 40, wl.BetCfg([0.5], [], max_raises=1)))
+    s.append(wl.Spot("river_geo", wl.board_ids("Qs9h2d7c3h"), "TT+,AKo,KQs",
+                     "99+,AJs+,KQo", 100, 450,
+                     wl.BetCfg([0.33], [2.0], allin=True, geometric=True,
+                               max_raises=2)))
+    s.append(wl.Spot("river_empty", wl.board_ids("AsAhAdKsKh"), "AA", "KK,QQ",
+                     100, 100, wl.BetCfg([0.5], [])))
+    return s
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def run_probe(mode, lines):
+    p = subprocess.run([os.path.join(REF_BIN, "ref_probe"), mode],
+                       input="\n".join(lines) + "\n", capture_output=True,
+                       text=True, check=True)
+    return p.stdout.strip("\n").split("\n")
+
+
+def main():
+    if not os.path.exists(os.path.join(REF_BIN, "ref_capture")):
+        raise SystemExit("build the reference tools first: sh oracle/ref/build_ref.sh")
+    small = [wl.river_c1(), wl.turn_api(), wl.turn_tiny()] + edge_spots()
+    for spot in small:
+        arrs = capture(spot)
+        np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % spot.name), **arrs)
+        print(spot.name, int(arrs["numNodes"][0]), "nodes")
+    hashes = {}
+    flop = wl.Spot("flop_small", wl.board_ids("Qs9h2d"), "AA,KK", "QQ,JJ,AKs",
+                   100, 100, wl.BetCfg([0.5], [], max_raises=1))
+    for spot in [wl.turn_w52(), wl.turn_c3(), wl.turn_c2(uniform_config=True), flop]:
+        arrs = capture(spot)
+        hashes[spot.name] = {k: [sha(v), int(v.size)] for k, v in arrs.items()}
+        print(spot.name, int(arrs["numNodes"][0]), "nodes (hashed)")
+    json.dump(hashes, open(os.path.join(HERE, "ref_hashes.json"), "w"), indent=0)
+
+    tiny = {}
+    out = subprocess.run([os.path.join(REF_BIN, "tiny_check")], capture_output=True,
+                         text=True, check=True).stdout
+    for line in out.splitlines():
+        for tag in ("TINY", "M7", "M9"):
+            if line.startswith(tag + ":"):
+                f = line.split()
+                tiny[tag] = {"ev0": float(f[2]), "ev1": float(f[4])}
+    json.dump(tiny, open(os.path.join(HERE, "tiny_check.json"), "w"), indent=1)
+
+    rng = wl.SplitMix64(7)
+    hands = []
+    for _ in range(20000):
+        cards = []
+        while len(cards) < 7:
+            c = rng.next() % 52
+            if c not in cards:
+                cards.append(c)
+        hands.append(cards)
+    for _ in range(4000):  # a hole card repeating a board card (blocked combos)
+        cards = []
+        while len(cards) < 6:
+            c = rng.next() % 52
+            if c not in cards:
+                cards.append(c)
+        cards.insert(1, cards[2 + rng.next() % 4])
+        hands.append(cards)
+    keys = run_probe("eval", [" ".join(map(str, h)) for h in hands])
+    np.savez_compressed(os.path.join(HERE, "eval_keys.npz"),
+                        hands=np.array(hands, dtype=np.uint8),
+                        keys=np.array([int(k) for k in keys], dtype=np.uint64))
+
+    rng = wl.SplitMix64(11)
+    states = []
+    for _ in range(6000):
+        pot = 1 + rng.next() % 600
+        stack = rng.next() % 2000
+        prev = rng.next() % (stack + 1) if rng.uniform() < 0.6 else 0
+        mine = rng.next() % (prev + 1)
+        actor = rng.next() % 2
+        sc = (mine, prev) if actor == 0 else (prev, mine)
+        if rng.uniform() < 0.5:
+            sc = (sc[1], sc[0]) if rng.uniform() < 0.5 else sc
+        nb = rng.next() % 5
+        bets = sorted({[0.25, 0.33, 0.5, 0.75, 1.0, 1.25, 1.5, 2.0][rng.next() % 8]
+                       for _ in range(nb)})
+        nr = rng.next() % 3
+        raises = sorted({[2.0, 2.5, 3.0, 4.0][rng.next() % 4] for _ in range(nr)})
+        st = {"pot": pot, "stack": stack, "sc0": sc[0], "sc1": sc[1],
+              "actor": actor, "after_allin": int(rng.uniform() < 0.2),
+              "num_bets": rng.next() % 4, "num_streets": 1 + rng.next() % 3,
+              "allin": int(rng.uniform() < 0.5), "geo": int(rng.uniform() < 0.2),
+              "max_raises": rng.next() % 4,
+              "add": [1.5, 0.0, 3.0][rng.next() % 3],
+              "force": [0.15, 0.0, 0.3][rng.next() % 3],
+              "merge": [0.1, 0.0, 0.25][rng.next() % 3],
+              "bets": bets, "raises": raises}
+        states.append(st)
+    lines = []
+    for s in states:
+        lines.append(" ".join(str(x) for x in [
+            s["pot"], s["stack"], s["sc0"], s["sc1"], s["actor"], s["after_allin"],
+            s["num_bets"], s["num_streets"], s["allin"], s["geo"], s["max_raises"],
+            repr(s["add"]), repr(s["force"]), repr(s["merge"]), len(s["bets"]),
+            len(s["raises"])] + [repr(x) for x in s["bets"] + s["raises"]]))
+    outs = run_probe("bet", lines)
+    for s, o in zip(states, outs):
+        f = [int(x) for x in o.split()]
+        s["out"] = [[f[1 + 2 * i], f[2 + 2 * i]] for i in range(f[0])]
+    json.dump(states, open(os.path.join(HERE, "bet_actions.json"), "w"))
+
+    range_strs = ["AA", "AKs", "AKo", "AK", "TT+", "A9s+", "T9s+", "A5s-A2s",
+                  "98s-65s", "55-22", "AA:0.5,KK", "AK,AA", "22+,A9s+,KTs+,QJs,JTs,T9s",
+                  "22+,A9s+,KTs+,QJs,JTs,T9s,AQo+", "TT+,AKo", "AQ+,KQs", "99+",
+                  "KTo-K7o", "KQo-JTo", " QQ , JJ:0.25 ", "AA,AA", "XX", "AKx", "A",
+                  "22-55", "A2s-A5s", "AK-QJ", "AA-KK", "T9o+", "AJo+:0.3"]
+    outs = run_probe("range", range_strs)
+    ranges = {}
+    for s, o in zip(range_strs, outs):
+        ranges[s] = None if o == "ERR" else [float(x) for x in o.split()]
+    json.dump(ranges, open(os.path.join(HERE, "ranges.json"), "w"))
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
