@@ -1,0 +1,69 @@
+// Device engine of one compiled spot: buffers, the per-iteration CUDA
+// graph, and the FP64 value / best-response walks. Host-facing types only
+// (no CUDA headers) so that plain C++ translation units can use it.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "compiler.h"
+#include "layout.h"
+
+namespace pps {
+namespace gb {
+
+class Engine {
+ public:
+  Engine(const Tree& t, HostLayout&& layout);
+  ~Engine();
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+
+  // Zeroes regret and strategy rows and the iteration counter.
+  void zeroRows();
+  // Uploads the discount table (3 floats per iteration index, covering
+  // [0, entries)) and sets the device iteration counter.
+  void setSchedule(const std::vector<float>& coef, int counter);
+  void setCounter(int counter);
+  // Enqueues n iterations (graph replays); returns without waiting.
+  void iterate(int n);
+  void sync();
+  // Runs one FP64 walk (mode 1 = average-strategy EV, 2 = best response)
+  // for traverser tr and waits for it; rows stay readable afterwards.
+  void walk(int tr, int mode);
+  // Rows of the last walk (double): the traverser's value row at `node`
+  // (n_tr entries) and the opponent reach row of layout tr (n_opp entries).
+  std::vector<double> walkCfv(int node, int tr) const;
+  std::vector<double> walkReach(int node, int tr) const;
+  // Regret (which = 0) or strategy (1) rows in the reference's dense
+  // layout (decide nodes in node order, na x n, action-major).
+  std::vector<float> denseRows(int which) const;
+  void setDenseRows(int which, const std::vector<float>& dense);
+  // One decide node's strategy rows (na x n, dense).
+  std::vector<float> nodeRows(int which, int node) const;
+
+  // Selects the iteration graph: 0 = depth-level kernels; 1 = fused
+  // leaf-street kernel where available. Recaptures on change.
+  void setEngineKind(int kind);
+  int engineKind() const { return engineKind_; }
+  int launchesPerIteration() const { return launchesPerIter_; }
+  size_t deviceBytes() const { return deviceBytes_; }
+  // The stream every launch of this engine is issued on.
+  void* stream() const;
+
+  struct Dev;  // device-side state (engine.cu)
+
+ private:
+  const Tree& t_;
+  HostLayout L_;
+  std::unique_ptr<Dev> d_;
+  int engineKind_ = 1;
+  int launchesPerIter_ = 0;
+  size_t deviceBytes_ = 0;
+  void capture();
+  void ensureWalkBuffers();
+};
+
+}  // namespace gb
+}  // namespace pps

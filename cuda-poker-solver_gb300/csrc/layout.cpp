@@ -1,0 +1,235 @@
+// Device layout builder (see layout.h).
+#include "layout.h"
+
+#include <algorithm>
+#include <numeric>
+#include <stdexcept>
+
+#include "pps_gb.h"
+
+namespace pps {
+namespace gb {
+
+namespace {
+
+int appendU16(std::vector<uint16_t>& pool, const std::vector<int>& v) {
+  const int off = (int)pool.size();
+  for (int x : v) pool.push_back((uint16_t)x);
+  return off;
+}
+
+int appendI16(std::vector<int16_t>& pool, const std::vector<int>& v) {
+  const int off = (int)pool.size();
+  for (int x : v) pool.push_back((int16_t)x);
+  return off;
+}
+
+// Slot of base combo `base` in an ascending list, or -1.
+int slotOf(const std::vector<uint16_t>& list, int base) {
+  auto it = std::lower_bound(list.begin(), list.end(), (uint16_t)base);
+  return it != list.end() && *it == base ? (int)(it - list.begin()) : -1;
+}
+
+}  // namespace
+
+HostLayout buildLayout(const Tree& t) {
+  HostLayout L;
+  const int N = (int)t.nodes.size();
+  const int S = (int)t.states.size();
+
+  // ---- board-state tables ----
+  L.states.resize(S);
+  for (int s = 0; s < S; ++s) {
+    const BoardState& st = t.states[s];
+    StateDev& sd = L.states[s];
+    for (int p = 0; p < 2; ++p) {
+      const Side& side = t.side[p];
+      const auto& list = st.list[p];
+      const int n = (int)list.size();
+      sd.n[p] = n;
+      L.maxN = std::max(L.maxN, n);
+      sd.cardsOff[p] = (int)L.poolU8.size();
+      for (uint16_t b : list) {
+        L.poolU8.push_back(side.cards[2 * b]);
+        L.poolU8.push_back(side.cards[2 * b + 1]);
+      }
+      std::vector<int> starts(53, 0), entries;
+      for (int c = 0; c < 52; ++c) {
+        starts[c] = (int)entries.size();
+        for (int j = 0; j < n; ++j)
+          if (side.cards[2 * list[j]] == c || side.cards[2 * list[j] + 1] == c)
+            entries.push_back(j);
+        L.maxCardSeg = std::max(L.maxCardSeg, (int)entries.size() - starts[c]);
+      }
+      starts[52] = (int)entries.size();
+      sd.csrOff[p] = appendU16(L.poolU16, starts);
+      appendU16(L.poolU16, entries);
+      std::vector<int> same(n, -1);
+      for (int j = 0; j < n; ++j) {
+        const int so = side.sameOther[list[j]];
+        if (so >= 0) same[j] = slotOf(st.list[1 - p], so);
+      }
+      sd.sameOff[p] = appendI16(L.poolI16, same);
+      sd.upOff[p] = sd.downOff[p] = -1;
+      if (st.parent >= 0) {
+        const auto& plist = t.states[st.parent].list[p];
+        std::vector<int> up(n), down(plist.size(), -1);
+        size_t i = 0;
+        for (int j = 0; j < n; ++j) {
+          while (plist[i] != list[j]) ++i;
+          up[j] = (int)i;
+          down[i] = j;
+        }
+        sd.upOff[p] = appendU16(L.poolU16, up);
+        sd.downOff[p] = appendI16(L.poolI16, down);
+      }
+      sd.sdOff[p] = sd.sdInfoOff[p] = -1;
+    }
+    if (st.nBoard != 5) continue;
+
+    // River strength tables over this state's own lists.
+    std::vector<uint64_t> keyBase[2] = {strengthKeys(t, 0, st.board),
+                                        strengthKeys(t, 1, st.board)};
+    for (int tr = 0; tr < 2; ++tr) {
+      const int opp = 1 - tr;
+      const auto& ol = st.list[opp];
+      const auto& tl = st.list[tr];
+      const int no = (int)ol.size();
+      std::vector<int> ord(no);
+      std::iota(ord.begin(), ord.end(), 0);
+      std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+        return keyBase[opp][ol[a]] < keyBase[opp][ol[b]];
+      });
+      std::vector<uint64_t> sortedKey(no);
+      for (int k = 0; k < no; ++k) sortedKey[k] = keyBase[opp][ol[ord[k]]];
+      std::vector<int> segStart(53, 0), segPos;
+      std::vector<std::vector<int>> posOfCard(52);
+      for (int k = 0; k < no; ++k) {
+        const int b = ol[ord[k]];
+        posOfCard[t.side[opp].cards[2 * b]].push_back(k);
+        posOfCard[t.side[opp].cards[2 * b + 1]].push_back(k);
+      }
+      for (int c = 0; c < 52; ++c) {
+        segStart[c] = (int)segPos.size();
+        segPos.insert(segPos.end(), posOfCard[c].begin(), posOfCard[c].end());
+      }
+      segStart[52] = (int)segPos.size();
+      sd.sdOff[tr] = appendU16(L.poolU16, ord);
+      appendU16(L.poolU16, segStart);
+      appendU16(L.poolU16, segPos);
+      sd.sdInfoOff[tr] = (int)L.poolSd.size();
+      for (int i = 0; i < (int)tl.size(); ++i) {
+        const int b = tl[i];
+        const uint64_t key = keyBase[tr][b];
+        const int le = (int)(std::lower_bound(sortedKey.begin(), sortedKey.end(), key) -
+                             sortedKey.begin());
+        const int te = (int)(std::upper_bound(sortedKey.begin(), sortedKey.end(), key) -
+                             sortedKey.begin());
+        const int c1 = t.side[tr].cards[2 * b], c2 = t.side[tr].cards[2 * b + 1];
+        auto below = [&](int c, int pos) {
+          const auto& v = posOfCard[c];
+          return (int)(std::lower_bound(v.begin(), v.end(), pos) - v.begin());
+        };
+        const int so = t.side[tr].sameOther[b];
+        const int same = so >= 0 ? slotOf(ol, so) : -1;
+        ShowdownInfo info;
+        info.x = (uint32_t)le | ((uint32_t)te << 16);
+        info.y = (uint32_t)c1 | ((uint32_t)c2 << 8) | ((uint32_t)below(c1, le) << 16) |
+                 ((uint32_t)below(c1, te) << 24);
+        info.z = (uint32_t)below(c2, le) | ((uint32_t)below(c2, te) << 8) |
+                 ((uint32_t)(same + 1) << 16);
+        info.w = 0;
+        L.poolSd.push_back(info);
+      }
+    }
+  }
+  // The showdown kernel scans one card segment per warp, two entries per
+  // lane plus the total slot: at most 63 entries (a card pairs with <= 51).
+  if (L.maxCardSeg > 63)
+    throw Error{PPS_GB_E_ARG, "card segment longer than 63 combos"};
+
+  // ---- nodes, rows, payoffs ----
+  L.nodes.resize(N);
+  L.rows.resize(N);
+  L.termVal.assign((size_t)N * 8, 0.0f);
+  L.children = t.children;
+  uint64_t regQ = 0, cfvQ = 0, reachQ[2] = {0, 0};
+  for (int u = 0; u < N; ++u) {
+    const Node& nd = t.nodes[u];
+    const int n0 = t.n(u, 0), n1 = t.n(u, 1);
+    NodeDev& dv = L.nodes[u];
+    dv.meta = packNode(nd.kind, nd.player, nd.foldBy,
+                       nd.kind == kDecide ? nd.na : nd.kind == kChance ? nd.nChildren : 0);
+    dv.state = nd.state;
+    dv.childBase = nd.childBase;
+    dv.regQ = 0;
+    if (nd.kind == kDecide) {
+      dv.regQ = (uint32_t)regQ;
+      regQ += (uint64_t)nd.na * quads(nd.player == 0 ? n0 : n1);
+    }
+    RowDev& rw = L.rows[u];
+    rw.cfvQ = (uint32_t)cfvQ;
+    cfvQ += quads(std::max(n0, n1));
+    for (int tr = 0; tr < 2; ++tr) {
+      const int par = nd.parent;
+      if (par >= 0 && t.nodes[par].kind == kDecide && t.nodes[par].player == tr) {
+        rw.reachQ[tr] = L.rows[par].reachQ[tr];
+      } else {
+        rw.reachQ[tr] = (uint32_t)reachQ[tr];
+        reachQ[tr] += quads(tr == 0 ? n1 : n0);
+      }
+    }
+    const int nBoard = t.states[nd.state].nBoard;
+    rw.chanceQ = 52 - nBoard - 4;
+    if (regQ > 0xffffffffull || cfvQ > 0xffffffffull || reachQ[0] > 0xffffffffull ||
+        reachQ[1] > 0xffffffffull)
+      throw Error{PPS_GB_E_MEMORY, "tree too large for 32-bit row offsets"};
+    // Terminal payoffs from the root baseline, computed in float exactly as
+    // the reference's terminal kernels do (cuda/gpu_cfr.cu:356-364, 433-439).
+    for (int tr = 0; tr < 2; ++tr) {
+      float* tv = &L.termVal[((size_t)u * 2 + tr) * 4];
+      const int64_t scTr = tr == 0 ? nd.sc0 : nd.sc1;
+      const int64_t pcTr = tr == 0 ? nd.pc0 : nd.pc1;
+      if (nd.kind == kShowdown) {
+        const int64_t diff = nd.sc0 > nd.sc1 ? nd.sc0 - nd.sc1 : nd.sc1 - nd.sc0;
+        const float totalPot = (float)(nd.potBase + nd.sc0 + nd.sc1 - diff);
+        const float mySc = (float)(scTr + pcTr);
+        tv[0] = totalPot - mySc;
+        tv[1] = totalPot * 0.5f - mySc;
+        tv[2] = -mySc;
+      } else if (nd.kind == kFold) {
+        const int fb = nd.foldBy;
+        const int64_t scF = fb == 0 ? nd.sc0 : nd.sc1;
+        const int64_t pcF = fb == 0 ? nd.pc0 : nd.pc1;
+        tv[0] = tr == fb ? -((float)scF + (float)pcF)
+                         : ((float)(nd.potBase + scF) - (float)pcTr);
+      }
+    }
+  }
+  L.regQuads = regQ;
+  L.cfvQuads = cfvQ;
+  L.reachQuads[0] = reachQ[0];
+  L.reachQuads[1] = reachQ[1];
+
+  // ---- work lists ----
+  const int D = t.maxDepth + 1;
+  for (int tr = 0; tr < 2; ++tr) {
+    L.fwdDecide[tr].assign(D, {});
+    L.fwdChance[tr].assign(D, {});
+  }
+  L.bwd.assign(D, {});
+  for (int u = 0; u < N; ++u) {
+    const Node& nd = t.nodes[u];
+    L.bwd[nd.depth].push_back(u);
+    for (int tr = 0; tr < 2; ++tr) {
+      if (nd.kind == kDecide && nd.player != tr) L.fwdDecide[tr][nd.depth].push_back(u);
+      if (nd.kind == kChance)
+        for (int br = 0; br < nd.nChildren; ++br)
+          L.fwdChance[tr][nd.depth].push_back(u * 64 + br);
+    }
+  }
+  return L;
+}
+
+}  // namespace gb
+}  // namespace pps

@@ -1,0 +1,105 @@
+// Device data layout of one compiled spot (built on the host, uploaded by
+// the engine).
+//
+// Rows. Every per-combo row (regret, strategy, reach, counterfactual value)
+// starts on a 16-byte boundary and is padded to a multiple of 4 entries,
+// so kernels move whole float4 (double2x2) quads; offsets are stored in
+// quad units. Regret and strategy rows of a decide node are na rows of
+// pad4(n_actor) entries, action-major (the reference's [a][c] order,
+// cuda/gpu_cfr.cu:1476-1481, plus padding). Reach rows exist per traverser
+// layout and alias the parent's row under the traverser's own decide nodes
+// (the reference's pass-through aliasing, cuda/gpu_cfr.cu:1491-1514).
+//
+// Board states. Combo lists and every table derived from them (cards per
+// list slot, card->slot lists, identical-combo maps, chance slot maps and
+// the river strength tables) exist once per BoardState, not per node.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "compiler.h"
+
+namespace pps {
+namespace gb {
+
+// Half-step modes: a DCFR iteration, an average-strategy value walk, a
+// best-response walk.
+enum WalkMode : int { kModeCFR = 0, kModeEV = 1, kModeBR = 2 };
+
+// Packed node word: kind (bits 0-1), player (bit 2), foldBy (bit 3),
+// na or branch count (bits 8-15).
+inline int packNode(int kind, int player, int foldBy, int na) {
+  return kind | (player << 2) | (foldBy << 3) | (na << 8);
+}
+
+struct alignas(16) NodeDev {
+  int meta;         // packNode(...)
+  int state;        // BoardState index
+  int childBase;    // into children[]
+  uint32_t regQ;    // decide: regret/strategy row start (quads)
+};
+
+struct alignas(16) RowDev {
+  uint32_t reachQ[2];  // reach row start per traverser layout (quads)
+  uint32_t cfvQ;       // counterfactual-value row start (quads)
+  int chanceQ;         // 52 - nBoard - 4: pair-conditional deal count
+};
+
+// Per board state, per side p (0/1); offsets index the pools below, -1 if
+// the table does not exist for this state.
+struct alignas(16) StateDev {
+  int n[2];         // list sizes
+  int cardsOff[2];  // u8 pool: 2 cards per list slot
+  int csrOff[2];    // u16 pool: 53 segment starts, then the slots holding
+                    // each card (card-major, ascending)
+  int sameOff[2];   // i16 pool: slot of the identical combo in the other
+                    // side's list, or -1
+  int upOff[2];     // u16 pool: child slot -> parent slot (dealt states)
+  int downOff[2];   // i16 pool: parent slot -> child slot or -1
+  int sdOff[2];     // river states, per traverser tr: u16 pool holding
+                    // ord[n_opp] (opponent slots, weakest first), 53
+                    // card-segment starts, then per card the sorted
+                    // positions of opponent combos holding it
+  int sdInfoOff[2]; // river states, per traverser: u32x4 pool, one entry
+                    // per traverser slot (see showdownInfo)
+};
+
+// Showdown entry of one traverser combo: x = le | te << 16 (opponents
+// strictly weaker / weaker-or-equal, in sorted positions); y = c1 | c2 <<
+// 8 | k1le << 16 | k1te << 24 and z = k2le | k2te << 8 | (same+1) << 16,
+// where kXle / kXte count card cX's segment entries below le / te and
+// `same` is the opponent slot of the identical combo (-1: none).
+struct alignas(16) ShowdownInfo {
+  uint32_t x, y, z, w;
+};
+
+struct HostLayout {
+  std::vector<NodeDev> nodes;
+  std::vector<RowDev> rows;
+  std::vector<float> termVal;  // 4 per (node, traverser): showdown
+                               // (win, tie, lose, 0); fold (v, 0, 0, 0)
+  std::vector<int> children;
+  std::vector<StateDev> states;
+  std::vector<uint8_t> poolU8;
+  std::vector<uint16_t> poolU16;
+  std::vector<int16_t> poolI16;
+  std::vector<ShowdownInfo> poolSd;
+  uint64_t regQuads = 0;          // regret (= strategy) pool size
+  uint64_t cfvQuads = 0;
+  uint64_t reachQuads[2] = {0, 0};
+  // Work lists per depth d. fwdDecide[tr][d]: the opponent's decide nodes
+  // (node ids); fwdChance[tr][d]: one item per chance branch, stored as
+  // node * 64 + branch; bwd[d]: every node at depth d.
+  std::vector<std::vector<int>> fwdDecide[2], fwdChance[2];
+  std::vector<std::vector<int>> bwd;
+  int maxN = 0;        // largest list size (either side)
+  int maxCardSeg = 0;  // longest card segment of any list
+};
+
+HostLayout buildLayout(const Tree& t);
+
+inline uint32_t quads(int n) { return (uint32_t)((n + 3) / 4); }
+
+}  // namespace gb
+}  // namespace pps

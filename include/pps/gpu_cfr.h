@@ -149,7 +149,7 @@ class GpuPostflopSolver {
   void debugDump();
 
   // The C-ABI handle (pps_gb_solver*) this object wraps.
-  void* handle() const { return impl_; }
+  void* handle() const;
 
  private:
   struct Impl;
