@@ -1,0 +1,287 @@
+"""Benchmark: DCFR iterations per second on the 48,255-node turn tree.
+
+Workload (turn_c3, BASELINE configs[2]): seeded 4-card board, 60% of combos
+at weight U(0.5,1) and the rest U(0,0.2) (all 1128 combos per side), pot
+100, stack 400, bets {25, 50, 100, 150}% + all-in on both streets, raises
+2x, max 4 bets per street. A step is one DCFR iteration (both alternating
+half-steps) over the whole tree; the data is synthetic (splitmix64, see
+pps/workloads.py).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line (rank 0). ``value`` is device-timed (CUDA events on the
+solver's stream, tree resident in HBM); ``e2e`` is the same metric through
+the C ABI from host buffers (compile + upload + K iterations + FP64 stats
+readback); ``roofline`` covers the dominant kernel class from a launch-by-
+launch CUDA-event profile pass; ``cpu_baseline`` times the CPU oracle
+(restatement of the reference iteration) on this host's cores.
+N > 1: replicas only (one spot per GPU, no collective in the data path);
+``value`` sums the ranks' iterations over the max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "cuda-poker-solver_gb300")
+for p in (REPO, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "DCFR iters/s (52k-node turn)"
+WORKLOAD = "turn_c3"
+
+
+def workload_config(spot, n_nodes):
+    return {"workload": "turn_c3: %d-node turn tree (BASELINE configs[2])" % n_nodes,
+            "board": spot.board_text(), "ranges": "all 1128 combos, 60% U(0.5,1) / 40% U(0,0.2)",
+            "pot": spot.pot, "stack": spot.stack, "bets": "0.25,0.5,1,1.5,a", "raises": "2",
+            "max_bets_per_street": 4, "iterations_e2e": 1000,
+            "l2": "inputs larger than L2 (row working set > 129 MB); no flush needed",
+            "parallelism": "replicas"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic(kernel):
+    """Per-launch DRAM bytes of the kernel from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "traffic.json")
+    try:
+        d = json.load(open(path))
+        return d.get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(spot, seconds=12.0):
+    """The CPU oracle (f32, all host threads) on a bounded sample: one
+    warm-up iteration, then iterations until ~`seconds` have passed."""
+    from oracle.cpu_oracle import oracle_for
+    threads = os.cpu_count() or 1
+    o = oracle_for(spot, threads)
+    o.iterate(1)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        o.iterate(1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 50:
+            break
+    return {"value": n / el, "unit": "iters/s", "cores": threads, "kind": "port",
+            "sample": "%d DCFR iterations of turn_c3 (after 1 warm-up), CPU oracle f32 "
+                      "restatement of the reference iteration, OpenMP over chance branches"
+                      % n}
+
+
+def run_reference(args, rank):
+    """--impl reference: the CPU restatement of the reference iteration (the
+    reference's own CPU path does not exist: its CPU river solver was
+    removed, and its GPU engine cannot be built on this machine)."""
+    if rank != 0:
+        return
+    from pps import workloads as wl
+    from oracle.cpu_oracle import oracle_for
+    spot = wl.turn_c3()
+    threads = os.cpu_count() or 1
+    o = oracle_for(spot, threads)
+    for _ in range(max(1, min(args.warmup, 2))):
+        o.iterate(1)
+    steps = max(1, args.steps)
+    budget = 150.0
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        o.iterate(1)
+        done += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    v = done / el
+    line = {"metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": args.gpus,
+            "steps": done, "warmup": args.warmup, "ms_per_step": 1000.0 * el / done,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(spot, o.num_nodes),
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
+                             "sample": "%d of %d requested steps within %.0f s (bounded); "
+                                       "CPU oracle restatement of cuda/gpu_cfr.cu's iteration"
+                                       % (done, steps, budget)},
+            "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo" if args.impl == "reference" else "nccl")
+    if args.impl == "reference":
+        run_reference(args, rank)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    import pps
+    from pps import workloads as wl
+
+    spot = wl.turn_c3()
+
+    def make():
+        return pps.Solver(board=spot.board_text(), oop=spot.oop, ip=spot.ip, pot=spot.pot,
+                          stack=spot.stack, bets=spot.cfg.bet_text(), raises=spot.cfg.raise_text(),
+                          max_raises=spot.cfg.max_raises)
+
+    # e2e through the public API from host buffers: compile + upload, the
+    # configured 1000 iterations, FP64 stats back to the host.
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s = make()
+    s.solve(1000)
+    st = s.stats()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    info = s.info()
+    e2e = {"value": 1000.0 / e2e_s, "unit": "iters/s",
+           "h2d_bytes_per_step": int(info.h2d_bytes) // 1000,
+           "d2h_bytes_per_step": int(info.d2h_bytes) // 1000,
+           "includes": "compile + upload + 1000 iterations + FP64 stats walks",
+           "stats": {"ev_oop": st["ev_oop"], "ev_ip": st["ev_ip"],
+                     "exploitability": st["exploitability"]}}
+
+    # Device-timed region: K graph replays, CUDA events on the solver stream.
+    s.time_iterations(args.warmup)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = s.time_iterations(args.steps)
+    torch.cuda.synchronize()
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * args.steps / (ms / 1000.0)
+
+    # Dominant kernel class: launch-by-launch CUDA-event profile.
+    prof = s.profile(min(args.steps, 20))
+    name, (launches, pms, pbytes) = max(prof.items(), key=lambda kv: kv[1][1])
+    peak, peak_kind = measured_peaks()
+    achieved = (pbytes / launches) / (pms / launches / 1000.0) / 1e9
+    traffic = committed_traffic(name)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "kernel": name,
+                "algo_bytes_per_launch": pbytes / launches,
+                "avg_launch_us": 1000.0 * pms / launches, "peak_source": peak_kind,
+                "iteration_gbs": (sum(v[2] for v in prof.values()) / min(args.steps, 20)) *
+                                 (value / world) / 1e9,
+                "profile": {k: {"launches": v[0], "ms": v[1], "algo_bytes": v[2]}
+                            for k, v in prof.items()}}
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    line = {"metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(spot, info.num_nodes),
+            "e2e": e2e, "roofline": roofline, "clocks": clk.summary(),
+            "gpu_launches": int(info.launches_per_iteration) * args.steps,
+            "engine": "fused leaf-street" if info.engine == 1 else "depth-level"}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(spot)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

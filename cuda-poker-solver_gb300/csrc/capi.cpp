@@ -197,6 +197,9 @@ int pps_gb_get_info(pps_gb_solver* h, pps_gb_info* out) {
     if (s.engine()) {
       out->launches_per_iteration = s.engine()->launchesPerIteration();
       out->device_bytes = (int64_t)s.engine()->deviceBytes();
+      out->h2d_bytes = s.engine()->h2dBytes();
+      out->d2h_bytes = s.engine()->d2hBytes();
+      out->engine = s.engine()->engineKind();
     }
   });
 }
@@ -394,6 +397,28 @@ int pps_gb_set_engine(pps_gb_solver* h, int engine) {
   return guarded([&] {
     SolverCore& s = core(h);
     if (s.engine()) s.engine()->setEngineKind(engine);
+  });
+}
+
+int pps_gb_time_iterations(pps_gb_solver* h, int n, double* ms) {
+  return guarded([&] {
+    if (!ms || n < 0) throw Error{PPS_GB_E_ARG, "bad arguments"};
+    *ms = core(h).timeIterations(n);
+  });
+}
+
+int pps_gb_profile(pps_gb_solver* h, int n, pps_gb_kernel_stat* out, int cap, int* n_out) {
+  return guarded([&] {
+    if (!out || !n_out || n < 1) throw Error{PPS_GB_E_ARG, "bad arguments"};
+    const auto stats = core(h).profile(n);
+    *n_out = std::min<int>((int)stats.size(), cap);
+    for (int i = 0; i < *n_out; ++i) {
+      std::memset(out[i].name, 0, sizeof(out[i].name));
+      std::strncpy(out[i].name, stats[i].name.c_str(), sizeof(out[i].name) - 1);
+      out[i].launches = stats[i].launches;
+      out[i].ms = stats[i].ms;
+      out[i].algo_bytes = stats[i].bytes;
+    }
   });
 }
 

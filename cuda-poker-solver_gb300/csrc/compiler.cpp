@@ -371,6 +371,9 @@ void exportReference(const Tree& t, const ArraySink& sink) {
   scalar("maxNa", t.maxNa);
   scalar("regTotal", t.rowTotal);
   if (t.empty) {
+    scalar("reachTotal", 0);
+    scalar("reachTotal0", 0);
+    scalar("reachTotal1", 0);
     scalar("empty", 1);
     return;
   }

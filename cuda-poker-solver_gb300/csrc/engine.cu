@@ -2,6 +2,10 @@
 // iteration (two alternating half-steps plus the counter bump, the
 // reference's captureGraph, cuda/gpu_cfr.cu:844-868) as a CUDA graph, and
 // runs the FP64 walks.
+//
+// An iteration is described once as a launch plan (kernel, list, traverser,
+// algorithmic bytes); graph capture, the profile pass and the walks all
+// replay a plan.
 #include "engine.h"
 
 #include <cuda_runtime.h>
@@ -30,22 +34,22 @@ namespace gb {
 namespace {
 
 template <typename V>
-V* upload(const std::vector<V>& v, size_t& bytes) {
-  if (v.empty()) return nullptr;
-  V* p = nullptr;
-  GB_CK(cudaMalloc(&p, v.size() * sizeof(V)));
-  GB_CK(cudaMemcpy(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice));
-  bytes += v.size() * sizeof(V);
-  return p;
-}
-
-template <typename V>
 V* alloc(size_t count, size_t& bytes) {
   V* p = nullptr;
   GB_CK(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(V)));
   bytes += std::max<size_t>(count, 1) * sizeof(V);
   return p;
 }
+
+enum LaunchKind { kFwdDecide, kFwdChance, kBwd, kLeafSweep, kCounter };
+const char* kLaunchName[] = {"fwd_decide", "fwd_chance", "bwd_level", "leaf_street", "counter"};
+
+struct Launch {
+  LaunchKind kind;
+  int tr;
+  ListRef list;
+  double bytes;  // algorithmic bytes of this launch (f32 rows)
+};
 
 }  // namespace
 
@@ -59,11 +63,14 @@ struct Engine::Dev {
   DevRows<double> rowsD{};
   float* coef = nullptr;
   size_t coefCap = 0;  // iterations the coef table holds
+  int coefValid = 0;   // leading entries uploaded
   int* counter = nullptr;
   int* lists = nullptr;
   std::vector<ListRef> fwdDecide[2], fwdChance[2], bwd;
-  LeafPlan leaf;       // fused leaf-street plan (empty if not applicable)
+  LeafPlan leaf;       // fused leaf-street plan (ok = false if not applicable)
+  std::vector<Launch> plan[2];  // per engine kind: one iteration
   bool walkReady = false;
+  size_t smemF = 0, smemD = 0;
 
   template <typename P>
   P* own(P* p) {
@@ -72,20 +79,61 @@ struct Engine::Dev {
   }
 };
 
+namespace {
+
+template <typename V>
+V* upload(Engine::Dev& d, const std::vector<V>& v, size_t& bytes, int64_t& h2d) {
+  if (v.empty()) return nullptr;
+  V* p = nullptr;
+  GB_CK(cudaMalloc(&p, v.size() * sizeof(V)));
+  GB_CK(cudaMemcpy(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice));
+  bytes += v.size() * sizeof(V);
+  h2d += (int64_t)(v.size() * sizeof(V));
+  return d.own(p);
+}
+
+unsigned gridOf(int count) { return (unsigned)std::min(count, 65535); }
+
+// Issues one planned launch on the engine stream (CFR mode, f32 rows).
+void issue(Engine::Dev& d, const Launch& l) {
+  switch (l.kind) {
+    case kFwdDecide:
+      fwdDecideK<float><<<gridOf(l.list.count), kThreads, 0, d.stream>>>(
+          d.tree, d.rowsF, d.lists + l.list.off, l.list.count, l.tr, 0);
+      break;
+    case kFwdChance:
+      fwdChanceK<float><<<gridOf(l.list.count), kThreads, 0, d.stream>>>(
+          d.tree, d.rowsF, d.lists + l.list.off, l.list.count, l.tr);
+      break;
+    case kBwd:
+      bwdK<float><<<gridOf(l.list.count), kThreads, d.smemF, d.stream>>>(
+          d.tree, d.rowsF, d.lists + l.list.off, l.list.count, l.tr, kModeCFR);
+      break;
+    case kLeafSweep:
+      launchLeaf(d.leaf, d.tree, d.rowsF, l.tr, d.stream);
+      break;
+    case kCounter:
+      advanceCounterK<<<1, 32, 0, d.stream>>>(d.counter);
+      break;
+  }
+}
+
+}  // namespace
+
 Engine::Engine(const Tree& t, HostLayout&& layout)
     : t_(t), L_(std::move(layout)), d_(new Dev()) {
   Dev& d = *d_;
   size_t& B = deviceBytes_;
   GB_CK(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
-  d.tree.nodes = d.own(upload(L_.nodes, B));
-  d.tree.rows = d.own(upload(L_.rows, B));
-  d.tree.termVal = d.own(upload(L_.termVal, B));
-  d.tree.children = d.own(upload(L_.children, B));
-  d.tree.states = d.own(upload(L_.states, B));
-  d.tree.poolU8 = d.own(upload(L_.poolU8, B));
-  d.tree.poolU16 = d.own(upload(L_.poolU16, B));
-  d.tree.poolI16 = d.own(upload(L_.poolI16, B));
-  d.tree.poolSd = d.own(upload(L_.poolSd, B));
+  d.tree.nodes = upload(d, L_.nodes, B, h2d_);
+  d.tree.rows = upload(d, L_.rows, B, h2d_);
+  d.tree.termVal = upload(d, L_.termVal, B, h2d_);
+  d.tree.children = upload(d, L_.children, B, h2d_);
+  d.tree.states = upload(d, L_.states, B, h2d_);
+  d.tree.poolU8 = upload(d, L_.poolU8, B, h2d_);
+  d.tree.poolU16 = upload(d, L_.poolU16, B, h2d_);
+  d.tree.poolI16 = upload(d, L_.poolI16, B, h2d_);
+  d.tree.poolSd = upload(d, L_.poolSd, B, h2d_);
   d.tree.regret = d.own(alloc<float>(L_.regQuads * 4, B));
   d.tree.strat = d.own(alloc<float>(L_.regQuads * 4, B));
   d.rowsF.cfv = d.own(alloc<float>(L_.cfvQuads * 4, B));
@@ -104,6 +152,7 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
     for (int j = 0; j < opp.n; ++j) row[j] = (float)opp.w[j];
     GB_CK(cudaMemcpy(d.rowsF.reach[tr], row.data(), row.size() * sizeof(float),
                      cudaMemcpyHostToDevice));
+    h2d_ += (int64_t)(row.size() * sizeof(float));
   }
 
   // Work lists, concatenated.
@@ -121,16 +170,17 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
     }
   for (int dd = 0; dd < D; ++dd) d.bwd.push_back(addList(L_.bwd[dd]));
   d.leaf = planLeaf(t_, L_, all);
-  d.lists = d.own(upload(all, B));
-  if (d.leaf.ok) d.leaf.scratch = d.own(alloc<float>(d.leaf.scratchFloats, B));
+  d.lists = upload(d, all, B, h2d_);
+  if (d.leaf.ok) finishLeaf(d.leaf, d.lists, [&](size_t n) { return d.own(alloc<float>(n, B)); });
 
+  d.smemF = bwdSmemBytes<float>(L_.maxN);
+  d.smemD = bwdSmemBytes<double>(L_.maxN);
   GB_CK(cudaFuncSetAttribute(bwdK<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)bwdSmemBytes<float>(L_.maxN)));
+                             (int)d.smemF));
   GB_CK(cudaFuncSetAttribute(bwdK<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)bwdSmemBytes<double>(L_.maxN)));
-  if (d.leaf.ok)
-    GB_CK(cudaFuncSetAttribute(leafK, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)d.leaf.smemBytes));
+                             (int)d.smemD));
+  if (d.leaf.ok) GB_CK(prepareLeaf(d.leaf));
+  buildPlans();
   engineKind_ = d.leaf.ok ? 1 : 0;
   zeroRows();
 }
@@ -145,6 +195,69 @@ Engine::~Engine() {
 }
 
 void* Engine::stream() const { return (void*)d_->stream; }
+
+// Algorithmic f32 row bytes of each launch: every row a launch must read or
+// write once (index tables excluded).
+void Engine::buildPlans() {
+  Dev& d = *d_;
+  const Tree& t = t_;
+  auto n = [&](int u, int p) { return (double)t.n(u, p); };
+  auto fwdDecideBytes = [&](const std::vector<int>& v, int tr) {
+    double b = 0;
+    for (int u : v) b += 4 * n(u, 1 - tr) * (1 + 2.0 * t.nodes[u].na);
+    return b;
+  };
+  auto fwdChanceBytes = [&](const std::vector<int>& v, int tr) {
+    double b = 0;
+    for (int item : v) {
+      const int u = item >> 6, br = item & 63;
+      const int ch = t.children[t.nodes[u].childBase + br];
+      b += 4 * n(ch, 1 - tr) + 4 * n(u, 1 - tr) / t.nodes[u].nChildren;
+    }
+    return b;
+  };
+  auto bwdNodeBytes = [&](int u, int tr) {
+    const Node& nd = t.nodes[u];
+    switch (nd.kind) {
+      case kDecide:
+        return nd.player == tr ? 4 * n(u, tr) * (5.0 * nd.na + 1) : 4 * n(u, tr) * (nd.na + 1.0);
+      case kChance: {
+        double b = 4 * n(u, tr);
+        for (int k = 0; k < nd.nChildren; ++k) b += 4 * n(t.children[nd.childBase + k], tr);
+        return b;
+      }
+      default:
+        return 4 * (n(u, 1 - tr) + n(u, tr));
+    }
+  };
+  const int D = (int)L_.bwd.size();
+  for (int kind = 0; kind < 2; ++kind) {
+    std::vector<Launch>& P = d.plan[kind];
+    P.clear();
+    const bool leaf = kind == 1 && d.leaf.ok;
+    for (int tr = 0; tr < 2; ++tr) {
+      const int fwdEnd = leaf ? d.leaf.upperDepth : D;
+      for (int dd = 0; dd < fwdEnd; ++dd) {
+        if (d.fwdDecide[tr][dd].count)
+          P.push_back({kFwdDecide, tr, d.fwdDecide[tr][dd],
+                       fwdDecideBytes(L_.fwdDecide[tr][dd], tr)});
+        if (d.fwdChance[tr][dd].count)
+          P.push_back({kFwdChance, tr, d.fwdChance[tr][dd],
+                       fwdChanceBytes(L_.fwdChance[tr][dd], tr)});
+      }
+      if (leaf) P.push_back({kLeafSweep, tr, ListRef{}, d.leaf.algoBytes[tr]});
+      for (int dd = (leaf ? d.leaf.upperDepth : D) - 1; dd >= 0; --dd) {
+        const ListRef b = leaf ? d.leaf.upperBwd[dd] : d.bwd[dd];
+        const std::vector<int>& nodes = leaf ? d.leaf.upperBwdNodes[dd] : L_.bwd[dd];
+        if (!b.count) continue;
+        double bytes = 0;
+        for (int u : nodes) bytes += bwdNodeBytes(u, tr);
+        P.push_back({kBwd, tr, b, bytes});
+      }
+    }
+    P.push_back({kCounter, 0, ListRef{}, 0.0});
+  }
+}
 
 void Engine::zeroRows() {
   Dev& d = *d_;
@@ -178,6 +291,8 @@ void Engine::setSchedule(const std::vector<float>& coef, int counter) {
   }
   GB_CK(cudaMemcpyAsync(d.coef, coef.data(), coef.size() * sizeof(float),
                         cudaMemcpyHostToDevice, d.stream));
+  h2d_ += (int64_t)(coef.size() * sizeof(float));
+  d.coefValid = (int)entries;
   setCounter(counter);
 }
 
@@ -188,70 +303,6 @@ void Engine::setCounter(int counter) {
   GB_CK(cudaStreamSynchronize(d.stream));
 }
 
-namespace {
-
-template <typename T>
-int halfStep(Engine::Dev& d, const DevRows<T>& rows, int D, int tr, int mode,
-             int sigSrc, size_t smem) {
-  int launches = 0;
-  auto grid = [](int count) { return (unsigned)std::min(count, 65535); };
-  for (int dd = 0; dd < D; ++dd) {
-    const ListRef a = d.fwdDecide[tr][dd], c = d.fwdChance[tr][dd];
-    if (a.count) {
-      fwdDecideK<T><<<grid(a.count), kThreads, 0, d.stream>>>(
-          d.tree, rows, d.lists + a.off, a.count, tr, sigSrc);
-      ++launches;
-    }
-    if (c.count) {
-      fwdChanceK<T><<<grid(c.count), kThreads, 0, d.stream>>>(
-          d.tree, rows, d.lists + c.off, c.count, tr);
-      ++launches;
-    }
-  }
-  for (int dd = D - 1; dd >= 0; --dd) {
-    const ListRef b = d.bwd[dd];
-    if (!b.count) continue;
-    bwdK<T><<<grid(b.count), kThreads, smem, d.stream>>>(d.tree, rows, d.lists + b.off,
-                                                          b.count, tr, mode);
-    ++launches;
-  }
-  GB_CK(cudaGetLastError());
-  return launches;
-}
-
-}  // namespace
-
-// Fused variant of one half-step: depth-level launches above the leaf
-// street, one persistent launch for every leaf subtree, depth-level below.
-static int halfStepLeaf(Engine::Dev& d, int D, int tr, size_t smem) {
-  int launches = 0;
-  auto grid = [](int count) { return (unsigned)std::min(count, 65535); };
-  const LeafPlan& lp = d.leaf;
-  for (int dd = 0; dd < lp.rootDepthMin; ++dd) {
-    const ListRef a = d.fwdDecide[tr][dd], c = d.fwdChance[tr][dd];
-    if (a.count) {
-      fwdDecideK<float><<<grid(a.count), kThreads, 0, d.stream>>>(
-          d.tree, d.rowsF, d.lists + a.off, a.count, tr, 0);
-      ++launches;
-    }
-    if (c.count) {
-      fwdChanceK<float><<<grid(c.count), kThreads, 0, d.stream>>>(
-          d.tree, d.rowsF, d.lists + c.off, c.count, tr);
-      ++launches;
-    }
-  }
-  launches += launchLeaf(lp, d.tree, d.rowsF, d.lists, tr, d.stream);
-  for (int dd = lp.rootDepthMin - 1; dd >= 0; --dd) {
-    const ListRef b = lp.upperBwd[dd];
-    if (!b.count) continue;
-    bwdK<float><<<grid(b.count), kThreads, smem, d.stream>>>(
-        d.tree, d.rowsF, d.lists + b.off, b.count, tr, kModeCFR);
-    ++launches;
-  }
-  GB_CK(cudaGetLastError());
-  return launches;
-}
-
 void Engine::capture() {
   Dev& d = *d_;
   if (d.exec) {
@@ -260,26 +311,23 @@ void Engine::capture() {
     d.exec = nullptr;
     d.graph = nullptr;
   }
-  const int D = (int)L_.bwd.size();
-  const size_t smem = bwdSmemBytes<float>(L_.maxN);
+  const std::vector<Launch>& P = d.plan[engineKind_];
   GB_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
-  int launches = 0;
-  try {
-    for (int tr = 0; tr < 2; ++tr)
-      launches += engineKind_ == 1 && d.leaf.ok
-                      ? halfStepLeaf(d, D, tr, smem)
-                      : halfStep<float>(d, d.rowsF, D, tr, kModeCFR, 0, smem);
-    advanceCounterK<<<1, 32, 0, d.stream>>>(d.counter);
-    ++launches;
-  } catch (...) {
-    cudaGraph_t g = nullptr;
-    cudaStreamEndCapture(d.stream, &g);
-    if (g) cudaGraphDestroy(g);
-    throw;
+  cudaError_t launchErr = cudaSuccess;
+  for (const Launch& l : P) {
+    issue(d, l);
+    if (launchErr == cudaSuccess) launchErr = cudaGetLastError();
   }
-  GB_CK(cudaStreamEndCapture(d.stream, &d.graph));
+  cudaGraph_t g = nullptr;
+  const cudaError_t endErr = cudaStreamEndCapture(d.stream, &g);
+  if (launchErr != cudaSuccess || endErr != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    GB_CK(launchErr);
+    GB_CK(endErr);
+  }
+  d.graph = g;
   GB_CK(cudaGraphInstantiate(&d.exec, d.graph, 0));
-  launchesPerIter_ = launches;
+  launchesPerIter_ = (int)P.size();
 }
 
 void Engine::setEngineKind(int kind) {
@@ -297,6 +345,57 @@ void Engine::iterate(int n) {
 
 void Engine::sync() { GB_CK(cudaStreamSynchronize(d_->stream)); }
 
+double Engine::timeIterations(int n) {
+  Dev& d = *d_;
+  if (!d.exec) capture();
+  cudaEvent_t a, b;
+  GB_CK(cudaEventCreate(&a));
+  GB_CK(cudaEventCreate(&b));
+  GB_CK(cudaEventRecord(a, d.stream));
+  iterate(n);
+  GB_CK(cudaEventRecord(b, d.stream));
+  GB_CK(cudaEventSynchronize(b));
+  float ms = 0.0f;
+  GB_CK(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms;
+}
+
+std::vector<Engine::KernelStat> Engine::profile(int n) {
+  Dev& d = *d_;
+  const std::vector<Launch>& P = d.plan[engineKind_];
+  std::vector<cudaEvent_t> ev(2 * P.size() * (size_t)n);
+  for (auto& e : ev) GB_CK(cudaEventCreate(&e));
+  size_t k = 0;
+  for (int it = 0; it < n; ++it)
+    for (const Launch& l : P) {
+      GB_CK(cudaEventRecord(ev[k++], d.stream));
+      issue(d, l);
+      GB_CK(cudaGetLastError());
+      GB_CK(cudaEventRecord(ev[k++], d.stream));
+    }
+  GB_CK(cudaStreamSynchronize(d.stream));
+  std::vector<KernelStat> out(5);
+  for (int c = 0; c < 5; ++c) out[c].name = kLaunchName[c];
+  k = 0;
+  for (int it = 0; it < n; ++it)
+    for (const Launch& l : P) {
+      float ms = 0.0f;
+      GB_CK(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+      k += 2;
+      KernelStat& s = out[l.kind];
+      s.launches += 1;
+      s.ms += ms;
+      s.bytes += l.bytes;
+    }
+  for (auto& e : ev) cudaEventDestroy(e);
+  out.erase(std::remove_if(out.begin(), out.end(),
+                           [](const KernelStat& s) { return s.launches == 0; }),
+            out.end());
+  return out;
+}
+
 void Engine::ensureWalkBuffers() {
   Dev& d = *d_;
   if (d.walkReady) return;
@@ -309,6 +408,7 @@ void Engine::ensureWalkBuffers() {
     for (int j = 0; j < opp.n; ++j) row[j] = opp.w[j];
     GB_CK(cudaMemcpy(d.rowsD.reach[tr], row.data(), row.size() * sizeof(double),
                      cudaMemcpyHostToDevice));
+    h2d_ += (int64_t)(row.size() * sizeof(double));
   }
   d.walkReady = true;
 }
@@ -316,8 +416,23 @@ void Engine::ensureWalkBuffers() {
 void Engine::walk(int tr, int mode) {
   Dev& d = *d_;
   ensureWalkBuffers();
-  halfStep<double>(d, d.rowsD, (int)L_.bwd.size(), tr, mode, 1,
-                   bwdSmemBytes<double>(L_.maxN));
+  const int D = (int)L_.bwd.size();
+  for (int dd = 0; dd < D; ++dd) {
+    const ListRef a = d.fwdDecide[tr][dd], c = d.fwdChance[tr][dd];
+    if (a.count)
+      fwdDecideK<double><<<gridOf(a.count), kThreads, 0, d.stream>>>(
+          d.tree, d.rowsD, d.lists + a.off, a.count, tr, 1);
+    if (c.count)
+      fwdChanceK<double><<<gridOf(c.count), kThreads, 0, d.stream>>>(
+          d.tree, d.rowsD, d.lists + c.off, c.count, tr);
+  }
+  for (int dd = D - 1; dd >= 0; --dd) {
+    const ListRef b = d.bwd[dd];
+    if (b.count)
+      bwdK<double><<<gridOf(b.count), kThreads, d.smemD, d.stream>>>(
+          d.tree, d.rowsD, d.lists + b.off, b.count, tr, mode);
+  }
+  GB_CK(cudaGetLastError());
   GB_CK(cudaStreamSynchronize(d.stream));
 }
 
@@ -327,6 +442,7 @@ std::vector<double> Engine::walkCfv(int node, int tr) const {
   if (n)
     GB_CK(cudaMemcpy(out.data(), d_->rowsD.cfv + (size_t)L_.rows[node].cfvQ * 4,
                      n * sizeof(double), cudaMemcpyDeviceToHost));
+  d2h_ += (int64_t)n * 8;
   return out;
 }
 
@@ -336,6 +452,7 @@ std::vector<double> Engine::walkReach(int node, int tr) const {
   if (n)
     GB_CK(cudaMemcpy(out.data(), d_->rowsD.reach[tr] + (size_t)L_.rows[node].reachQ[tr] * 4,
                      n * sizeof(double), cudaMemcpyDeviceToHost));
+  d2h_ += (int64_t)n * 8;
   return out;
 }
 
@@ -345,6 +462,7 @@ std::vector<float> Engine::denseRows(int which) const {
   if (!padded.empty())
     GB_CK(cudaMemcpy(padded.data(), which == 0 ? d_->tree.regret : d_->tree.strat,
                      padded.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  d2h_ += (int64_t)(padded.size() * sizeof(float));
   std::vector<float> dense;
   dense.reserve((size_t)t_.rowTotal);
   for (int u : t_.decideNodes) {
@@ -374,6 +492,7 @@ void Engine::setDenseRows(int which, const std::vector<float>& dense) {
   if (!padded.empty())
     GB_CK(cudaMemcpy(which == 0 ? d_->tree.regret : d_->tree.strat, padded.data(),
                      padded.size() * sizeof(float), cudaMemcpyHostToDevice));
+  h2d_ += (int64_t)(padded.size() * sizeof(float));
 }
 
 std::vector<float> Engine::nodeRows(int which, int node) const {
@@ -387,6 +506,7 @@ std::vector<float> Engine::nodeRows(int which, int node) const {
                      (which == 0 ? d_->tree.regret : d_->tree.strat) +
                          (size_t)L_.nodes[node].regQ * 4,
                      padded.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  d2h_ += (int64_t)(padded.size() * sizeof(float));
   for (int a = 0; a < nd.na; ++a)
     std::copy(padded.begin() + a * stride, padded.begin() + a * stride + n,
               out.begin() + (size_t)a * n);

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "compiler.h"
@@ -43,6 +44,18 @@ class Engine {
   // One decide node's strategy rows (na x n, dense).
   std::vector<float> nodeRows(int which, int node) const;
 
+  // Benchmark helpers (see pps_gb_time_iterations / pps_gb_profile).
+  double timeIterations(int n);
+  struct KernelStat {
+    std::string name;
+    int64_t launches = 0;
+    double ms = 0.0;
+    double bytes = 0.0;
+  };
+  std::vector<KernelStat> profile(int n);
+  int64_t h2dBytes() const { return h2d_; }
+  int64_t d2hBytes() const { return d2h_; }
+
   // Selects the iteration graph: 0 = depth-level kernels; 1 = fused
   // leaf-street kernel where available. Recaptures on change.
   void setEngineKind(int kind);
@@ -61,7 +74,9 @@ class Engine {
   int engineKind_ = 1;
   int launchesPerIter_ = 0;
   size_t deviceBytes_ = 0;
+  mutable int64_t h2d_ = 0, d2h_ = 0;
   void capture();
+  void buildPlans();
   void ensureWalkBuffers();
 };
 

@@ -1,9 +1,11 @@
-// Fused leaf-street iteration kernel (plan + launch). Placeholder plan:
-// not applicable, so the engine uses the depth-level kernels only.
+// Fused leaf-street iteration kernel: plan + launch interface.
+// (Not applicable yet: the plan reports ok = false and the engine runs the
+// depth-level kernels.)
 #pragma once
 
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <vector>
 
 #include "compiler.h"
@@ -19,23 +21,20 @@ struct ListRef {
 
 struct LeafPlan {
   bool ok = false;
-  int rootDepthMin = 0;
-  std::vector<ListRef> upperBwd;
-  float* scratch = nullptr;
-  size_t scratchFloats = 0;
-  size_t smemBytes = 0;
+  int upperDepth = 0;                         // depth levels run by the level kernels
+  std::vector<ListRef> upperBwd;              // per depth: upper nodes
+  std::vector<std::vector<int>> upperBwdNodes;
+  double algoBytes[2] = {0.0, 0.0};           // per traverser launch
 };
 
-__global__ void leafK() {}
+inline LeafPlan planLeaf(const Tree&, const HostLayout&, std::vector<int>&) { return LeafPlan{}; }
 
-inline LeafPlan planLeaf(const Tree&, const HostLayout&, std::vector<int>&) {
-  return LeafPlan{};
-}
+inline void finishLeaf(LeafPlan&, const int*, const std::function<float*(size_t)>&) {}
 
-inline int launchLeaf(const LeafPlan&, const DevTree&, const DevRows<float>&,
-                      const int*, int, cudaStream_t) {
-  return 0;
-}
+inline cudaError_t prepareLeaf(LeafPlan&) { return cudaSuccess; }
+
+inline void launchLeaf(const LeafPlan&, const DevTree&, const DevRows<float>&, int,
+                       cudaStream_t) {}
 
 }  // namespace gb
 }  // namespace pps

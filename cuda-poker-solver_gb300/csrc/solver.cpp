@@ -150,6 +150,42 @@ void SolverCore::continueSolve(int iterations, double target) {
   replayChunks(iterations, target);
 }
 
+// Makes the device schedule cover the next n iterations (benchmarks run
+// past a planned solve; DCFR needs only the absolute index).
+void SolverCore::extendSchedule(int n) {
+  requireEngine();
+  if (lastAlgo_.empty() || sched_.hs30) {
+    lastAlgo_ = "dcfr";
+    sched_ = Schedule{};
+  }
+  const int64_t t0 = totalIters_, tEnd = t0 + n;
+  if (tEnd > (int64_t)std::numeric_limits<int>::max())
+    throw Error{PPS_GB_E_ARG, "schedule index overflow"};
+  std::vector<float> tab((size_t)tEnd * 3);
+  for (int64_t t = 0; t < tEnd; ++t) {
+    double c[3];
+    sched_.coefs((int)t, (int)tEnd, c);
+    for (int k = 0; k < 3; ++k) tab[(size_t)t * 3 + k] = (float)c[k];
+  }
+  eng_->setSchedule(tab, (int)t0);
+}
+
+double SolverCore::timeIterations(int n) {
+  extendSchedule(n);
+  const double ms = eng_->timeIterations(n);
+  totalIters_ += n;
+  iterationsRun_ = n;
+  return ms;
+}
+
+std::vector<Engine::KernelStat> SolverCore::profile(int n) {
+  extendSchedule(n);
+  auto out = eng_->profile(n);
+  totalIters_ += n;
+  iterationsRun_ = n;
+  return out;
+}
+
 // ---------------------------------------------------------------------------
 // Walks and stats.
 // ---------------------------------------------------------------------------

@@ -49,6 +49,10 @@ class SolverCore {
   gpu::TreeStructure treeStructure() const;
   void save(const std::string& path) const;
   void debugDump();
+  // Benchmark helpers: n more iterations continuing the DCFR schedule
+  // (CUDA-event timed / profiled launch by launch).
+  double timeIterations(int n);
+  std::vector<Engine::KernelStat> profile(int n);
   // Root value (chips) of one FP64 walk; fills the traverser's root row.
   double walkValue(int tr, int mode, std::vector<double>* rootRow);
 
@@ -70,6 +74,7 @@ class SolverCore {
   void replayChunks(int iterations, double target);
   double explNow();
   void checkDecide(int decideIdx) const;
+  void extendSchedule(int n);
   void requireEngine() const;
 };
 

@@ -47,7 +47,13 @@ class Info(C.Structure):
                 ("num_decide_nodes", C.c_int32), ("iterations_run", C.c_int32),
                 ("total_iterations", C.c_int64), ("n_base", C.c_int32 * 2),
                 ("row_total", C.c_int64), ("empty", C.c_int32),
-                ("launches_per_iteration", C.c_int32), ("device_bytes", C.c_int64)]
+                ("launches_per_iteration", C.c_int32), ("device_bytes", C.c_int64),
+                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("engine", C.c_int32)]
+
+
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("ms", C.c_double),
+                ("algo_bytes", C.c_double)]
 
 
 class DecideInfo(C.Structure):
@@ -96,6 +102,8 @@ _SIGS = {
     "pps_gb_write_rows": (C.c_int, [H, C.c_int, P(C.c_float), C.c_int64]),
     "pps_gb_walk": (C.c_int, [H, C.c_int, C.c_int, P(C.c_double), P(C.c_double)]),
     "pps_gb_set_engine": (C.c_int, [H, C.c_int]),
+    "pps_gb_time_iterations": (C.c_int, [H, C.c_int, P(C.c_double)]),
+    "pps_gb_profile": (C.c_int, [H, C.c_int, P(KernelStat), C.c_int, P(C.c_int)]),
     "pps_gb_compile_export": (C.c_int, [P(Spot), P(BetConfig), C.c_int, ARRAY_CB, C.c_void_p]),
     "pps_gb_hand_keys": (C.c_int, [P(C.c_uint8), C.c_int, P(C.c_uint64)]),
     "pps_gb_bet_actions": (C.c_int, [C.c_int64, C.c_int64, P(BetConfig), C.c_int64, C.c_int64,

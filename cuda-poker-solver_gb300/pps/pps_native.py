@@ -412,6 +412,21 @@ class Solver:
     def set_engine(self, kind: int) -> None:
         check(lib.pps_gb_set_engine(self._h, int(kind)))
 
+    def time_iterations(self, n: int) -> float:
+        """Milliseconds of n more iterations (graph replays, CUDA events on
+        the solver's stream)."""
+        ms = C.c_double()
+        check(lib.pps_gb_time_iterations(self._h, int(n), C.byref(ms)))
+        return ms.value
+
+    def profile(self, n: int):
+        """Per kernel class over n iterations: {name: (launches, ms, bytes)}."""
+        out = (_abi.KernelStat * 16)()
+        k = C.c_int()
+        check(lib.pps_gb_profile(self._h, int(n), out, 16, C.byref(k)))
+        return {out[i].name.decode(): (int(out[i].launches), out[i].ms, out[i].algo_bytes)
+                for i in range(k.value)}
+
     def debug_dump(self) -> None:
         check(lib.pps_gb_debug_dump(self._h))
 

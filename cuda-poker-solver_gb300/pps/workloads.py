@@ -197,6 +197,33 @@ def batched(count: int = 256, seed: int = 404) -> List[Spot]:
     return out
 
 
+def turn_short() -> Spot:
+    """Short stack: all-in on the turn, the river is a dead-street runout
+    (the regression spot of tools/quality/gpu_postflop_parity.sh:139)."""
+    a = turn_api()
+    return Spot("turn_short", a.board, a.oop, a.ip, 500, 150, BetCfg([0.5, 0.75], [2.5, 3.0]))
+
+
+def flop_short() -> Spot:
+    return Spot("flop_short", board_ids("Qs9h2d"), "AA,KK", "QQ,JJ,AKs", 100, 40,
+                BetCfg([0.5], [], max_raises=1))
+
+
+def flop_small() -> Spot:
+    return Spot("flop_small", board_ids("Qs9h2d"), "AA,KK", "QQ,JJ,AKs", 100, 100,
+                BetCfg([0.5], [], max_raises=1))
+
+
+def river_geo() -> Spot:
+    return Spot("river_geo", board_ids("Qs9h2d7c3h"), "TT+,AKo,KQs", "99+,AJs+,KQo", 100, 450,
+                BetCfg([0.33], [2.0], allin=True, geometric=True, max_raises=2))
+
+
+def river_empty() -> Spot:
+    return Spot("river_empty", board_ids("AsAhAdKsKh"), "AA", "KK,QQ", 100, 100,
+                BetCfg([0.5], []))
+
+
 NAMED = {
     "river_c1": river_c1,
     "turn_c2": turn_c2,
@@ -205,4 +232,9 @@ NAMED = {
     "turn_w52": turn_w52,
     "turn_api": turn_api,
     "turn_tiny": turn_tiny,
+    "turn_short": turn_short,
+    "flop_short": flop_short,
+    "flop_small": flop_small,
+    "river_geo": river_geo,
+    "river_empty": river_empty,
 }

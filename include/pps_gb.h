@@ -94,7 +94,18 @@ typedef struct {
   int32_t empty;     /* 1 when a range compiled to no combos */
   int32_t launches_per_iteration;
   int64_t device_bytes;
+  int64_t h2d_bytes; /* host->device bytes copied since creation */
+  int64_t d2h_bytes; /* device->host bytes copied since creation */
+  int32_t engine;    /* 0 depth-level kernels, 1 fused leaf-street kernel */
 } pps_gb_info;
+
+/* Per kernel class of one profile pass (pps_gb_profile). */
+typedef struct {
+  char name[32];
+  int64_t launches;
+  double ms;          /* summed CUDA-event time of the launches */
+  double algo_bytes;  /* summed algorithmic bytes (see the byte model) */
+} pps_gb_kernel_stat;
 
 /* gpu::DecideNodeInfo (cuda/gpu_cfr.h:54-62). */
 typedef struct {
@@ -208,6 +219,19 @@ int pps_gb_walk(pps_gb_solver* h, int traverser, int mode, double* root_cfv,
 /* Iteration engine choice for the CFR graph: 0 = depth-level kernels,
  * 1 = fused leaf-street kernel where the tree allows it (default). */
 int pps_gb_set_engine(pps_gb_solver* h, int engine);
+
+/* Benchmark helper: enqueues n further DCFR iterations (graph replays that
+ * continue the current DCFR schedule) bracketed by CUDA events recorded on
+ * the solver's own stream, waits, and returns the elapsed milliseconds.
+ * Plays the role of the reference's solve-loop timing in tools/gpu_pfflop.cu:
+ * 169-180. */
+int pps_gb_time_iterations(pps_gb_solver* h, int n, double* ms);
+/* Profile pass (the reference's GPU_CFR_PROFILE mode, cuda/gpu_cfr.cu:
+ * 1895-1987): runs n further iterations launch by launch, each launch
+ * bracketed by CUDA events, and sums time and algorithmic bytes per kernel
+ * class into out[cap]; *n_out = classes written. */
+int pps_gb_profile(pps_gb_solver* h, int n, pps_gb_kernel_stat* out, int cap,
+                   int* n_out);
 
 /* Host-only compile (no device use): runs the tree compiler and reports
  * every artifact in the reference's own layout (cuda/gpu_cfr.cu:1331-1827)

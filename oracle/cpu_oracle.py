@@ -145,6 +145,19 @@ class Oracle:
         lib().orc_set_rows(self.h, int(which), a.ctypes.data_as(C.POINTER(C.c_float)))
 
 
+def oracle_for(spot, threads=None, precision=32, parse_range=None):
+    """An Oracle for a workloads.Spot; string ranges need `parse_range`."""
+    def w(r):
+        if isinstance(r, str):
+            if parse_range is None:
+                raise ValueError("string range needs a parser")
+            return np.asarray(parse_range(r), dtype=np.float64)
+        return np.array(r, dtype=np.float64)
+    cfgs = [cfg_from(c) for c in spot.street_cfgs] if spot.street_cfgs else [cfg_from(spot.cfg)]
+    return Oracle(spot.board, w(spot.oop), w(spot.ip), spot.pot, spot.stack, cfgs, precision,
+                  threads)
+
+
 def strength7(cards) -> int:
     b = (C.c_uint8 * 7)(*[int(c) for c in cards])
     return int(lib().orc_strength7(b))

@@ -77,19 +77,7 @@ def capture(spot: wl.Spot):
 
 
 def edge_spots():
-    s = []
-    api = wl.turn_api()
-    s.append(wl.Spot("turn_short", api.board, api.oop, api.ip, 500, 150,
-                     wl.BetCfg([0.5, 0.75], [2.5, 3.0])))
-    s.append(wl.Spot("flop_short", wl.board_ids("Qs9h2d"), "AA,KK", "QQ,JJ,AKs",
-                     100, 40, wl.BetCfg([0.5], [], max_raises=1)))
-    s.append(wl.Spot("river_geo", wl.board_ids("Qs9h2d7c3h"), "TT+,AKo,KQs",
-                     "99+,AJs+,KQo", 100, 450,
-                     wl.BetCfg([0.33], [2.0], allin=True, geometric=True,
-                               max_raises=2)))
-    s.append(wl.Spot("river_empty", wl.board_ids("AsAhAdKsKh"), "AA", "KK,QQ",
-                     100, 100, wl.BetCfg([0.5], [])))
-    return s
+    return [wl.turn_short(), wl.flop_short(), wl.river_geo(), wl.river_empty()]
 
 
 def sha(a: np.ndarray) -> str:
@@ -112,9 +100,8 @@ def main():
         np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % spot.name), **arrs)
         print(spot.name, int(arrs["numNodes"][0]), "nodes")
     hashes = {}
-    flop = wl.Spot("flop_small", wl.board_ids("Qs9h2d"), "AA,KK", "QQ,JJ,AKs",
-                   100, 100, wl.BetCfg([0.5], [], max_raises=1))
-    for spot in [wl.turn_w52(), wl.turn_c3(), wl.turn_c2(uniform_config=True), flop]:
+    for spot in [wl.turn_w52(), wl.turn_c3(), wl.turn_c2(uniform_config=True),
+                 wl.flop_small()]:
         arrs = capture(spot)
         hashes[spot.name] = {k: [sha(v), int(v.size)] for k, v in arrs.items()}
         print(spot.name, int(arrs["numNodes"][0]), "nodes (hashed)")
