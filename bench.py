@@ -190,6 +190,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-iters", type=int, default=1000,
+                    help="iterations of the end-to-end solve (BASELINE: 1000)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -224,15 +226,15 @@ def main():
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     s = make()
-    s.solve(1000)
+    s.solve(args.e2e_iters)
     st = s.stats()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     info = s.info()
-    e2e = {"value": 1000.0 / e2e_s, "unit": "iters/s",
-           "h2d_bytes_per_step": int(info.h2d_bytes) // 1000,
-           "d2h_bytes_per_step": int(info.d2h_bytes) // 1000,
-           "includes": "compile + upload + 1000 iterations + FP64 stats walks",
+    e2e = {"value": args.e2e_iters / e2e_s, "unit": "iters/s",
+           "h2d_bytes_per_step": int(info.h2d_bytes) // args.e2e_iters,
+           "d2h_bytes_per_step": int(info.d2h_bytes) // args.e2e_iters,
+           "includes": "compile + upload + %d iterations + FP64 stats walks" % args.e2e_iters,
            "stats": {"ev_oop": st["ev_oop"], "ev_ip": st["ev_ip"],
                      "exploitability": st["exploitability"]}}
 

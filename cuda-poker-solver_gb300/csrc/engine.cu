@@ -3,9 +3,9 @@
 // reference's captureGraph, cuda/gpu_cfr.cu:844-868) as a CUDA graph, and
 // runs the FP64 walks.
 //
-// An iteration is described once as a launch plan (kernel, list, traverser,
-// algorithmic bytes); graph capture, the profile pass and the walks all
-// replay a plan.
+// An iteration is described once as a launch plan (kernel, task list,
+// traverser, algorithmic bytes); graph capture and the profile pass replay
+// the plan.
 #include "engine.h"
 
 #include <cuda_runtime.h>
@@ -41,8 +41,8 @@ V* alloc(size_t count, size_t& bytes) {
   return p;
 }
 
-enum LaunchKind { kFwdDecide, kFwdChance, kBwd, kLeafSweep, kCounter };
-const char* kLaunchName[] = {"fwd_decide", "fwd_chance", "bwd_level", "leaf_street", "counter"};
+enum LaunchKind { kFwd, kBwd, kLeafSweep, kCounter };
+const char* kLaunchName[] = {"fwd_level", "bwd_level", "leaf_street", "counter"};
 
 struct Launch {
   LaunchKind kind;
@@ -63,13 +63,13 @@ struct Engine::Dev {
   DevRows<double> rowsD{};
   float* coef = nullptr;
   size_t coefCap = 0;  // iterations the coef table holds
-  int coefValid = 0;   // leading entries uploaded
   int* counter = nullptr;
-  int* lists = nullptr;
-  std::vector<ListRef> fwdDecide[2], fwdChance[2], bwd;
+  int* tasks = nullptr;
+  std::vector<ListRef> fwd[2], bwd[2];
   LeafPlan leaf;       // fused leaf-street plan (ok = false if not applicable)
   std::vector<Launch> plan[2];  // per engine kind: one iteration
   bool walkReady = false;
+  int maxN = 0;
   size_t smemF = 0, smemD = 0;
 
   template <typename P>
@@ -92,22 +92,20 @@ V* upload(Engine::Dev& d, const std::vector<V>& v, size_t& bytes, int64_t& h2d) 
   return d.own(p);
 }
 
-unsigned gridOf(int count) { return (unsigned)std::min(count, 65535); }
+unsigned gridOf(int count) {
+  return (unsigned)std::min((count + kWarps - 1) / kWarps, 1 << 20);
+}
 
 // Issues one planned launch on the engine stream (CFR mode, f32 rows).
 void issue(Engine::Dev& d, const Launch& l) {
   switch (l.kind) {
-    case kFwdDecide:
-      fwdDecideK<float><<<gridOf(l.list.count), kThreads, 0, d.stream>>>(
-          d.tree, d.rowsF, d.lists + l.list.off, l.list.count, l.tr, 0);
-      break;
-    case kFwdChance:
-      fwdChanceK<float><<<gridOf(l.list.count), kThreads, 0, d.stream>>>(
-          d.tree, d.rowsF, d.lists + l.list.off, l.list.count, l.tr);
+    case kFwd:
+      fwdLevelK<float><<<gridOf(l.list.count), kThreads, 0, d.stream>>>(
+          d.tree, d.rowsF, d.tasks + l.list.off, l.list.count, l.tr, 0);
       break;
     case kBwd:
-      bwdK<float><<<gridOf(l.list.count), kThreads, d.smemF, d.stream>>>(
-          d.tree, d.rowsF, d.lists + l.list.off, l.list.count, l.tr, kModeCFR);
+      bwdLevelK<float><<<gridOf(l.list.count), kThreads, d.smemF, d.stream>>>(
+          d.tree, d.rowsF, d.tasks + l.list.off, l.list.count, l.tr, kModeCFR, d.maxN);
       break;
     case kLeafSweep:
       launchLeaf(d.leaf, d.tree, d.rowsF, l.tr, d.stream);
@@ -155,29 +153,29 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
     h2d_ += (int64_t)(row.size() * sizeof(float));
   }
 
-  // Work lists, concatenated.
+  // Task lists, concatenated.
   std::vector<int> all;
   auto addList = [&](const std::vector<int>& v) {
     ListRef r{(int)all.size(), (int)v.size()};
     all.insert(all.end(), v.begin(), v.end());
     return r;
   };
-  const int D = (int)L_.bwd.size();
+  const int D = (int)L_.bwdTasks[0].size();
   for (int tr = 0; tr < 2; ++tr)
     for (int dd = 0; dd < D; ++dd) {
-      d.fwdDecide[tr].push_back(addList(L_.fwdDecide[tr][dd]));
-      d.fwdChance[tr].push_back(addList(L_.fwdChance[tr][dd]));
+      d.fwd[tr].push_back(addList(L_.fwdTasks[tr][dd]));
+      d.bwd[tr].push_back(addList(L_.bwdTasks[tr][dd]));
     }
-  for (int dd = 0; dd < D; ++dd) d.bwd.push_back(addList(L_.bwd[dd]));
   d.leaf = planLeaf(t_, L_, all);
-  d.lists = upload(d, all, B, h2d_);
-  if (d.leaf.ok) finishLeaf(d.leaf, d.lists, [&](size_t n) { return d.own(alloc<float>(n, B)); });
+  d.tasks = upload(d, all, B, h2d_);
+  if (d.leaf.ok) finishLeaf(d.leaf, d.tasks, [&](size_t n) { return d.own(alloc<float>(n, B)); });
 
-  d.smemF = bwdSmemBytes<float>(L_.maxN);
-  d.smemD = bwdSmemBytes<double>(L_.maxN);
-  GB_CK(cudaFuncSetAttribute(bwdK<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  d.maxN = L_.maxN;
+  d.smemF = kWarps * warpScratchBytes<float>(d.maxN);
+  d.smemD = kWarps * warpScratchBytes<double>(d.maxN);
+  GB_CK(cudaFuncSetAttribute(bwdLevelK<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)d.smemF));
-  GB_CK(cudaFuncSetAttribute(bwdK<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  GB_CK(cudaFuncSetAttribute(bwdLevelK<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)d.smemD));
   if (d.leaf.ok) GB_CK(prepareLeaf(d.leaf));
   buildPlans();
@@ -196,67 +194,64 @@ Engine::~Engine() {
 
 void* Engine::stream() const { return (void*)d_->stream; }
 
-// Algorithmic f32 row bytes of each launch: every row a launch must read or
+// Algorithmic f32 row bytes of one task: every row the task must read or
 // write once (index tables excluded).
+double Engine::taskBytes(int task, int tr, bool fwd) const {
+  const Tree& t = t_;
+  const int u = task >> 8, sub = (task >> 2) & 63, kind = task & 3;
+  const Node& nd = t.nodes[u];
+  auto share = [&](int n) {  // the quads of this task's chunk
+    const int q = (int)quads(n), q0 = sub * kChunkQuads, q1 = std::min(q, q0 + kChunkQuads);
+    return std::max(0, q1 - q0) * 4.0 * n / std::max(4 * q, 1);
+  };
+  if (fwd) {
+    if (kind == kTaskChance) {
+      const int ch = t.children[nd.childBase + sub];
+      return 4.0 * t.n(ch, 1 - tr) + 4.0 * t.n(u, 1 - tr) / nd.nChildren;
+    }
+    return 4.0 * share(t.n(u, 1 - tr)) * (1 + 2.0 * nd.na);
+  }
+  switch (kind) {
+    case kTaskShowdown:
+    case kTaskFold:
+      return 4.0 * (t.n(u, 1 - tr) + t.n(u, tr));
+    case kTaskChance: {
+      double kids = 0;
+      for (int k = 0; k < nd.nChildren; ++k) kids += t.n(t.children[nd.childBase + k], tr);
+      return 4.0 * share(t.n(u, tr)) * (1.0 + kids / std::max(t.n(u, tr), 1));
+    }
+    default:
+      return nd.player == tr ? 4.0 * share(t.n(u, tr)) * (5.0 * nd.na + 1)
+                             : 4.0 * share(t.n(u, tr)) * (nd.na + 1.0);
+  }
+}
+
 void Engine::buildPlans() {
   Dev& d = *d_;
-  const Tree& t = t_;
-  auto n = [&](int u, int p) { return (double)t.n(u, p); };
-  auto fwdDecideBytes = [&](const std::vector<int>& v, int tr) {
+  const int D = (int)L_.bwdTasks[0].size();
+  auto listBytes = [&](const std::vector<int>& v, int tr, bool fwd) {
     double b = 0;
-    for (int u : v) b += 4 * n(u, 1 - tr) * (1 + 2.0 * t.nodes[u].na);
+    for (int task : v) b += taskBytes(task, tr, fwd);
     return b;
   };
-  auto fwdChanceBytes = [&](const std::vector<int>& v, int tr) {
-    double b = 0;
-    for (int item : v) {
-      const int u = item >> 6, br = item & 63;
-      const int ch = t.children[t.nodes[u].childBase + br];
-      b += 4 * n(ch, 1 - tr) + 4 * n(u, 1 - tr) / t.nodes[u].nChildren;
-    }
-    return b;
-  };
-  auto bwdNodeBytes = [&](int u, int tr) {
-    const Node& nd = t.nodes[u];
-    switch (nd.kind) {
-      case kDecide:
-        return nd.player == tr ? 4 * n(u, tr) * (5.0 * nd.na + 1) : 4 * n(u, tr) * (nd.na + 1.0);
-      case kChance: {
-        double b = 4 * n(u, tr);
-        for (int k = 0; k < nd.nChildren; ++k) b += 4 * n(t.children[nd.childBase + k], tr);
-        return b;
-      }
-      default:
-        return 4 * (n(u, 1 - tr) + n(u, tr));
-    }
-  };
-  const int D = (int)L_.bwd.size();
   for (int kind = 0; kind < 2; ++kind) {
     std::vector<Launch>& P = d.plan[kind];
     P.clear();
     const bool leaf = kind == 1 && d.leaf.ok;
     for (int tr = 0; tr < 2; ++tr) {
-      const int fwdEnd = leaf ? d.leaf.upperDepth : D;
-      for (int dd = 0; dd < fwdEnd; ++dd) {
-        if (d.fwdDecide[tr][dd].count)
-          P.push_back({kFwdDecide, tr, d.fwdDecide[tr][dd],
-                       fwdDecideBytes(L_.fwdDecide[tr][dd], tr)});
-        if (d.fwdChance[tr][dd].count)
-          P.push_back({kFwdChance, tr, d.fwdChance[tr][dd],
-                       fwdChanceBytes(L_.fwdChance[tr][dd], tr)});
-      }
+      const std::vector<std::vector<int>>& fw = leaf ? d.leaf.fwdTasks[tr] : L_.fwdTasks[tr];
+      const std::vector<std::vector<int>>& bw = leaf ? d.leaf.bwdTasks[tr] : L_.bwdTasks[tr];
+      const std::vector<ListRef>& fr = leaf ? d.leaf.fwd[tr] : d.fwd[tr];
+      const std::vector<ListRef>& brf = leaf ? d.leaf.bwd[tr] : d.bwd[tr];
+      for (int dd = 0; dd < (int)fr.size(); ++dd)
+        if (fr[dd].count) P.push_back({kFwd, tr, fr[dd], listBytes(fw[dd], tr, true)});
       if (leaf) P.push_back({kLeafSweep, tr, ListRef{}, d.leaf.algoBytes[tr]});
-      for (int dd = (leaf ? d.leaf.upperDepth : D) - 1; dd >= 0; --dd) {
-        const ListRef b = leaf ? d.leaf.upperBwd[dd] : d.bwd[dd];
-        const std::vector<int>& nodes = leaf ? d.leaf.upperBwdNodes[dd] : L_.bwd[dd];
-        if (!b.count) continue;
-        double bytes = 0;
-        for (int u : nodes) bytes += bwdNodeBytes(u, tr);
-        P.push_back({kBwd, tr, b, bytes});
-      }
+      for (int dd = (int)brf.size() - 1; dd >= 0; --dd)
+        if (brf[dd].count) P.push_back({kBwd, tr, brf[dd], listBytes(bw[dd], tr, false)});
     }
     P.push_back({kCounter, 0, ListRef{}, 0.0});
   }
+  (void)D;
 }
 
 void Engine::zeroRows() {
@@ -292,7 +287,6 @@ void Engine::setSchedule(const std::vector<float>& coef, int counter) {
   GB_CK(cudaMemcpyAsync(d.coef, coef.data(), coef.size() * sizeof(float),
                         cudaMemcpyHostToDevice, d.stream));
   h2d_ += (int64_t)(coef.size() * sizeof(float));
-  d.coefValid = (int)entries;
   setCounter(counter);
 }
 
@@ -376,8 +370,8 @@ std::vector<Engine::KernelStat> Engine::profile(int n) {
       GB_CK(cudaEventRecord(ev[k++], d.stream));
     }
   GB_CK(cudaStreamSynchronize(d.stream));
-  std::vector<KernelStat> out(5);
-  for (int c = 0; c < 5; ++c) out[c].name = kLaunchName[c];
+  std::vector<KernelStat> out(4);
+  for (int c = 0; c < 4; ++c) out[c].name = kLaunchName[c];
   k = 0;
   for (int it = 0; it < n; ++it)
     for (const Launch& l : P) {
@@ -416,21 +410,18 @@ void Engine::ensureWalkBuffers() {
 void Engine::walk(int tr, int mode) {
   Dev& d = *d_;
   ensureWalkBuffers();
-  const int D = (int)L_.bwd.size();
+  const int D = (int)d.fwd[tr].size();
   for (int dd = 0; dd < D; ++dd) {
-    const ListRef a = d.fwdDecide[tr][dd], c = d.fwdChance[tr][dd];
+    const ListRef a = d.fwd[tr][dd];
     if (a.count)
-      fwdDecideK<double><<<gridOf(a.count), kThreads, 0, d.stream>>>(
-          d.tree, d.rowsD, d.lists + a.off, a.count, tr, 1);
-    if (c.count)
-      fwdChanceK<double><<<gridOf(c.count), kThreads, 0, d.stream>>>(
-          d.tree, d.rowsD, d.lists + c.off, c.count, tr);
+      fwdLevelK<double><<<gridOf(a.count), kThreads, 0, d.stream>>>(
+          d.tree, d.rowsD, d.tasks + a.off, a.count, tr, 1);
   }
   for (int dd = D - 1; dd >= 0; --dd) {
-    const ListRef b = d.bwd[dd];
+    const ListRef b = d.bwd[tr][dd];
     if (b.count)
-      bwdK<double><<<gridOf(b.count), kThreads, d.smemD, d.stream>>>(
-          d.tree, d.rowsD, d.lists + b.off, b.count, tr, mode);
+      bwdLevelK<double><<<gridOf(b.count), kThreads, d.smemD, d.stream>>>(
+          d.tree, d.rowsD, d.tasks + b.off, b.count, tr, mode, d.maxN);
   }
   GB_CK(cudaGetLastError());
   GB_CK(cudaStreamSynchronize(d.stream));

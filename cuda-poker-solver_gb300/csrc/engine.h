@@ -77,6 +77,7 @@ class Engine {
   mutable int64_t h2d_ = 0, d2h_ = 0;
   void capture();
   void buildPlans();
+  double taskBytes(int task, int tr, bool fwd) const;
   void ensureWalkBuffers();
 };
 

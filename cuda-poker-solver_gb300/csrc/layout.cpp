@@ -102,7 +102,7 @@ HostLayout buildLayout(const Tree& t) {
       });
       std::vector<uint64_t> sortedKey(no);
       for (int k = 0; k < no; ++k) sortedKey[k] = keyBase[opp][ol[ord[k]]];
-      std::vector<int> segStart(53, 0), segPos;
+      std::vector<int> segStart(53, 0), segSlot;
       std::vector<std::vector<int>> posOfCard(52);
       for (int k = 0; k < no; ++k) {
         const int b = ol[ord[k]];
@@ -110,13 +110,13 @@ HostLayout buildLayout(const Tree& t) {
         posOfCard[t.side[opp].cards[2 * b + 1]].push_back(k);
       }
       for (int c = 0; c < 52; ++c) {
-        segStart[c] = (int)segPos.size();
-        segPos.insert(segPos.end(), posOfCard[c].begin(), posOfCard[c].end());
+        segStart[c] = (int)segSlot.size();
+        for (int k : posOfCard[c]) segSlot.push_back(ord[k]);
       }
-      segStart[52] = (int)segPos.size();
+      segStart[52] = (int)segSlot.size();
       sd.sdOff[tr] = appendU16(L.poolU16, ord);
       appendU16(L.poolU16, segStart);
-      appendU16(L.poolU16, segPos);
+      appendU16(L.poolU16, segSlot);
       sd.sdInfoOff[tr] = (int)L.poolSd.size();
       for (int i = 0; i < (int)tl.size(); ++i) {
         const int b = tl[i];
@@ -211,23 +211,40 @@ HostLayout buildLayout(const Tree& t) {
   L.reachQuads[0] = reachQ[0];
   L.reachQuads[1] = reachQ[1];
 
-  // ---- work lists ----
+  // ---- warp task lists ----
   const int D = t.maxDepth + 1;
   for (int tr = 0; tr < 2; ++tr) {
-    L.fwdDecide[tr].assign(D, {});
-    L.fwdChance[tr].assign(D, {});
-  }
-  L.bwd.assign(D, {});
-  for (int u = 0; u < N; ++u) {
-    const Node& nd = t.nodes[u];
-    L.bwd[nd.depth].push_back(u);
-    for (int tr = 0; tr < 2; ++tr) {
-      if (nd.kind == kDecide && nd.player != tr) L.fwdDecide[tr][nd.depth].push_back(u);
-      if (nd.kind == kChance)
-        for (int br = 0; br < nd.nChildren; ++br)
-          L.fwdChance[tr][nd.depth].push_back(u * 64 + br);
+    L.fwdTasks[tr].assign(D, {});
+    L.bwdTasks[tr].assign(D, {});
+    std::vector<std::vector<int>> sd(D), fd(D), ch(D), dc(D);
+    for (int u = 0; u < N; ++u) {
+      const Node& nd = t.nodes[u];
+      const int chunksTr = (int)((quads(t.n(u, tr)) + kChunkQuads - 1) / kChunkQuads);
+      switch (nd.kind) {
+        case kShowdown: sd[nd.depth].push_back(makeTask(kTaskShowdown, 0, u)); break;
+        case kFold: fd[nd.depth].push_back(makeTask(kTaskFold, 0, u)); break;
+        case kChance:
+          for (int c = 0; c < chunksTr; ++c) ch[nd.depth].push_back(makeTask(kTaskChance, c, u));
+          for (int br = 0; br < nd.nChildren; ++br)
+            L.fwdTasks[tr][nd.depth].push_back(makeTask(kTaskChance, br, u));
+          break;
+        default: {
+          for (int c = 0; c < chunksTr; ++c) dc[nd.depth].push_back(makeTask(kTaskDecide, c, u));
+          if (nd.player != tr) {
+            const int chunksOpp =
+                (int)((quads(t.n(u, 1 - tr)) + kChunkQuads - 1) / kChunkQuads);
+            for (int c = 0; c < chunksOpp; ++c)
+              L.fwdTasks[tr][nd.depth].push_back(makeTask(kTaskDecide, c, u));
+          }
+        }
+      }
+    }
+    for (int d = 0; d < D; ++d) {
+      auto& b = L.bwdTasks[tr][d];
+      for (auto* v : {&sd[d], &fd[d], &ch[d], &dc[d]}) b.insert(b.end(), v->begin(), v->end());
     }
   }
+  if (N >= (1 << 24)) throw Error{PPS_GB_E_MEMORY, "tree too large for 24-bit task node ids"};
   return L;
 }
 

@@ -33,6 +33,12 @@ inline int packNode(int kind, int player, int foldBy, int na) {
   return kind | (player << 2) | (foldBy << 3) | (na << 8);
 }
 
+// Warp task word: kind (bits 0-1), sub = quad chunk or chance branch (bits
+// 2-7), node (bits 8-31).
+enum TaskKind : int { kTaskDecide = 0, kTaskChance = 1, kTaskFold = 2, kTaskShowdown = 3 };
+constexpr int kChunkQuads = 128;  // row quads per decide/chance task
+inline int makeTask(int kind, int sub, int node) { return kind | (sub << 2) | (node << 8); }
+
 struct alignas(16) NodeDev {
   int meta;         // packNode(...)
   int state;        // BoardState index
@@ -59,8 +65,8 @@ struct alignas(16) StateDev {
   int downOff[2];   // i16 pool: parent slot -> child slot or -1
   int sdOff[2];     // river states, per traverser tr: u16 pool holding
                     // ord[n_opp] (opponent slots, weakest first), 53
-                    // card-segment starts, then per card the sorted
-                    // positions of opponent combos holding it
+                    // card-segment starts, then per card (in strength
+                    // order) the slots of the opponent combos holding it
   int sdInfoOff[2]; // river states, per traverser: u32x4 pool, one entry
                     // per traverser slot (see showdownInfo)
 };
@@ -88,11 +94,11 @@ struct HostLayout {
   uint64_t regQuads = 0;          // regret (= strategy) pool size
   uint64_t cfvQuads = 0;
   uint64_t reachQuads[2] = {0, 0};
-  // Work lists per depth d. fwdDecide[tr][d]: the opponent's decide nodes
-  // (node ids); fwdChance[tr][d]: one item per chance branch, stored as
-  // node * 64 + branch; bwd[d]: every node at depth d.
-  std::vector<std::vector<int>> fwdDecide[2], fwdChance[2];
-  std::vector<std::vector<int>> bwd;
+  // Warp task lists (kernels.cuh task words) per traverser and depth:
+  // forward = the opponent's decide nodes in 128-quad chunks plus one task
+  // per chance branch; backward = showdowns, folds, chance chunks, decide
+  // chunks (longest tasks first).
+  std::vector<std::vector<int>> fwdTasks[2], bwdTasks[2];
   int maxN = 0;        // largest list size (either side)
   int maxCardSeg = 0;  // longest card segment of any list
 };

@@ -21,10 +21,10 @@ struct ListRef {
 
 struct LeafPlan {
   bool ok = false;
-  int upperDepth = 0;                         // depth levels run by the level kernels
-  std::vector<ListRef> upperBwd;              // per depth: upper nodes
-  std::vector<std::vector<int>> upperBwdNodes;
-  double algoBytes[2] = {0.0, 0.0};           // per traverser launch
+  // Level task lists of the nodes above the leaf street, per traverser.
+  std::vector<std::vector<int>> fwdTasks[2], bwdTasks[2];
+  std::vector<ListRef> fwd[2], bwd[2];
+  double algoBytes[2] = {0.0, 0.0};  // per traverser launch
 };
 
 inline LeafPlan planLeaf(const Tree&, const HostLayout&, std::vector<int>&) { return LeafPlan{}; }
