@@ -407,10 +407,11 @@ int pps_gb_time_iterations(pps_gb_solver* h, int n, double* ms) {
   });
 }
 
-int pps_gb_profile(pps_gb_solver* h, int n, pps_gb_kernel_stat* out, int cap, int* n_out) {
+int pps_gb_profile(pps_gb_solver* h, int n, int flags, pps_gb_kernel_stat* out, int cap,
+                   int* n_out) {
   return guarded([&] {
     if (!out || !n_out || n < 1) throw Error{PPS_GB_E_ARG, "bad arguments"};
-    const auto stats = core(h).profile(n);
+    const auto stats = core(h).profile(n, (flags & 1) != 0);
     *n_out = std::min<int>((int)stats.size(), cap);
     for (int i = 0; i < *n_out; ++i) {
       std::memset(out[i].name, 0, sizeof(out[i].name));

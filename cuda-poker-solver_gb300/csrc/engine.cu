@@ -65,6 +65,7 @@ struct Engine::Dev {
   size_t coefCap = 0;  // iterations the coef table holds
   int* counter = nullptr;
   int* tasks = nullptr;
+  std::vector<int> hostTasks;  // host copy of the concatenated task lists
   std::vector<ListRef> fwd[2], bwd[2];
   LeafPlan leaf;       // fused leaf-street plan (ok = false if not applicable)
   std::vector<Launch> plan[2];  // per engine kind: one iteration
@@ -92,9 +93,7 @@ V* upload(Engine::Dev& d, const std::vector<V>& v, size_t& bytes, int64_t& h2d) 
   return d.own(p);
 }
 
-unsigned gridOf(int count) {
-  return (unsigned)std::min((count + kWarps - 1) / kWarps, 1 << 20);
-}
+unsigned gridOf(int count) { return (unsigned)std::min(count, 1 << 20); }
 
 // Issues one planned launch on the engine stream (CFR mode, f32 rows).
 void issue(Engine::Dev& d, const Launch& l) {
@@ -168,11 +167,12 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
     }
   d.leaf = planLeaf(t_, L_, all);
   d.tasks = upload(d, all, B, h2d_);
+  d.hostTasks = all;
   if (d.leaf.ok) finishLeaf(d.leaf, d.tasks, [&](size_t n) { return d.own(alloc<float>(n, B)); });
 
   d.maxN = L_.maxN;
-  d.smemF = kWarps * warpScratchBytes<float>(d.maxN);
-  d.smemD = kWarps * warpScratchBytes<double>(d.maxN);
+  d.smemF = bwdScratchBytes<float>(d.maxN);
+  d.smemD = bwdScratchBytes<double>(d.maxN);
   GB_CK(cudaFuncSetAttribute(bwdLevelK<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)d.smemF));
   GB_CK(cudaFuncSetAttribute(bwdLevelK<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -218,7 +218,9 @@ double Engine::taskBytes(int task, int tr, bool fwd) const {
     case kTaskChance: {
       double kids = 0;
       for (int k = 0; k < nd.nChildren; ++k) kids += t.n(t.children[nd.childBase + k], tr);
-      return 4.0 * share(t.n(u, tr)) * (1.0 + kids / std::max(t.n(u, tr), 1));
+      const int n = t.n(u, tr);
+      const int e = std::max(0, std::min(n, (sub + 1) * kChanceChunk) - sub * kChanceChunk);
+      return 4.0 * e * (1.0 + kids / std::max(n, 1));
     }
     default:
       return nd.player == tr ? 4.0 * share(t.n(u, tr)) * (5.0 * nd.na + 1)
@@ -356,32 +358,55 @@ double Engine::timeIterations(int n) {
   return ms;
 }
 
-std::vector<Engine::KernelStat> Engine::profile(int n) {
+std::vector<Engine::KernelStat> Engine::profile(int n, bool splitKinds) {
   Dev& d = *d_;
-  const std::vector<Launch>& P = d.plan[engineKind_];
+  // With splitKinds, each backward level launch is issued as one launch per
+  // task kind (the lists are sorted by kind), attributing time per kind.
+  static const char* kKindName[] = {"bwd_decide", "bwd_chance", "bwd_fold", "bwd_showdown"};
+  std::vector<std::pair<Launch, std::string>> P;
+  for (const Launch& l : d.plan[engineKind_]) {
+    if (l.kind != kBwd || !splitKinds) {
+      P.push_back({l, kLaunchName[l.kind]});
+      continue;
+    }
+    int i = l.list.off;
+    const int end = l.list.off + l.list.count;
+    while (i < end) {
+      const int kind = d.hostTasks[i] & 3;
+      int j = i;
+      double bytes = 0;
+      while (j < end && (d.hostTasks[j] & 3) == kind) bytes += taskBytes(d.hostTasks[j++], l.tr, false);
+      P.push_back({Launch{kBwd, l.tr, ListRef{i, j - i}, bytes}, kKindName[kind]});
+      i = j;
+    }
+  }
   std::vector<cudaEvent_t> ev(2 * P.size() * (size_t)n);
   for (auto& e : ev) GB_CK(cudaEventCreate(&e));
   size_t k = 0;
   for (int it = 0; it < n; ++it)
-    for (const Launch& l : P) {
+    for (const auto& pl : P) {
       GB_CK(cudaEventRecord(ev[k++], d.stream));
-      issue(d, l);
+      issue(d, pl.first);
       GB_CK(cudaGetLastError());
       GB_CK(cudaEventRecord(ev[k++], d.stream));
     }
   GB_CK(cudaStreamSynchronize(d.stream));
-  std::vector<KernelStat> out(4);
-  for (int c = 0; c < 4; ++c) out[c].name = kLaunchName[c];
+  std::vector<KernelStat> out;
   k = 0;
   for (int it = 0; it < n; ++it)
-    for (const Launch& l : P) {
+    for (const auto& pl : P) {
       float ms = 0.0f;
       GB_CK(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
       k += 2;
-      KernelStat& s = out[l.kind];
-      s.launches += 1;
-      s.ms += ms;
-      s.bytes += l.bytes;
+      auto it2 = std::find_if(out.begin(), out.end(),
+                              [&](const KernelStat& s) { return s.name == pl.second; });
+      if (it2 == out.end()) {
+        out.push_back(KernelStat{pl.second});
+        it2 = out.end() - 1;
+      }
+      it2->launches += 1;
+      it2->ms += ms;
+      it2->bytes += pl.first.bytes;
     }
   for (auto& e : ev) cudaEventDestroy(e);
   out.erase(std::remove_if(out.begin(), out.end(),

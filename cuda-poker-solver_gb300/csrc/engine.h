@@ -52,7 +52,7 @@ class Engine {
     double ms = 0.0;
     double bytes = 0.0;
   };
-  std::vector<KernelStat> profile(int n);
+  std::vector<KernelStat> profile(int n, bool splitKinds = false);
   int64_t h2dBytes() const { return h2d_; }
   int64_t d2hBytes() const { return d2h_; }
 

@@ -6,13 +6,14 @@
 // bottom-up backward pass (bwdLevelK per depth: showdown, fold, chance sum,
 // decide value and the DCFR regret/strategy update).
 //
-// Work is split into warp-sized tasks, one 32-bit task word each:
+// Work is split into CTA-sized tasks, one 32-bit task word each:
 //   bits 0-1 kind, bits 2-7 sub (quad chunk or chance branch), bits 8-31 node.
-// Forward kinds: 0 = decide chunk (128 row quads), 1 = chance branch.
-// Backward kinds: 0 = decide chunk, 1 = chance chunk (128 quads),
-// 2 = fold node, 3 = showdown node (one warp per terminal node). A CTA is
-// kWarps warps; each warp takes tasks independently, so there is no
-// block-wide barrier on the hot path.
+// Forward kinds: 0 = decide chunk (128 row quads, one thread per quad),
+// 1 = chance branch. Backward kinds: 0 = decide chunk, 1 = chance chunk,
+// 2 = fold node, 3 = showdown node. Task lists put the long terminal tasks
+// first. Registers are capped (launch bounds) so that at least 6 CTAs of
+// 128 threads share an SM; the terminal tasks' scratch (one reach row plus
+// prefix arrays, ~19 KB at 1128 combos) fits that budget.
 //
 // Rows are 16-byte-aligned quads (4 floats or 4 doubles) with zero padding.
 // T is the value type of reach and cfv rows: float for CFR iterations,
@@ -27,9 +28,8 @@
 namespace pps {
 namespace gb {
 
-constexpr int kWarps = 4;              // warps per CTA
-constexpr int kThreads = kWarps * 32;  // threads per CTA
-constexpr int kRegNa = 8;              // actions kept in registers
+constexpr int kThreads = 128;  // threads per CTA
+constexpr int kRegNa = 6;      // actions kept in registers by the decide update
 
 struct DevTree {
   const NodeDev* nodes;
@@ -129,54 +129,54 @@ __device__ __forceinline__ void addComp(T& hi, T& lo, T b) {
 }
 
 // ---------------------------------------------------------------------------
-// Forward pass (one launch per depth level).
+// Forward pass (one launch per depth level; one CTA per task).
 // ---------------------------------------------------------------------------
 
+// Opponent decide chunk: child reach = reach x sigma_a, one thread per quad.
 template <typename T>
 __device__ void fwdDecideChunk(const DevTree& t, const DevRows<T>& rows, int u, int chunk,
-                               int tr, int sigSrc, int lane) {
+                               int tr, int sigSrc) {
   const NodeDev nd = t.nodes[u];
   const int na = nodeCount(nd.meta);
   const int n = t.states[nd.state].n[1 - tr];
   const int nq = quadsOf(n);
+  const int q = chunk * kChunkQuads + (int)threadIdx.x;
+  if (q >= nq) return;
   const float* src = (sigSrc == 0 ? t.regret : t.strat) + (size_t)nd.regQ * 4;
   const T* r = rows.reach[tr] + (size_t)t.rows[u].reachQ[tr] * 4;
   const int* kids = t.children + nd.childBase;
   const T uniform = T(1) / T(na);
-  const int q1 = min(nq, (chunk + 1) * kChunkQuads);
-  for (int q = chunk * kChunkQuads + lane; q < q1; q += 32) {
-    T rr[4], acc[4] = {T(0), T(0), T(0), T(0)};
-    ldq(r + 4 * q, rr);
-    if (na <= kRegNa) {
-      T x[kRegNa][4];
+  T rr[4], acc[4] = {T(0), T(0), T(0), T(0)};
+  ldq(r + 4 * q, rr);
+  if (na <= kRegNa) {
+    T x[kRegNa][4];
 #pragma unroll
-      for (int a = 0; a < kRegNa; ++a)
-        if (a < na) {
-          ldqf(src + ((size_t)a * nq + q) * 4, x[a]);
-          for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[a][l], sigSrc);
-        }
-#pragma unroll
-      for (int a = 0; a < kRegNa; ++a)
-        if (a < na) {
-          T out[4];
-          for (int l = 0; l < 4; ++l)
-            out[l] = 4 * q + l < n ? rr[l] * sigmaOf(x[a][l], acc[l], uniform, sigSrc) : T(0);
-          stq(rows.reach[tr] + (size_t)t.rows[kids[a]].reachQ[tr] * 4 + 4 * q, out);
-        }
-    } else {
-      for (int a = 0; a < na; ++a) {
-        T x[4];
-        ldqf(src + ((size_t)a * nq + q) * 4, x);
-        for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], sigSrc);
+    for (int a = 0; a < kRegNa; ++a)
+      if (a < na) {
+        ldqf(src + ((size_t)a * nq + q) * 4, x[a]);
+        for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[a][l], sigSrc);
       }
-      for (int a = 0; a < na; ++a) {
-        T x[4], out[4];
-        ldqf(src + ((size_t)a * nq + q) * 4, x);
+#pragma unroll
+    for (int a = 0; a < kRegNa; ++a)
+      if (a < na) {
+        T out[4];
         for (int l = 0; l < 4; ++l)
-          out[l] = 4 * q + l < n ? rr[l] * sigmaOf(x[l], acc[l], uniform, sigSrc) : T(0);
+          out[l] = 4 * q + l < n ? rr[l] * sigmaOf(x[a][l], acc[l], uniform, sigSrc) : T(0);
         stq(rows.reach[tr] + (size_t)t.rows[kids[a]].reachQ[tr] * 4 + 4 * q, out);
       }
-    }
+    return;
+  }
+  for (int a = 0; a < na; ++a) {
+    T x[4];
+    ldqf(src + ((size_t)a * nq + q) * 4, x);
+    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], sigSrc);
+  }
+  for (int a = 0; a < na; ++a) {
+    T x[4], out[4];
+    ldqf(src + ((size_t)a * nq + q) * 4, x);
+    for (int l = 0; l < 4; ++l)
+      out[l] = 4 * q + l < n ? rr[l] * sigmaOf(x[l], acc[l], uniform, sigSrc) : T(0);
+    stq(rows.reach[tr] + (size_t)t.rows[kids[a]].reachQ[tr] * 4 + 4 * q, out);
   }
 }
 
@@ -185,7 +185,7 @@ __device__ void fwdDecideChunk(const DevTree& t, const DevRows<T>& rows, int u, 
 // probability 1 / (52 - nBoard - 4) (cuda/gpu_cfr.cu:276-293).
 template <typename T>
 __device__ void fwdChanceBranch(const DevTree& t, const DevRows<T>& rows, int u, int br,
-                                int tr, int lane) {
+                                int tr) {
   const int opp = 1 - tr;
   const int child = t.children[t.nodes[u].childBase + br];
   const StateDev& cs = t.states[t.nodes[child].state];
@@ -195,7 +195,7 @@ __device__ void fwdChanceBranch(const DevTree& t, const DevRows<T>& rows, int u,
   const T inv = T(1) / T(ru.chanceQ);
   const T* pr = rows.reach[tr] + (size_t)ru.reachQ[tr] * 4;
   T* cr = rows.reach[tr] + (size_t)t.rows[child].reachQ[tr] * 4;
-  for (int q = lane; q < quadsOf(nc); q += 32) {
+  for (int q = threadIdx.x; q < quadsOf(nc); q += blockDim.x) {
     T out[4];
     for (int l = 0; l < 4; ++l) {
       const int j = 4 * q + l;
@@ -206,126 +206,175 @@ __device__ void fwdChanceBranch(const DevTree& t, const DevRows<T>& rows, int u,
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 6)
 fwdLevelK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int count, int tr,
           int sigSrc) {
-  const int lane = threadIdx.x & 31;
-  for (int i = blockIdx.x * kWarps + (threadIdx.x >> 5); i < count; i += gridDim.x * kWarps) {
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
     const int w = tasks[i];
     const int node = w >> 8, sub = (w >> 2) & 63;
-    if ((w & 3) == kTaskDecide) fwdDecideChunk<T>(t, rows, node, sub, tr, sigSrc, lane);
-    else fwdChanceBranch<T>(t, rows, node, sub, tr, lane);
+    if ((w & 3) == kTaskDecide) fwdDecideChunk<T>(t, rows, node, sub, tr, sigSrc);
+    else fwdChanceBranch<T>(t, rows, node, sub, tr);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Backward pass (one launch per depth level).
+// Backward pass (one launch per depth level; one CTA per task).
 // ---------------------------------------------------------------------------
 
-// Per-warp shared scratch of the terminal tasks, for lists of up to maxN
-// combos: s_local [maxN + 32], block prefix pairs bh/bl [maxN/32 + 2] each,
-// card-segment scans X [2 maxN + 52], segment starts [53].
+// Shared scratch of the terminal tasks for lists of up to maxN combos:
+// staged reach rs [4 quads(maxN)], block-local exclusive prefixes
+// sl [maxN + 32], compensated block prefixes bh/bl [maxN/32 + 2] each,
+// card-segment scans X [2 maxN + 52], and the node's staged u16 index
+// table tab [3 maxN + 64] (showdown: order, segment starts, segment slots;
+// fold: card lists).
+__host__ __device__ inline int scratchBlocks(int maxN) { return maxN / 32 + 2; }
+__host__ __device__ inline int scratchTab(int maxN) { return (3 * maxN + 53 + 7) / 8 * 8 + 8; }
+
+// Chance tasks keep 64 row pointers and 64 slot-map pointers at the start of
+// the same scratch (a chance node has at most 49 branches).
+constexpr size_t kChanceScratchBytes = 2 * 64 * sizeof(void*);
+
 template <typename T>
-struct WarpScratch {
+__host__ __device__ inline size_t bwdScratchBytes(int maxN) {
+  const size_t elems = 4 * (size_t)((maxN + 3) / 4) + (size_t)(maxN + 32) +
+                       2 * (size_t)scratchBlocks(maxN) + 2 * (size_t)maxN + 52;
+  const size_t valBytes = (elems * sizeof(T) + 15) / 16 * 16;
+  const size_t total = valBytes + (size_t)scratchTab(maxN) * sizeof(uint16_t);
+  return total > kChanceScratchBytes ? total : kChanceScratchBytes;
+}
+
+template <typename T>
+struct Scratch {
+  T* rs;
   T* sl;
   T* bh;
   T* bl;
   T* X;
-  int* seg;
+  uint16_t* tab;
 };
 
-__host__ __device__ inline int scratchBlocks(int maxN) { return maxN / 32 + 2; }
-
 template <typename T>
-__host__ __device__ inline size_t warpScratchBytes(int maxN) {
-  const size_t elems = (size_t)(maxN + 32) + 2 * (size_t)scratchBlocks(maxN) +
-                       2 * (size_t)maxN + 52;
-  return ((elems * sizeof(T) + 53 * sizeof(int)) + 15) / 16 * 16;
-}
-
-template <typename T>
-__device__ WarpScratch<T> warpScratch(unsigned char* smem, int warp, int maxN) {
-  unsigned char* base = smem + (size_t)warp * warpScratchBytes<T>(maxN);
-  WarpScratch<T> s;
-  s.sl = reinterpret_cast<T*>(base);
+__device__ Scratch<T> scratchOf(unsigned char* smem, int maxN) {
+  Scratch<T> s;
+  s.rs = reinterpret_cast<T*>(smem);
+  s.sl = s.rs + 4 * ((maxN + 3) / 4);
   s.bh = s.sl + maxN + 32;
   s.bl = s.bh + scratchBlocks(maxN);
   s.X = s.bl + scratchBlocks(maxN);
-  s.seg = reinterpret_cast<int*>(s.X + 2 * maxN + 52);
+  const size_t elems = 4 * (size_t)((maxN + 3) / 4) + (size_t)(maxN + 32) +
+                       2 * (size_t)scratchBlocks(maxN) + 2 * (size_t)maxN + 52;
+  s.tab = reinterpret_cast<uint16_t*>(smem + (elems * sizeof(T) + 15) / 16 * 16);
   return s;
 }
 
-// Showdown (one warp per node): combo i wins against opponents strictly
+// Copies n u16 table entries (16-byte aligned in the pool, which is padded
+// to a multiple of 8 entries) into shared memory with 16-byte loads.
+__device__ __forceinline__ void stageTab(uint16_t* dst, const uint16_t* src, int n) {
+  const uint4* s4 = reinterpret_cast<const uint4*>(src);
+  uint4* d4 = reinterpret_cast<uint4*>(dst);
+  for (int k = threadIdx.x; k < (n + 7) / 8; k += blockDim.x) d4[k] = s4[k];
+}
+
+// Stages row r (n entries, quad padded) into shared memory.
+template <typename T>
+__device__ __forceinline__ void stageRow(T* dst, const T* r, int n) {
+  for (int q = threadIdx.x; q < quadsOf(n); q += blockDim.x) {
+    T x[4];
+    ldq(r + 4 * q, x);
+    for (int l = 0; l < 4; ++l) dst[4 * q + l] = x[l];
+  }
+}
+
+// Showdown (one CTA per node): combo i wins against opponents strictly
 // weaker, ties the equal band, loses to the rest (payoffs as
 // cuda/gpu_cfr.cu:356-406). Band masses come from an exclusive prefix of the
-// strength-sorted opponent reach, kept as a compensated (hi, lo) prefix per
-// 32-entry block plus a block-local offset. Opponents sharing a card with i
-// are removed with per-card exclusive scans (X) at precomputed counts; the
-// identical combo (in the tie band, removed twice) is added back once.
+// strength-sorted opponent reach: block-local prefixes of 32 entries plus a
+// compensated (hi, lo) prefix of the block totals. Opponents sharing a card
+// with i are removed with per-card exclusive scans (X) read at precomputed
+// counts; the identical combo (in the tie band, removed twice) is added
+// back once.
 template <typename T>
-__device__ void showdownTask(const DevTree& t, const DevRows<T>& rows, int u, int tr,
-                             int lane, const WarpScratch<T>& ws) {
+__device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, int tr,
+                             const Scratch<T>& ws) {
   const NodeDev nd = t.nodes[u];
   const StateDev& st = t.states[nd.state];
   const int opp = 1 - tr;
   const int no = st.n[opp], nt = st.n[tr];
-  const uint16_t* ord = t.poolU16 + st.sdOff[tr];
-  const uint16_t* segStart = ord + no;
-  const uint16_t* segSlot = segStart + 53;
+  const uint16_t* ord = ws.tab;
+  const uint16_t* seg = ord + no;
+  const uint16_t* segSlot = seg + 53;
   const ShowdownInfo* info = t.poolSd + st.sdInfoOff[tr];
   const RowDev ru = t.rows[u];
-  const T* r = rows.reach[tr] + (size_t)ru.reachQ[tr] * 4;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 
-  for (int c = lane; c < 53; c += 32) ws.seg[c] = segStart[c];
-  // Sorted prefix: 32-entry blocks, block prefixes accumulated compensated.
-  T runHi = T(0), runLo = T(0);
-  for (int b = 0; b <= (no >> 5); ++b) {
+  stageRow(ws.rs, rows.reach[tr] + (size_t)ru.reachQ[tr] * 4, no);
+  stageTab(ws.tab, t.poolU16 + st.sdOff[tr], 3 * no + 53);
+  __syncthreads();
+  // Block-local prefixes of the sorted reach; block totals into bh.
+  const int nb = (no >> 5) + 1;
+  for (int b = warp; b < nb; b += nw) {
     const int k = (b << 5) + lane;
-    const T v = k < no ? r[ord[k]] : T(0);
+    const T v = k < no ? ws.rs[ord[k]] : T(0);
     const T incl = warpInclScan(v, lane);
     T excl = __shfl_up_sync(0xffffffffu, incl, 1);
-    if (lane == 0) excl = T(0);
-    ws.sl[k] = excl;
-    if (lane == 0) {
-      ws.bh[b] = runHi;
-      ws.bl[b] = runLo;
-    }
-    addComp(runHi, runLo, __shfl_sync(0xffffffffu, incl, 31));
+    ws.sl[k] = lane == 0 ? T(0) : excl;
+    if (lane == 31) ws.bh[b] = incl;
   }
-  __syncwarp();
   // Card segments: X[seg[c] + c + k] = reach of the first k entries.
-  for (int c = 0; c < 52; ++c) {
-    const int s0 = ws.seg[c], len = ws.seg[c + 1] - s0;
+  for (int c = warp; c < 52; c += nw) {
+    const int s0 = seg[c], len = seg[c + 1] - s0;
     T* xo = ws.X + s0 + c;
     const int e0 = 2 * lane, e1 = e0 + 1;
-    const T v0 = e0 < len ? r[segSlot[s0 + e0]] : T(0);
-    const T v1 = e1 < len ? r[segSlot[s0 + e1]] : T(0);
+    const T v0 = e0 < len ? ws.rs[segSlot[s0 + e0]] : T(0);
+    const T v1 = e1 < len ? ws.rs[segSlot[s0 + e1]] : T(0);
     const T incl = warpInclScan(v0 + v1, lane);
     const T excl = incl - (v0 + v1);
     if (e0 <= len) xo[e0] = excl;
     if (e1 <= len) xo[e1] = excl + v0;
   }
-  __syncwarp();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T hi = T(0), lo = T(0);
+    for (int b = 0; b < nb; ++b) {
+      const T tot = ws.bh[b];
+      ws.bh[b] = hi;
+      ws.bl[b] = lo;
+      addComp(hi, lo, tot);
+    }
+  }
+  __syncthreads();
 
   const float* tv = t.termVal + ((size_t)u * 2 + tr) * 4;
   const T winV = (T)tv[0], tieV = (T)tv[1], loseV = (T)tv[2];
   T* out = rows.cfv + (size_t)ru.cfvQ * 4;
   const int nt4 = quadsOf(nt) * 4;
   const int bn = no >> 5;
-  for (int i = lane; i < nt4; i += 32) {
+  // Four combos per thread per round: their table entries are loaded first
+  // so the loads overlap.
+  for (int i0 = threadIdx.x; i0 < nt4; i0 += 4 * blockDim.x) {
+    ShowdownInfo fs[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i = i0 + j * blockDim.x;
+      if (i < nt) fs[j] = info[i];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+    const int i = i0 + j * blockDim.x;
+    if (i >= nt4) break;
     if (i >= nt) {
       out[i] = T(0);
       continue;
     }
-    const ShowdownInfo f = info[i];
+    const ShowdownInfo f = fs[j];
     const int le = f.x & 0xffff, te = f.x >> 16;
     const int c1 = f.y & 0xff, c2 = (f.y >> 8) & 0xff;
-    const int a1 = ws.seg[c1] + c1, a2 = ws.seg[c2] + c2;
-    const int len1 = ws.seg[c1 + 1] - ws.seg[c1], len2 = ws.seg[c2 + 1] - ws.seg[c2];
+    const int a1 = seg[c1] + c1, a2 = seg[c2] + c2;
+    const int len1 = seg[c1 + 1] - seg[c1], len2 = seg[c2 + 1] - seg[c2];
     const T x1le = ws.X[a1 + ((f.y >> 16) & 0xff)], x1te = ws.X[a1 + (f.y >> 24)];
     const T x2le = ws.X[a2 + (f.z & 0xff)], x2te = ws.X[a2 + ((f.z >> 8) & 0xff)];
     const int same = (int)(f.z >> 16) - 1;
-    const T sameR = same >= 0 ? r[same] : T(0);
+    const T sameR = same >= 0 ? ws.rs[same] : T(0);
     const int bl = le >> 5, bt = te >> 5;
     const T below = ws.bh[bl] + (ws.bl[bl] + ws.sl[le]);
     const T band = (ws.bh[bt] - ws.bh[bl]) + (ws.bl[bt] - ws.bl[bl]) + (ws.sl[te] - ws.sl[le]);
@@ -337,111 +386,145 @@ __device__ void showdownTask(const DevTree& t, const DevRows<T>& rows, int u, in
     tm = tm > T(0) ? tm : T(0);
     gm = gm > T(0) ? gm : T(0);
     out[i] = lm * winV + tm * tieV + gm * loseV;
+    }
   }
-  __syncwarp();
 }
 
-// Fold (one warp per node): every opponent combo not sharing a card with i
+// Fold (one CTA per node): every opponent combo not sharing a card with i
 // pays (cuda/gpu_cfr.cu:409-455); per-card sums over the card lists, one
-// card per lane, fixed order (no atomics).
+// card per thread, and a fixed-order total (no atomics).
 template <typename T>
-__device__ void foldTask(const DevTree& t, const DevRows<T>& rows, int u, int tr, int lane,
-                         const WarpScratch<T>& ws) {
+__device__ void foldNode(const DevTree& t, const DevRows<T>& rows, int u, int tr,
+                         const Scratch<T>& ws) {
   const NodeDev nd = t.nodes[u];
   const StateDev& st = t.states[nd.state];
   const int opp = 1 - tr;
   const int no = st.n[opp], nt = st.n[tr];
   const RowDev ru = t.rows[u];
-  const T* r = rows.reach[tr] + (size_t)ru.reachQ[tr] * 4;
-  const uint16_t* csr = t.poolU16 + st.csrOff[opp];
-  T* cs = ws.X;  // [52]
-  for (int c = lane; c < 52; c += 32) {
+  const uint16_t* csr = ws.tab;
+  stageRow(ws.rs, rows.reach[tr] + (size_t)ru.reachQ[tr] * 4, no);
+  stageTab(ws.tab, t.poolU16 + st.csrOff[opp], 53 + 2 * no);
+  __syncthreads();
+  T* cs = ws.X;  // [52], then the total at [52]
+  for (int c = threadIdx.x; c < 52; c += blockDim.x) {
     const int s0 = csr[c], s1 = csr[c + 1];
     T a0 = T(0), a1 = T(0);
     int e = s0;
     for (; e + 1 < s1; e += 2) {
-      a0 += r[csr[53 + e]];
-      a1 += r[csr[54 + e]];
+      a0 += ws.rs[csr[53 + e]];
+      a1 += ws.rs[csr[54 + e]];
     }
-    if (e < s1) a0 += r[csr[53 + e]];
+    if (e < s1) a0 += ws.rs[csr[53 + e]];
     cs[c] = a0 + a1;
   }
-  T part = T(0);
-  for (int j = lane; j < no; j += 32) part += r[j];
-  const T tot = warpSum(part);
-  __syncwarp();
+  if (threadIdx.x < 32) {
+    T part = T(0);
+    for (int j = threadIdx.x; j < no; j += 32) part += ws.rs[j];
+    part = warpSum(part);
+    if (threadIdx.x == 0) cs[52] = part;
+  }
+  __syncthreads();
+  const T tot = cs[52];
   const T v = (T)t.termVal[((size_t)u * 2 + tr) * 4];
-  const uint8_t* cards = t.poolU8 + st.cardsOff[tr];
+  // Card pairs as one u16 per combo (cardsOff is even).
+  const uint16_t* cards = reinterpret_cast<const uint16_t*>(t.poolU8 + st.cardsOff[tr]);
   const int16_t* same = t.poolI16 + st.sameOff[tr];
   T* out = rows.cfv + (size_t)ru.cfvQ * 4;
   const int nt4 = quadsOf(nt) * 4;
-  for (int i = lane; i < nt4; i += 32) {
-    if (i >= nt) {
-      out[i] = T(0);
-      continue;
+  for (int i0 = threadIdx.x; i0 < nt4; i0 += 4 * blockDim.x) {
+    int cp[4], sm[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i = i0 + j * blockDim.x;
+      cp[j] = i < nt ? cards[i] : 0;
+      sm[j] = i < nt ? same[i] : -1;
     }
-    T w = tot - cs[cards[2 * i]] - cs[cards[2 * i + 1]];
-    const int s = same[i];
-    if (s >= 0) w += r[s];
-    if (w < T(0)) w = T(0);
-    out[i] = w * v;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i = i0 + j * blockDim.x;
+      if (i >= nt4) break;
+      if (i >= nt) {
+        out[i] = T(0);
+        continue;
+      }
+      T w = tot - cs[cp[j] & 0xff] - cs[cp[j] >> 8];
+      if (sm[j] >= 0) w += ws.rs[sm[j]];
+      if (w < T(0)) w = T(0);
+      out[i] = w * v;
+    }
   }
-  __syncwarp();
 }
 
 // Chance chunk: the parent's value of combo i sums the children's values
 // over the branches it survives, in branch order (cuda/gpu_cfr.cu:529-555).
+// One thread per parent combo (kChanceChunk combos per task); each branch's
+// value row and slot map are resolved once per CTA into shared memory, and
+// the per-branch loads go out in batches of 8 independent loads.
 template <typename T>
 __device__ void chanceChunk(const DevTree& t, const DevRows<T>& rows, int u, int chunk,
-                            int tr, int lane) {
+                            int tr, unsigned char* smem) {
   const NodeDev nd = t.nodes[u];
   const int nb = nodeCount(nd.meta);
   const int nt = t.states[nd.state].n[tr];
-  T* out = rows.cfv + (size_t)t.rows[u].cfvQ * 4;
-  const int i0 = chunk * kChunkQuads * 4;
-  const int i1 = min(quadsOf(nt) * 4, i0 + kChunkQuads * 4);
-  for (int i = i0 + lane; i < i1; i += 32) {
-    T v = T(0);
-    if (i < nt)
-      for (int b = 0; b < nb; ++b) {
-        const int ch = t.children[nd.childBase + b];
-        const int k = t.poolI16[t.states[t.nodes[ch].state].downOff[tr] + i];
-        if (k >= 0) v += rows.cfv[(size_t)t.rows[ch].cfvQ * 4 + k];
-      }
-    out[i] = v;
+  const T** rowOf = reinterpret_cast<const T**>(smem);
+  const int16_t** downOf = reinterpret_cast<const int16_t**>(smem + 64 * sizeof(void*));
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    const int ch = t.children[nd.childBase + b];
+    rowOf[b] = rows.cfv + (size_t)t.rows[ch].cfvQ * 4;
+    downOf[b] = t.poolI16 + t.states[t.nodes[ch].state].downOff[tr];
   }
+  __syncthreads();
+  T* out = rows.cfv + (size_t)t.rows[u].cfvQ * 4;
+  const int i = chunk * kChanceChunk + (int)threadIdx.x;
+  if (i >= quadsOf(nt) * 4) return;
+  T v = T(0);
+  if (i < nt) {
+    for (int b0 = 0; b0 < nb; b0 += 8) {
+      int k[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) k[j] = b0 + j < nb ? downOf[b0 + j][i] : -1;
+      T x[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) x[j] = k[j] >= 0 ? rowOf[b0 + j][k[j]] : T(0);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v += x[j];
+    }
+  }
+  out[i] = v;
 }
 
-// Decide chunk. Opponent node: the traverser's value sums the children.
-// Traverser node, CFR: regret-matching+ strategy from the pre-update
-// regrets, the node value, then the DCFR update (cuda/gpu_cfr.cu:479-523)
+// Decide chunk, one thread per quad. Opponent node: the traverser's value
+// sums the children. Traverser node, CFR: regret-matching+ strategy from
+// the pre-update regrets, the node value, then the DCFR update
+// (cuda/gpu_cfr.cu:479-523)
 //   strat = strat * avg + sigma
 //   regret = regret * (regret >= 0 ? pos : neg) + (cfv_a - value).
 // EV: the average strategy's value. BR: the best action's value.
 template <typename T>
 __device__ void decideChunk(const DevTree& t, const DevRows<T>& rows, int u, int chunk, int tr,
-                            int mode, int lane) {
+                            int mode) {
   const NodeDev nd = t.nodes[u];
   const int na = nodeCount(nd.meta);
   const int n = t.states[nd.state].n[tr];
   const int nq = quadsOf(n);
+  const int q = chunk * kChunkQuads + (int)threadIdx.x;
+  if (q >= nq) return;
   const int* kids = t.children + nd.childBase;
   T* out = rows.cfv + (size_t)t.rows[u].cfvQ * 4;
-  const int q1 = min(nq, (chunk + 1) * kChunkQuads);
+  bool live[4];
+  for (int l = 0; l < 4; ++l) live[l] = 4 * q + l < n;
   if (nodePlayer(nd.meta) != tr || mode == kModeBR) {
     const bool best = nodePlayer(nd.meta) == tr;
-    for (int q = chunk * kChunkQuads + lane; q < q1; q += 32) {
-      T v[4];
-      for (int l = 0; l < 4; ++l) v[l] = best ? T(-1e30) : T(0);
-      for (int a = 0; a < na; ++a) {
-        T c[4];
-        ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, c);
-        for (int l = 0; l < 4; ++l) v[l] = best ? (c[l] > v[l] ? c[l] : v[l]) : v[l] + c[l];
-      }
-      for (int l = 0; l < 4; ++l)
-        if (4 * q + l >= n) v[l] = T(0);
-      stq(out + 4 * q, v);
+    T v[4];
+    for (int l = 0; l < 4; ++l) v[l] = best ? T(-1e30) : T(0);
+    for (int a = 0; a < na; ++a) {
+      T c[4];
+      ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, c);
+      for (int l = 0; l < 4; ++l) v[l] = best ? (c[l] > v[l] ? c[l] : v[l]) : v[l] + c[l];
     }
+    for (int l = 0; l < 4; ++l)
+      if (!live[l]) v[l] = T(0);
+    stq(out + 4 * q, v);
     return;
   }
   float* reg = t.regret + (size_t)nd.regQ * 4;
@@ -456,92 +539,88 @@ __device__ void decideChunk(const DevTree& t, const DevRows<T>& rows, int u, int
     neg = c[1];
     avg = c[2];
   }
-  for (int q = chunk * kChunkQuads + lane; q < q1; q += 32) {
-    bool live[4];
-    for (int l = 0; l < 4; ++l) live[l] = 4 * q + l < n;
-    T val[4] = {T(0), T(0), T(0), T(0)}, acc[4] = {T(0), T(0), T(0), T(0)};
-    if (na <= kRegNa) {
-      T x[kRegNa][4], cv[kRegNa][4];
+  T val[4] = {T(0), T(0), T(0), T(0)}, acc[4] = {T(0), T(0), T(0), T(0)};
+  if (na <= kRegNa) {
+    T x[kRegNa][4], cv[kRegNa][4];
 #pragma unroll
-      for (int a = 0; a < kRegNa; ++a)
-        if (a < na) {
-          ldqf(src + ((size_t)a * nq + q) * 4, x[a]);
-          ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, cv[a]);
-          for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[a][l], sigSrc);
-        }
-#pragma unroll
-      for (int a = 0; a < kRegNa; ++a)
-        if (a < na)
-          for (int l = 0; l < 4; ++l) {
-            x[a][l] = live[l] ? sigmaOf(x[a][l], acc[l], uniform, sigSrc) : T(0);
-            val[l] += x[a][l] * cv[a][l];
-          }
-      stq(out + 4 * q, val);
-      if (mode != kModeCFR) continue;
-#pragma unroll
-      for (int a = 0; a < kRegNa; ++a)
-        if (a < na) {
-          float rg[4], sg[4];
-          const size_t o = ((size_t)a * nq + q) * 4;
-          ldq(reg + o, rg);
-          ldq(str + o, sg);
-          for (int l = 0; l < 4; ++l) {
-            sg[l] = sg[l] * avg + (float)x[a][l];
-            rg[l] = rg[l] * (rg[l] >= 0.0f ? pos : neg) + (float)(cv[a][l] - val[l]);
-          }
-          stq(str + o, sg);
-          stq(reg + o, rg);
-        }
-    } else {
-      for (int a = 0; a < na; ++a) {
-        T x[4];
-        ldqf(src + ((size_t)a * nq + q) * 4, x);
-        for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], sigSrc);
+    for (int a = 0; a < kRegNa; ++a)
+      if (a < na) {
+        ldqf(src + ((size_t)a * nq + q) * 4, x[a]);
+        ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, cv[a]);
+        for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[a][l], sigSrc);
       }
-      for (int a = 0; a < na; ++a) {
-        T x[4], c[4];
-        ldqf(src + ((size_t)a * nq + q) * 4, x);
-        ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, c);
-        for (int l = 0; l < 4; ++l)
-          val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, sigSrc) : T(0)) * c[l];
-      }
-      stq(out + 4 * q, val);
-      if (mode != kModeCFR) continue;
-      for (int a = 0; a < na; ++a) {
+#pragma unroll
+    for (int a = 0; a < kRegNa; ++a)
+      if (a < na)
+        for (int l = 0; l < 4; ++l) {
+          x[a][l] = live[l] ? sigmaOf(x[a][l], acc[l], uniform, sigSrc) : T(0);
+          val[l] += x[a][l] * cv[a][l];
+        }
+    stq(out + 4 * q, val);
+    if (mode != kModeCFR) return;
+#pragma unroll
+    for (int a = 0; a < kRegNa; ++a)
+      if (a < na) {
         float rg[4], sg[4];
-        T c[4];
         const size_t o = ((size_t)a * nq + q) * 4;
         ldq(reg + o, rg);
         ldq(str + o, sg);
-        ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, c);
         for (int l = 0; l < 4; ++l) {
-          const T s = live[l] ? sigmaOf((T)rg[l], acc[l], uniform, 0) : T(0);
-          sg[l] = sg[l] * avg + (float)s;
-          rg[l] = rg[l] * (rg[l] >= 0.0f ? pos : neg) + (float)(c[l] - val[l]);
+          sg[l] = sg[l] * avg + (float)x[a][l];
+          rg[l] = rg[l] * (rg[l] >= 0.0f ? pos : neg) + (float)(cv[a][l] - val[l]);
         }
         stq(str + o, sg);
         stq(reg + o, rg);
       }
+    return;
+  }
+  for (int a = 0; a < na; ++a) {
+    T x[4];
+    ldqf(src + ((size_t)a * nq + q) * 4, x);
+    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], sigSrc);
+  }
+  for (int a = 0; a < na; ++a) {
+    T x[4], c[4];
+    ldqf(src + ((size_t)a * nq + q) * 4, x);
+    ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, c);
+    for (int l = 0; l < 4; ++l)
+      val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, sigSrc) : T(0)) * c[l];
+  }
+  stq(out + 4 * q, val);
+  if (mode != kModeCFR) return;
+  for (int a = 0; a < na; ++a) {
+    float rg[4], sg[4];
+    T c[4];
+    const size_t o = ((size_t)a * nq + q) * 4;
+    ldq(reg + o, rg);
+    ldq(str + o, sg);
+    ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, c);
+    for (int l = 0; l < 4; ++l) {
+      const T s = live[l] ? sigmaOf((T)rg[l], acc[l], uniform, 0) : T(0);
+      sg[l] = sg[l] * avg + (float)s;
+      rg[l] = rg[l] * (rg[l] >= 0.0f ? pos : neg) + (float)(c[l] - val[l]);
     }
+    stq(str + o, sg);
+    stq(reg + o, rg);
   }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 6)
 bwdLevelK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int count, int tr,
           int mode, int maxN) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const WarpScratch<T> ws = warpScratch<T>(smem, warp, maxN);
-  for (int i = blockIdx.x * kWarps + warp; i < count; i += gridDim.x * kWarps) {
+  const Scratch<T> ws = scratchOf<T>(smem, maxN);
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
     const int w = tasks[i];
     const int node = w >> 8, sub = (w >> 2) & 63;
     switch (w & 3) {
-      case kTaskShowdown: showdownTask<T>(t, rows, node, tr, lane, ws); break;
-      case kTaskFold: foldTask<T>(t, rows, node, tr, lane, ws); break;
-      case kTaskChance: chanceChunk<T>(t, rows, node, sub, tr, lane); break;
-      default: decideChunk<T>(t, rows, node, sub, tr, mode, lane);
+      case kTaskShowdown: showdownNode<T>(t, rows, node, tr, ws); break;
+      case kTaskFold: foldNode<T>(t, rows, node, tr, ws); break;
+      case kTaskChance: chanceChunk<T>(t, rows, node, sub, tr, smem); break;
+      default: decideChunk<T>(t, rows, node, sub, tr, mode);
     }
+    __syncthreads();  // the next task reuses the shared scratch
   }
 }
 

@@ -12,6 +12,12 @@ namespace gb {
 
 namespace {
 
+// Tables that kernels stage into shared memory start on a 16-byte boundary
+// (8 entries) so they can be copied with 16-byte vector loads.
+void alignU16(std::vector<uint16_t>& pool) {
+  while (pool.size() % 8) pool.push_back(0);
+}
+
 int appendU16(std::vector<uint16_t>& pool, const std::vector<int>& v) {
   const int off = (int)pool.size();
   for (int x : v) pool.push_back((uint16_t)x);
@@ -62,6 +68,7 @@ HostLayout buildLayout(const Tree& t) {
         L.maxCardSeg = std::max(L.maxCardSeg, (int)entries.size() - starts[c]);
       }
       starts[52] = (int)entries.size();
+      alignU16(L.poolU16);
       sd.csrOff[p] = appendU16(L.poolU16, starts);
       appendU16(L.poolU16, entries);
       std::vector<int> same(n, -1);
@@ -114,6 +121,7 @@ HostLayout buildLayout(const Tree& t) {
         for (int k : posOfCard[c]) segSlot.push_back(ord[k]);
       }
       segStart[52] = (int)segSlot.size();
+      alignU16(L.poolU16);
       sd.sdOff[tr] = appendU16(L.poolU16, ord);
       appendU16(L.poolU16, segStart);
       appendU16(L.poolU16, segSlot);
@@ -224,7 +232,8 @@ HostLayout buildLayout(const Tree& t) {
         case kShowdown: sd[nd.depth].push_back(makeTask(kTaskShowdown, 0, u)); break;
         case kFold: fd[nd.depth].push_back(makeTask(kTaskFold, 0, u)); break;
         case kChance:
-          for (int c = 0; c < chunksTr; ++c) ch[nd.depth].push_back(makeTask(kTaskChance, c, u));
+          for (int c = 0; c < (int)(quads(t.n(u, tr)) * 4 + kChanceChunk - 1) / kChanceChunk; ++c)
+            ch[nd.depth].push_back(makeTask(kTaskChance, c, u));
           for (int br = 0; br < nd.nChildren; ++br)
             L.fwdTasks[tr][nd.depth].push_back(makeTask(kTaskChance, br, u));
           break;
@@ -245,6 +254,7 @@ HostLayout buildLayout(const Tree& t) {
     }
   }
   if (N >= (1 << 24)) throw Error{PPS_GB_E_MEMORY, "tree too large for 24-bit task node ids"};
+  alignU16(L.poolU16);
   return L;
 }
 

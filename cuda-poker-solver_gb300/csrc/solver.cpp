@@ -178,9 +178,9 @@ double SolverCore::timeIterations(int n) {
   return ms;
 }
 
-std::vector<Engine::KernelStat> SolverCore::profile(int n) {
+std::vector<Engine::KernelStat> SolverCore::profile(int n, bool splitKinds) {
   extendSchedule(n);
-  auto out = eng_->profile(n);
+  auto out = eng_->profile(n, splitKinds);
   totalIters_ += n;
   iterationsRun_ = n;
   return out;

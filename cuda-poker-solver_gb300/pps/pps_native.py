@@ -419,11 +419,12 @@ class Solver:
         check(lib.pps_gb_time_iterations(self._h, int(n), C.byref(ms)))
         return ms.value
 
-    def profile(self, n: int):
-        """Per kernel class over n iterations: {name: (launches, ms, bytes)}."""
+    def profile(self, n: int, split_kinds: bool = False):
+        """Per kernel class over n iterations: {name: (launches, ms, bytes)};
+        split_kinds reports the backward pass per node kind."""
         out = (_abi.KernelStat * 16)()
         k = C.c_int()
-        check(lib.pps_gb_profile(self._h, int(n), out, 16, C.byref(k)))
+        check(lib.pps_gb_profile(self._h, int(n), int(split_kinds), out, 16, C.byref(k)))
         return {out[i].name.decode(): (int(out[i].launches), out[i].ms, out[i].algo_bytes)
                 for i in range(k.value)}
 

@@ -229,9 +229,11 @@ int pps_gb_time_iterations(pps_gb_solver* h, int n, double* ms);
 /* Profile pass (the reference's GPU_CFR_PROFILE mode, cuda/gpu_cfr.cu:
  * 1895-1987): runs n further iterations launch by launch, each launch
  * bracketed by CUDA events, and sums time and algorithmic bytes per kernel
- * class into out[cap]; *n_out = classes written. */
-int pps_gb_profile(pps_gb_solver* h, int n, pps_gb_kernel_stat* out, int cap,
-                   int* n_out);
+ * class into out[cap]; *n_out = classes written. flags bit 0: issue each
+ * backward level once per node kind (showdown / fold / chance / decide)
+ * and report the kinds separately (the reference's kindMask breakdown). */
+int pps_gb_profile(pps_gb_solver* h, int n, int flags, pps_gb_kernel_stat* out,
+                   int cap, int* n_out);
 
 /* Host-only compile (no device use): runs the tree compiler and reports
  * every artifact in the reference's own layout (cuda/gpu_cfr.cu:1331-1827)
