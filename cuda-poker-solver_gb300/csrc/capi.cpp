@@ -10,6 +10,7 @@
 
 #include "compiler.h"
 #include "engine.h"
+#include "noalloc.h"
 #include "solver.h"
 
 using pps::gb::Error;
@@ -420,6 +421,18 @@ int pps_gb_profile(pps_gb_solver* h, int n, int flags, pps_gb_kernel_stat* out, 
       out[i].ms = stats[i].ms;
       out[i].algo_bytes = stats[i].bytes;
     }
+  });
+}
+
+int pps_gb_solve_noalloc(const pps_gb_spot* spot, const pps_gb_bet_config* cfg,
+                         float* d_regret, float* d_strat, int64_t row_capacity,
+                         int first_iteration, int iterations, void* stream, int64_t* n_rows) {
+  return guarded([&] {
+    if (!spot || !cfg) throw Error{PPS_GB_E_ARG, "null argument"};
+    const int64_t n = pps::gb::noallocSolve(toSpot(*spot), toConfig(*cfg), d_regret, d_strat,
+                                            row_capacity, first_iteration, iterations,
+                                            static_cast<cudaStream_t>(stream));
+    if (n_rows) *n_rows = n;
   });
 }
 

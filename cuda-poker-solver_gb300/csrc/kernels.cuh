@@ -624,7 +624,8 @@ bwdLevelK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int count, 
   }
 }
 
-__global__ void advanceCounterK(int* counter) {
+// Internal linkage: this header is included by more than one translation unit.
+static __global__ void advanceCounterK(int* counter) {
   if (threadIdx.x == 0 && blockIdx.x == 0) ++(*counter);
 }
 

@@ -1,0 +1,252 @@
+// No-allocation DCFR solve over caller-owned rows (pps_gb_solve_noalloc in
+// include/pps_gb.h).
+//
+// For callers that cannot call cudaMalloc (their device memory belongs to
+// another allocator, or they must avoid cudaMalloc's implicit
+// synchronization): the caller passes its regret and strategy rows; every
+// other device buffer of the solve - tree tables, task lists, reach and
+// value rows, the schedule - is carved out of gNoAllocScratch, one
+// file-scope static device array of PPS_GB_NOALLOC_SCRATCH_BYTES. Nothing
+// here allocates device memory.
+//
+// Host code never dereferences or passes gNoAllocScratch itself: on the
+// host that name is a stand-in, not a device address. Its device address is
+// looked up once per device with cudaGetSymbolAddress (with that device
+// current) and kept; the first call on a device does this set-up, so it
+// should come before any stream capture. All calls share the array and leave
+// their contents in it; every buffer a call reads is written by that call
+// first (or cleared), and calls that overlap on a GPU race on it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "compiler.h"
+#include "kernels.cuh"
+#include "layout.h"
+#include "noalloc.h"
+#include "pps_gb.h"
+#include "solver.h"
+
+namespace pps {
+namespace gb {
+
+static __device__ __align__(256) unsigned char gNoAllocScratch[PPS_GB_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+#define NA_CK(call)                                                          \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      throw Error{PPS_GB_E_CUDA, std::string("CUDA error: ") +               \
+                                     cudaGetErrorString(e_) + " (" #call ")"}; \
+  } while (0)
+
+constexpr int kMaxDevices = 128;
+std::mutex gSetupMutex;
+unsigned char* gScratchOnDevice[kMaxDevices] = {};
+
+// Device address of gNoAllocScratch on the current device (set up once).
+unsigned char* scratchBase() {
+  int dev = 0;
+  NA_CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) throw Error{PPS_GB_E_CUDA, "device index out of range"};
+  std::lock_guard<std::mutex> lock(gSetupMutex);
+  if (!gScratchOnDevice[dev]) {
+    void* p = nullptr;
+    NA_CK(cudaGetSymbolAddress(&p, gNoAllocScratch));
+    gScratchOnDevice[dev] = static_cast<unsigned char*>(p);
+  }
+  return gScratchOnDevice[dev];
+}
+
+// Per decide node: where its rows sit in the caller's dense layout and in
+// the padded scratch layout.
+struct RowMap {
+  int dense;     // first dense entry
+  uint32_t padQ; // first padded quad
+  int na;
+  int n;
+};
+
+// Copies rows between the caller's dense layout and the padded layout the
+// kernels use (toPadded: dense -> padded); padding lanes are left as set.
+__global__ void repackK(const RowMap* __restrict__ map, int count, const float* src, float* dst,
+                        int toPadded) {
+  for (int k = blockIdx.x; k < count; k += gridDim.x) {
+    const RowMap m = map[k];
+    const int stride = quadsOf(m.n) * 4;
+    for (int e = threadIdx.x; e < m.na * m.n; e += blockDim.x) {
+      const int a = e / m.n, c = e - a * m.n;
+      const size_t pad = (size_t)m.padQ * 4 + (size_t)a * stride + c;
+      const size_t dense = (size_t)m.dense + e;
+      if (toPadded) dst[pad] = src[dense];
+      else dst[dense] = src[pad];
+    }
+  }
+}
+
+struct Arena {
+  size_t used = 0;
+  size_t take(size_t bytes) {
+    const size_t off = used;
+    used += (bytes + 255) / 256 * 256;
+    return off;
+  }
+};
+
+}  // namespace
+
+int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, float* dRegret,
+                     float* dStrat, int64_t rowCapacity, int firstIteration, int iterations,
+                     cudaStream_t stream) {
+  if (firstIteration < 0 || iterations < 0 ||
+      (int64_t)firstIteration + iterations > (int64_t)INT_MAX)
+    throw Error{PPS_GB_E_ARG, "bad iteration range"};
+  gpu::StreetBetConfigs cfgs;
+  cfgs.street[0] = cfgs.street[1] = cfgs.street[2] = cfg;
+  const Tree t = compileTree(spot, cfgs, false);
+  if (t.empty) throw Error{PPS_GB_E_STATE, "solver compiled to empty ranges"};
+  if (t.rowTotal > (int64_t)INT_MAX) throw Error{PPS_GB_E_BUDGET, "row table too large"};
+  if (!dRegret || !dStrat) throw Error{PPS_GB_E_ARG, "null row buffer"};
+  if (rowCapacity < t.rowTotal)
+    throw Error{PPS_GB_E_ARG, "row buffers hold " + std::to_string(rowCapacity) +
+                                  " floats; the spot needs " + std::to_string(t.rowTotal)};
+  const HostLayout L = buildLayout(t);
+
+  // Task lists (as the engine concatenates them) and the row map.
+  std::vector<int> tasks;
+  const int D = (int)L.bwdTasks[0].size();
+  std::vector<std::pair<int, int>> fwd[2], bwd[2];
+  for (int tr = 0; tr < 2; ++tr)
+    for (int d = 0; d < D; ++d) {
+      fwd[tr].push_back({(int)tasks.size(), (int)L.fwdTasks[tr][d].size()});
+      tasks.insert(tasks.end(), L.fwdTasks[tr][d].begin(), L.fwdTasks[tr][d].end());
+      bwd[tr].push_back({(int)tasks.size(), (int)L.bwdTasks[tr][d].size()});
+      tasks.insert(tasks.end(), L.bwdTasks[tr][d].begin(), L.bwdTasks[tr][d].end());
+    }
+  std::vector<RowMap> rowMap;
+  int dense = 0;
+  for (int u : t.decideNodes) {
+    const Node& nd = t.nodes[u];
+    const int n = t.n(u, nd.player);
+    rowMap.push_back({dense, L.nodes[u].regQ, nd.na, n});
+    dense += nd.na * n;
+  }
+  std::vector<float> coef((size_t)(firstIteration + iterations) * 3 + 3, 0.0f);
+  Schedule sched;
+  for (int k = 0; k < firstIteration + iterations; ++k) {
+    double c[3];
+    sched.coefs(k, firstIteration + iterations, c);
+    for (int j = 0; j < 3; ++j) coef[(size_t)k * 3 + j] = (float)c[j];
+  }
+  std::vector<float> rootReach[2];
+  for (int tr = 0; tr < 2; ++tr) {
+    const Side& opp = t.side[1 - tr];
+    rootReach[tr].assign(quads(opp.n) * 4, 0.0f);
+    for (int j = 0; j < opp.n; ++j) rootReach[tr][j] = (float)opp.w[j];
+  }
+
+  // Scratch plan.
+  Arena A;
+  auto bytesOf = [](const auto& v) { return v.size() * sizeof(v[0]); };
+  const size_t oNodes = A.take(bytesOf(L.nodes)), oRows = A.take(bytesOf(L.rows)),
+               oTerm = A.take(bytesOf(L.termVal)), oKids = A.take(bytesOf(L.children)),
+               oStates = A.take(bytesOf(L.states)), oU8 = A.take(bytesOf(L.poolU8)),
+               oU16 = A.take(bytesOf(L.poolU16)), oI16 = A.take(bytesOf(L.poolI16)),
+               oSd = A.take(bytesOf(L.poolSd)), oTasks = A.take(bytesOf(tasks)),
+               oMap = A.take(bytesOf(rowMap)), oReg = A.take(L.regQuads * 16),
+               oStr = A.take(L.regQuads * 16), oCfv = A.take(L.cfvQuads * 16),
+               oReach0 = A.take(L.reachQuads[0] * 16), oReach1 = A.take(L.reachQuads[1] * 16),
+               oCoef = A.take(bytesOf(coef)), oCounter = A.take(sizeof(int));
+  if (A.used > (size_t)PPS_GB_NOALLOC_SCRATCH_BYTES)
+    throw Error{PPS_GB_E_BUDGET, "spot needs " + std::to_string(A.used) +
+                                     " bytes of scratch; the static scratch holds " +
+                                     std::to_string((size_t)PPS_GB_NOALLOC_SCRATCH_BYTES)};
+
+  unsigned char* base = scratchBase();
+  auto put = [&](size_t off, const auto& v) {
+    if (!v.empty())
+      NA_CK(cudaMemcpyAsync(base + off, v.data(), bytesOf(v), cudaMemcpyHostToDevice, stream));
+  };
+  put(oNodes, L.nodes);
+  put(oRows, L.rows);
+  put(oTerm, L.termVal);
+  put(oKids, L.children);
+  put(oStates, L.states);
+  put(oU8, L.poolU8);
+  put(oU16, L.poolU16);
+  put(oI16, L.poolI16);
+  put(oSd, L.poolSd);
+  put(oTasks, tasks);
+  put(oMap, rowMap);
+  put(oCoef, coef);
+  put(oReach0, rootReach[0]);
+  put(oReach1, rootReach[1]);
+  NA_CK(cudaMemcpyAsync(base + oCounter, &firstIteration, sizeof(int), cudaMemcpyHostToDevice,
+                        stream));
+  // Padded rows start from zero (padding lanes must stay zero), then take
+  // the caller's values.
+  NA_CK(cudaMemsetAsync(base + oReg, 0, L.regQuads * 16, stream));
+  NA_CK(cudaMemsetAsync(base + oStr, 0, L.regQuads * 16, stream));
+  float* reg = reinterpret_cast<float*>(base + oReg);
+  float* str = reinterpret_cast<float*>(base + oStr);
+  const RowMap* map = reinterpret_cast<const RowMap*>(base + oMap);
+  const int nMap = (int)rowMap.size();
+  const unsigned gMap = (unsigned)std::min(nMap, 1 << 20);
+  repackK<<<gMap, 128, 0, stream>>>(map, nMap, dRegret, reg, 1);
+  repackK<<<gMap, 128, 0, stream>>>(map, nMap, dStrat, str, 1);
+
+  DevTree tree{};
+  tree.nodes = reinterpret_cast<const NodeDev*>(base + oNodes);
+  tree.rows = reinterpret_cast<const RowDev*>(base + oRows);
+  tree.termVal = reinterpret_cast<const float*>(base + oTerm);
+  tree.children = reinterpret_cast<const int*>(base + oKids);
+  tree.states = reinterpret_cast<const StateDev*>(base + oStates);
+  tree.poolU8 = base + oU8;
+  tree.poolU16 = reinterpret_cast<const uint16_t*>(base + oU16);
+  tree.poolI16 = reinterpret_cast<const int16_t*>(base + oI16);
+  tree.poolSd = reinterpret_cast<const ShowdownInfo*>(base + oSd);
+  tree.regret = reg;
+  tree.strat = str;
+  tree.coef = reinterpret_cast<const float*>(base + oCoef);
+  int* counter = reinterpret_cast<int*>(base + oCounter);
+  tree.counter = counter;
+  DevRows<float> rows{};
+  rows.reach[0] = reinterpret_cast<float*>(base + oReach0);
+  rows.reach[1] = reinterpret_cast<float*>(base + oReach1);
+  rows.cfv = reinterpret_cast<float*>(base + oCfv);
+  const int* dTasks = reinterpret_cast<const int*>(base + oTasks);
+
+  const size_t smem = bwdScratchBytes<float>(L.maxN);
+  NA_CK(cudaFuncSetAttribute(bwdLevelK<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem));
+  auto grid = [](int count) { return (unsigned)std::min(count, 1 << 20); };
+  for (int it = 0; it < iterations; ++it) {
+    for (int tr = 0; tr < 2; ++tr) {
+      for (int d = 0; d < D; ++d)
+        if (fwd[tr][d].second)
+          fwdLevelK<float><<<grid(fwd[tr][d].second), kThreads, 0, stream>>>(
+              tree, rows, dTasks + fwd[tr][d].first, fwd[tr][d].second, tr, 0);
+      for (int d = D - 1; d >= 0; --d)
+        if (bwd[tr][d].second)
+          bwdLevelK<float><<<grid(bwd[tr][d].second), kThreads, smem, stream>>>(
+              tree, rows, dTasks + bwd[tr][d].first, bwd[tr][d].second, tr, kModeCFR, L.maxN);
+    }
+    advanceCounterK<<<1, 32, 0, stream>>>(counter);
+    NA_CK(cudaGetLastError());
+  }
+  repackK<<<gMap, 128, 0, stream>>>(map, nMap, reg, dRegret, 0);
+  repackK<<<gMap, 128, 0, stream>>>(map, nMap, str, dStrat, 0);
+  NA_CK(cudaGetLastError());
+  NA_CK(cudaStreamSynchronize(stream));
+  return t.rowTotal;
+}
+
+}  // namespace gb
+}  // namespace pps

@@ -104,6 +104,8 @@ _SIGS = {
     "pps_gb_set_engine": (C.c_int, [H, C.c_int]),
     "pps_gb_time_iterations": (C.c_int, [H, C.c_int, P(C.c_double)]),
     "pps_gb_profile": (C.c_int, [H, C.c_int, C.c_int, P(KernelStat), C.c_int, P(C.c_int)]),
+    "pps_gb_solve_noalloc": (C.c_int, [P(Spot), P(BetConfig), C.c_void_p, C.c_void_p, C.c_int64,
+                                       C.c_int, C.c_int, C.c_void_p, P(C.c_int64)]),
     "pps_gb_compile_export": (C.c_int, [P(Spot), P(BetConfig), C.c_int, ARRAY_CB, C.c_void_p]),
     "pps_gb_hand_keys": (C.c_int, [P(C.c_uint8), C.c_int, P(C.c_uint64)]),
     "pps_gb_bet_actions": (C.c_int, [C.c_int64, C.c_int64, P(BetConfig), C.c_int64, C.c_int64,

@@ -235,6 +235,36 @@ int pps_gb_time_iterations(pps_gb_solver* h, int n, double* ms);
 int pps_gb_profile(pps_gb_solver* h, int n, int flags, pps_gb_kernel_stat* out,
                    int cap, int* n_out);
 
+/* Size in bytes of the static device array behind pps_gb_solve_noalloc. */
+#define PPS_GB_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+/* No-allocation solve. No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc - processes whose device memory is
+ * owned by another allocator (a framework's caching allocator holding the
+ * GPU, a fixed budget carved out at start-up) and callers that must not
+ * trigger cudaMalloc's implicit device-wide synchronization.
+ *
+ * Runs `iterations` DCFR iterations (the "dcfr" schedule, absolute indices
+ * first_iteration .. first_iteration + iterations - 1) of the spot over the
+ * caller's cumulative regret and strategy rows: device memory in the
+ * reference's dense layout (see pps_gb_read_rows), row_capacity floats
+ * each, read at entry and written back at exit. Every other device buffer
+ * (tree tables, reach and value rows, schedule) lives in ONE static device
+ * array of PPS_GB_NOALLOC_SCRATCH_BYTES (64 MiB), held by every GPU that
+ * loads the library until the process exits; spots that need more are
+ * rejected with PPS_GB_E_BUDGET and a message giving both sizes. The call
+ * allocates no device memory (no cudaMalloc, cudaFree or allocating library
+ * routine), issues its work on `stream` (NULL: the legacy default stream)
+ * and waits for it. The first call on a device looks up the array's device
+ * address with cudaGetSymbolAddress; make that first call before any stream
+ * capture. All calls share the array and leave their contents in it: calls
+ * that overlap on a GPU (other threads or streams) race - serialize them.
+ * *n_rows receives the row count the spot needs. */
+int pps_gb_solve_noalloc(const pps_gb_spot* spot, const pps_gb_bet_config* cfg,
+                         float* d_regret, float* d_strat, int64_t row_capacity,
+                         int first_iteration, int iterations, void* stream,
+                         int64_t* n_rows);
+
 /* Host-only compile (no device use): runs the tree compiler and reports
  * every artifact in the reference's own layout (cuda/gpu_cfr.cu:1331-1827)
  * through cb(user, name, dtype, data, count); dtype 'i' int32, 'q' int64,
