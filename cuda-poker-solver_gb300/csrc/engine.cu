@@ -41,20 +41,24 @@ V* alloc(size_t count, size_t& bytes) {
   return p;
 }
 
-enum LaunchKind { kFwd, kBwd, kLeafSweep, kCounter };
-const char* kLaunchName[] = {"fwd_level", "bwd_level", "leaf_street", "counter"};
+enum LaunchKind { kFwd, kBwd, kBwdTerm, kBwdInt, kLeafSweep, kCounter };
+const char* kLaunchName[] = {"fwd_level", "bwd_level", "bwd_terminal", "bwd_interior",
+                             "leaf_street", "counter"};
 
 struct Launch {
   LaunchKind kind;
   int tr;
   ListRef list;
-  double bytes;  // algorithmic bytes of this launch (f32 rows)
+  double bytes;           // algorithmic bytes of this launch (f32 rows)
+  bool withNext = false;  // independent of the next launch: run both at once
 };
 
 }  // namespace
 
 struct Engine::Dev {
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;                  // second graph branch
+  cudaEvent_t fork = nullptr, join = nullptr;  // branch fork / join
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<void*> owned;
@@ -95,23 +99,50 @@ V* upload(Engine::Dev& d, const std::vector<V>& v, size_t& bytes, int64_t& h2d) 
 
 unsigned gridOf(int count) { return (unsigned)std::min(count, 1 << 20); }
 
-// Issues one planned launch on the engine stream (CFR mode, f32 rows).
-void issue(Engine::Dev& d, const Launch& l) {
+// Issues one planned launch (CFR mode, f32 rows) on stream s.
+void issue(Engine::Dev& d, const Launch& l, cudaStream_t s) {
+  const unsigned g = gridOf(l.list.count);
+  const int* tk = d.tasks + l.list.off;
   switch (l.kind) {
     case kFwd:
-      fwdLevelK<float><<<gridOf(l.list.count), kThreads, 0, d.stream>>>(
-          d.tree, d.rowsF, d.tasks + l.list.off, l.list.count, l.tr, 0);
+      fwdLevelK<float><<<g, kThreads, 0, s>>>(d.tree, d.rowsF, tk, l.list.count, l.tr, 0);
       break;
     case kBwd:
-      bwdLevelK<float><<<gridOf(l.list.count), kThreads, d.smemF, d.stream>>>(
-          d.tree, d.rowsF, d.tasks + l.list.off, l.list.count, l.tr, kModeCFR, d.maxN);
+      bwdLevelK<float><<<g, kThreads, d.smemF, s>>>(d.tree, d.rowsF, tk, l.list.count, l.tr,
+                                                    kModeCFR, d.maxN);
+      break;
+    case kBwdTerm:
+      bwdTerminalK<float><<<g, kThreads, d.smemF, s>>>(d.tree, d.rowsF, tk, l.list.count, l.tr,
+                                                       d.maxN);
+      break;
+    case kBwdInt:
+      bwdInteriorK<float><<<g, kThreads, 0, s>>>(d.tree, d.rowsF, tk, l.list.count, l.tr,
+                                                 kModeCFR);
       break;
     case kLeafSweep:
-      launchLeaf(d.leaf, d.tree, d.rowsF, l.tr, d.stream);
+      launchLeaf(d.leaf, d.tree, d.rowsF, l.tr, s);
       break;
     case kCounter:
-      advanceCounterK<<<1, 32, 0, d.stream>>>(d.counter);
+      advanceCounterK<<<1, 32, 0, s>>>(d.counter);
       break;
+  }
+}
+
+// Issues a plan; launches marked withNext run on a side branch forked from
+// and joined back into the main stream (graph branches under capture).
+void issuePlan(Engine::Dev& d, const std::vector<Launch>& P) {
+  for (size_t i = 0; i < P.size(); ++i) {
+    if (P[i].withNext && i + 1 < P.size()) {
+      GB_CK(cudaEventRecord(d.fork, d.stream));
+      GB_CK(cudaStreamWaitEvent(d.side, d.fork, 0));
+      issue(d, P[i], d.stream);
+      issue(d, P[i + 1], d.side);
+      GB_CK(cudaEventRecord(d.join, d.side));
+      GB_CK(cudaStreamWaitEvent(d.stream, d.join, 0));
+      ++i;
+    } else {
+      issue(d, P[i], d.stream);
+    }
   }
 }
 
@@ -122,6 +153,9 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
   Dev& d = *d_;
   size_t& B = deviceBytes_;
   GB_CK(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
+  GB_CK(cudaStreamCreateWithFlags(&d.side, cudaStreamNonBlocking));
+  GB_CK(cudaEventCreateWithFlags(&d.fork, cudaEventDisableTiming));
+  GB_CK(cudaEventCreateWithFlags(&d.join, cudaEventDisableTiming));
   d.tree.nodes = upload(d, L_.nodes, B, h2d_);
   d.tree.rows = upload(d, L_.rows, B, h2d_);
   d.tree.termVal = upload(d, L_.termVal, B, h2d_);
@@ -177,6 +211,8 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
                              (int)d.smemF));
   GB_CK(cudaFuncSetAttribute(bwdLevelK<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)d.smemD));
+  GB_CK(cudaFuncSetAttribute(bwdTerminalK<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)d.smemF));
   if (d.leaf.ok) GB_CK(prepareLeaf(d.leaf));
   buildPlans();
   engineKind_ = d.leaf.ok ? 1 : 0;
@@ -190,6 +226,9 @@ Engine::~Engine() {
   if (d_->stream) cudaStreamSynchronize(d_->stream);
   for (void* p : d_->owned) cudaFree(p);
   if (d_->stream) cudaStreamDestroy(d_->stream);
+  if (d_->side) cudaStreamDestroy(d_->side);
+  if (d_->fork) cudaEventDestroy(d_->fork);
+  if (d_->join) cudaEventDestroy(d_->join);
 }
 
 void* Engine::stream() const { return (void*)d_->stream; }
@@ -248,8 +287,24 @@ void Engine::buildPlans() {
       for (int dd = 0; dd < (int)fr.size(); ++dd)
         if (fr[dd].count) P.push_back({kFwd, tr, fr[dd], listBytes(fw[dd], tr, true)});
       if (leaf) P.push_back({kLeafSweep, tr, ListRef{}, d.leaf.algoBytes[tr]});
-      for (int dd = (int)brf.size() - 1; dd >= 0; --dd)
-        if (brf[dd].count) P.push_back({kBwd, tr, brf[dd], listBytes(bw[dd], tr, false)});
+      for (int dd = (int)brf.size() - 1; dd >= 0; --dd) {
+        if (!brf[dd].count) continue;
+        if (leaf) {
+          P.push_back({kBwd, tr, brf[dd], listBytes(bw[dd], tr, false)});
+          continue;
+        }
+        // The list is sorted showdown, fold, chance, decide: terminal tasks
+        // (kinds 2-3) lead. Terminals read only the traverser's reach row and
+        // write their own cfv rows; interior tasks read child cfv rows of
+        // deeper levels, so both halves of a level run at once.
+        const std::vector<int>& v = bw[dd];
+        int nt = 0;
+        while (nt < (int)v.size() && (v[nt] & 3) >= 2) ++nt;
+        const std::vector<int> vt(v.begin(), v.begin() + nt), vi(v.begin() + nt, v.end());
+        const ListRef lt{brf[dd].off, nt}, li{brf[dd].off + nt, brf[dd].count - nt};
+        if (nt) P.push_back({kBwdTerm, tr, lt, listBytes(vt, tr, false), li.count > 0});
+        if (li.count) P.push_back({kBwdInt, tr, li, listBytes(vi, tr, false)});
+      }
     }
     P.push_back({kCounter, 0, ListRef{}, 0.0});
   }
@@ -310,10 +365,8 @@ void Engine::capture() {
   const std::vector<Launch>& P = d.plan[engineKind_];
   GB_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t launchErr = cudaSuccess;
-  for (const Launch& l : P) {
-    issue(d, l);
-    if (launchErr == cudaSuccess) launchErr = cudaGetLastError();
-  }
+  issuePlan(d, P);
+  launchErr = cudaGetLastError();
   cudaGraph_t g = nullptr;
   const cudaError_t endErr = cudaStreamEndCapture(d.stream, &g);
   if (launchErr != cudaSuccess || endErr != cudaSuccess) {
@@ -365,7 +418,8 @@ std::vector<Engine::KernelStat> Engine::profile(int n, bool splitKinds) {
   static const char* kKindName[] = {"bwd_decide", "bwd_chance", "bwd_fold", "bwd_showdown"};
   std::vector<std::pair<Launch, std::string>> P;
   for (const Launch& l : d.plan[engineKind_]) {
-    if (l.kind != kBwd || !splitKinds) {
+    const bool bwd = l.kind == kBwd || l.kind == kBwdTerm || l.kind == kBwdInt;
+    if (!bwd || !splitKinds) {
       P.push_back({l, kLaunchName[l.kind]});
       continue;
     }
@@ -376,7 +430,7 @@ std::vector<Engine::KernelStat> Engine::profile(int n, bool splitKinds) {
       int j = i;
       double bytes = 0;
       while (j < end && (d.hostTasks[j] & 3) == kind) bytes += taskBytes(d.hostTasks[j++], l.tr, false);
-      P.push_back({Launch{kBwd, l.tr, ListRef{i, j - i}, bytes}, kKindName[kind]});
+      P.push_back({Launch{l.kind, l.tr, ListRef{i, j - i}, bytes}, kKindName[kind]});
       i = j;
     }
   }
@@ -386,7 +440,7 @@ std::vector<Engine::KernelStat> Engine::profile(int n, bool splitKinds) {
   for (int it = 0; it < n; ++it)
     for (const auto& pl : P) {
       GB_CK(cudaEventRecord(ev[k++], d.stream));
-      issue(d, pl.first);
+      issue(d, pl.first, d.stream);
       GB_CK(cudaGetLastError());
       GB_CK(cudaEventRecord(ev[k++], d.stream));
     }

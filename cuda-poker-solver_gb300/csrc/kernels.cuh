@@ -128,6 +128,16 @@ __device__ __forceinline__ void addComp(T& hi, T& lo, T b) {
   lo = e - (hi - s);
 }
 
+// (hi, lo) += (bh, bl), renormalized (double-word addition).
+template <typename T>
+__device__ __forceinline__ void addPair(T& hi, T& lo, T bh, T bl) {
+  T s, e;
+  twoSum(hi, bh, s, e);
+  e += lo + bl;
+  hi = s + e;
+  lo = e - (hi - s);
+}
+
 // ---------------------------------------------------------------------------
 // Forward pass (one launch per depth level; one CTA per task).
 // ---------------------------------------------------------------------------
@@ -333,13 +343,33 @@ __device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, in
     if (e1 <= len) xo[e1] = excl + v0;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    T hi = T(0), lo = T(0);
-    for (int b = 0; b < nb; ++b) {
-      const T tot = ws.bh[b];
-      ws.bh[b] = hi;
-      ws.bl[b] = lo;
-      addComp(hi, lo, tot);
+  // Compensated exclusive prefix of the block totals (nb <= 64: two blocks
+  // per lane of warp 0).
+  if (warp == 0) {
+    const int b0 = 2 * lane, b1 = b0 + 1;
+    const T t0 = b0 < nb ? ws.bh[b0] : T(0), t1 = b1 < nb ? ws.bh[b1] : T(0);
+    T hi = t0, lo = T(0);
+    addComp(hi, lo, t1);
+    for (int off = 1; off < 32; off <<= 1) {
+      const T oh = __shfl_up_sync(0xffffffffu, hi, off);
+      const T ol = __shfl_up_sync(0xffffffffu, lo, off);
+      if (lane >= off) {
+        T h = oh, l = ol;
+        addPair(h, l, hi, lo);
+        hi = h;
+        lo = l;
+      }
+    }
+    T eh = __shfl_up_sync(0xffffffffu, hi, 1), el = __shfl_up_sync(0xffffffffu, lo, 1);
+    if (lane == 0) eh = el = T(0);
+    if (b0 < nb) {
+      ws.bh[b0] = eh;
+      ws.bl[b0] = el;
+    }
+    addComp(eh, el, t0);
+    if (b1 < nb) {
+      ws.bh[b1] = eh;
+      ws.bl[b1] = el;
     }
   }
   __syncthreads();
@@ -406,22 +436,21 @@ __device__ void foldNode(const DevTree& t, const DevRows<T>& rows, int u, int tr
   stageTab(ws.tab, t.poolU16 + st.csrOff[opp], 53 + 2 * no);
   __syncthreads();
   T* cs = ws.X;  // [52], then the total at [52]
-  for (int c = threadIdx.x; c < 52; c += blockDim.x) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // One warp per card: lanes sum the card's list entries, then a fixed
+  // shuffle tree (card lists hold at most 51 combos: two entries per lane).
+  for (int c = warp; c < 52; c += nw) {
     const int s0 = csr[c], s1 = csr[c + 1];
-    T a0 = T(0), a1 = T(0);
-    int e = s0;
-    for (; e + 1 < s1; e += 2) {
-      a0 += ws.rs[csr[53 + e]];
-      a1 += ws.rs[csr[54 + e]];
-    }
-    if (e < s1) a0 += ws.rs[csr[53 + e]];
-    cs[c] = a0 + a1;
+    T a = T(0);
+    for (int e = s0 + lane; e < s1; e += 32) a += ws.rs[csr[53 + e]];
+    a = warpSum(a);
+    if (lane == 0) cs[c] = a;
   }
-  if (threadIdx.x < 32) {
+  if (warp == nw - 1) {
     T part = T(0);
-    for (int j = threadIdx.x; j < no; j += 32) part += ws.rs[j];
+    for (int j = lane; j < no; j += 32) part += ws.rs[j];
     part = warpSum(part);
-    if (threadIdx.x == 0) cs[52] = part;
+    if (lane == 0) cs[52] = part;
   }
   __syncthreads();
   const T tot = cs[52];
@@ -621,6 +650,39 @@ bwdLevelK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int count, 
       default: decideChunk<T>(t, rows, node, sub, tr, mode);
     }
     __syncthreads();  // the next task reuses the shared scratch
+  }
+}
+
+// The same level split in two: terminal tasks (showdown, fold: shared
+// scratch, 6 CTAs per SM) and interior tasks (decide, chance: 1 KB of
+// shared memory, 8 CTAs per SM, memory-latency bound). The two halves of a
+// level are independent and run concurrently (graph branches); the
+// per-node arithmetic is bwdLevelK's.
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 6)
+bwdTerminalK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int count, int tr,
+             int maxN) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Scratch<T> ws = scratchOf<T>(smem, maxN);
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
+    const int w = tasks[i];
+    if ((w & 3) == kTaskShowdown) showdownNode<T>(t, rows, w >> 8, tr, ws);
+    else foldNode<T>(t, rows, w >> 8, tr, ws);
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 8)
+bwdInteriorK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int count, int tr,
+             int mode) {
+  __shared__ __align__(16) unsigned char smem[kChanceScratchBytes];
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
+    const int w = tasks[i];
+    const int node = w >> 8, sub = (w >> 2) & 63;
+    if ((w & 3) == kTaskChance) chanceChunk<T>(t, rows, node, sub, tr, smem);
+    else decideChunk<T>(t, rows, node, sub, tr, mode);
+    __syncthreads();
   }
 }
 
