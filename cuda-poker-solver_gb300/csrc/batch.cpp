@@ -1,0 +1,420 @@
+// Batched and served solving (see batch.h).
+#include "batch.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+
+#include "layout.h"
+#include "pps_gb.h"
+#include "solver.h"
+
+namespace pps {
+namespace gb {
+
+namespace {
+
+void cudaCheck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess)
+    throw Error{e == cudaErrorMemoryAllocation ? PPS_GB_E_MEMORY : PPS_GB_E_CUDA,
+                std::string("CUDA error: ") + cudaGetErrorString(e) + " (" + what + ")"};
+}
+
+std::vector<float> scheduleTable(const Schedule& s, int entries) {
+  std::vector<float> tab((size_t)entries * 3);
+  for (int t = 0; t < entries; ++t) {
+    double c[3];
+    s.coefs(t, entries, c);
+    for (int k = 0; k < 3; ++k) tab[(size_t)t * 3 + k] = (float)c[k];
+  }
+  return tab;
+}
+
+}  // namespace
+
+BatchServer::BatchServer(const BatchConfig& cfg) : cfg_(cfg), t0_(std::chrono::steady_clock::now()) {
+  Schedule s;
+  if (!Schedule::parse(cfg_.algo, s) || s.hs30)
+    throw Error{PPS_GB_E_ARG, "batch: algo must be a DCFR schedule (dcfr, dcfr-g2, "
+                              "dcfr-noreset, dcfr-g2-noreset), got '" + cfg_.algo + "'"};
+  if (cfg_.checkEvery <= 0) cfg_.checkEvery = 64;
+  if (cfg_.maxIterations <= 0) cfg_.maxIterations = 4096;
+  cfg_.maxIterations =
+      (cfg_.maxIterations + cfg_.checkEvery - 1) / cfg_.checkEvery * cfg_.checkEvery;
+  cudaCheck(cudaGetDevice(&device_), "cudaGetDevice");
+  budget_ = cfg_.budget;
+  if (budget_ <= 0) {
+    size_t freeB = 0, totalB = 0;
+    cudaCheck(cudaMemGetInfo(&freeB, &totalB), "cudaMemGetInfo");
+    budget_ = (int64_t)(0.8 * (double)freeB);
+  }
+  forest_.reset(new Forest(scheduleTable(s, cfg_.maxIterations)));
+  stats_.checkEvery = cfg_.checkEvery;
+  stats_.maxIterations = cfg_.maxIterations;
+  int n = cfg_.threads;
+  if (n <= 0) n = std::min(16, std::max(1, (int)std::thread::hardware_concurrency()));
+  for (int i = 0; i < n; ++i) compilers_.emplace_back([this] { compileLoop(); });
+}
+
+BatchServer::~BatchServer() {
+  stop();
+  {
+    std::lock_guard<std::mutex> lock(m_);
+    closing_ = true;
+  }
+  cvCompile_.notify_all();
+  for (auto& t : compilers_) t.join();
+}
+
+double BatchServer::nowMs() const {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0_)
+      .count();
+}
+
+int64_t BatchServer::submit(const gpu::PostflopSpot& spot, const gpu::StreetBetConfigs& cfgs,
+                            bool perStreet, double target) {
+  std::lock_guard<std::mutex> lock(m_);
+  const int64_t ticket = nextTicket_++;
+  Request& r = reqs_[ticket];
+  r.spot = spot;
+  r.cfgs = cfgs;
+  r.perStreet = perStreet;
+  r.target = target;
+  r.result.ticket = ticket;
+  r.result.target = target;
+  r.result.submitMs = nowMs();
+  compileQueue_.push_back(ticket);
+  ++pending_;
+  ++stats_.submitted;
+  ++stats_.compiling;
+  cvCompile_.notify_one();
+  return ticket;
+}
+
+void BatchServer::setBudget(int64_t bytes) {
+  std::lock_guard<std::mutex> lock(m_);
+  budget_ = bytes;
+}
+
+void BatchServer::compileLoop() {
+  for (;;) {
+    int64_t ticket;
+    gpu::PostflopSpot spot;
+    gpu::StreetBetConfigs cfgs;
+    bool perStreet;
+    {
+      std::unique_lock<std::mutex> lock(m_);
+      cvCompile_.wait(lock, [&] { return closing_ || compileHead_ < compileQueue_.size(); });
+      if (closing_) return;
+      ticket = compileQueue_[compileHead_++];
+      if (compileHead_ == compileQueue_.size()) {
+        compileQueue_.clear();
+        compileHead_ = 0;
+      }
+      const Request& r = reqs_.at(ticket);
+      spot = r.spot;
+      cfgs = r.cfgs;
+      perStreet = r.perStreet;
+    }
+    std::unique_ptr<CompiledSpot> cs;
+    int code = PPS_GB_OK;
+    std::string msg;
+    try {
+      cs = compileSpot(spot, cfgs, perStreet);
+    } catch (const Error& e) {
+      code = e.code;
+      msg = e.msg;
+    } catch (const std::exception& e) {
+      code = PPS_GB_E_MEMORY;
+      msg = e.what();
+    }
+    std::unique_lock<std::mutex> lock(m_);
+    --stats_.compiling;
+    Request& r = reqs_.at(ticket);
+    if (code != PPS_GB_OK || cs->tree.empty) {
+      // Failed compiles and empty ranges finish at once (empty: zero stats,
+      // as a lone solver reports).
+      BatchResult res = r.result;
+      res.status = code;
+      res.error = msg;
+      res.admitMs = res.finishMs = nowMs();
+      if (code == PPS_GB_OK) res.converged = true;
+      lock.unlock();
+      finish(ticket, std::move(res));
+      continue;
+    }
+    r.result.numNodes = (int)cs->tree.nodes.size();
+    r.result.deviceBytes = cs->bytes;
+    r.state = kWaiting;
+    ++stats_.waiting;
+    ready_[ticket] = std::move(cs);
+    cvReady_.notify_all();
+  }
+}
+
+void BatchServer::finish(int64_t ticket, BatchResult&& r) {
+  std::lock_guard<std::mutex> lock(m_);
+  Request& q = reqs_.at(ticket);
+  q.state = kDone;
+  if (r.status != PPS_GB_OK) ++stats_.failed;
+  ++stats_.done;
+  q.result = std::move(r);
+  --pending_;
+  cvDone_.notify_all();
+}
+
+bool BatchServer::epoch() {
+  Forest& F = *forest_;
+  const double tStart = nowMs();
+  // Admission in ticket order while the budget allows.
+  std::vector<std::pair<int64_t, std::unique_ptr<CompiledSpot>>> admit;
+  {
+    std::lock_guard<std::mutex> lock(m_);
+    int64_t used = (int64_t)F.usedBytes();
+    bool resident = !F.slots().empty();
+    while (!ready_.empty()) {
+      auto it = ready_.begin();
+      const int64_t b = (int64_t)it->second->bytes;
+      if (b > budget_) {
+        Request& q = reqs_.at(it->first);
+        q.result.status = PPS_GB_E_BUDGET;
+        q.result.error = "spot needs " + std::to_string(b) + " device bytes, budget is " +
+                         std::to_string(budget_);
+        q.result.admitMs = q.result.finishMs = nowMs();
+        q.state = kDone;
+        ++stats_.failed;
+        ++stats_.done;
+        --stats_.waiting;
+        --pending_;
+        ready_.erase(it);
+        cvDone_.notify_all();
+        continue;
+      }
+      if (resident && used + b > budget_) break;
+      used += b;
+      resident = true;
+      admit.emplace_back(it->first, std::move(it->second));
+      ready_.erase(it);
+      --stats_.waiting;
+    }
+  }
+  for (auto& a : admit) {
+    const int64_t ticket = a.first;
+    try {
+      const int slot = F.admit(std::move(a.second));
+      std::lock_guard<std::mutex> lock(m_);
+      slotTicket_[slot] = ticket;
+      Request& q = reqs_.at(ticket);
+      q.state = kActive;
+      q.result.admitMs = nowMs();
+      ++stats_.active;
+    } catch (const Error& e) {
+      BatchResult res;
+      {
+        std::lock_guard<std::mutex> lock(m_);
+        res = reqs_.at(ticket).result;
+      }
+      res.status = e.code;
+      res.error = e.msg;
+      res.admitMs = res.finishMs = nowMs();
+      finish(ticket, std::move(res));
+    }
+  }
+  const std::vector<int> slots = F.slots();
+  const double tAdmitted = nowMs();
+  {
+    std::lock_guard<std::mutex> lock(m_);
+    stats_.admitMs += tAdmitted - tStart;
+    stats_.peakActive = std::max<int64_t>(stats_.peakActive, (int64_t)slots.size());
+    stats_.usedBytes = (int64_t)F.usedBytes();
+    stats_.peakUsed = std::max(stats_.peakUsed, stats_.usedBytes);
+    stats_.deviceBytes = (int64_t)F.deviceBytes();
+  }
+  if (slots.empty()) return !admit.empty();
+
+  F.iterate(cfg_.checkEvery);
+  const std::vector<double> br0 = F.walkValues(slots, 0, kModeBR);
+  const std::vector<double> br1 = F.walkValues(slots, 1, kModeBR);
+  std::vector<int> done;
+  std::vector<double> doneExpl;
+  for (size_t i = 0; i < slots.size(); ++i) {
+    const CompiledSpot& cs = F.spot(slots[i]);
+    const double expl = (br0[i] + br1[i] - (double)cs.tree.spot.pot) / 2.0;
+    double target;
+    {
+      std::lock_guard<std::mutex> lock(m_);
+      target = reqs_.at(slotTicket_.at(slots[i])).target;
+    }
+    if ((target > 0.0 && expl <= target) || F.iterations(slots[i]) >= cfg_.maxIterations) {
+      done.push_back(slots[i]);
+      doneExpl.push_back(expl);
+    }
+  }
+  const double tChecked = nowMs();
+  const double iterMs = F.lastIterateMs();
+  {
+    std::lock_guard<std::mutex> lock(m_);
+    ++stats_.epochs;
+    stats_.spotIterations += (int64_t)slots.size() * cfg_.checkEvery;
+    stats_.captures = F.captures();
+    stats_.iterateMs += iterMs;
+    stats_.checkMs += tChecked - tAdmitted;
+  }
+  if (done.empty()) return true;
+
+  const std::vector<double> ev0 = F.walkValues(done, 0, kModeEV);
+  const std::vector<double> ev1 = F.walkValues(done, 1, kModeEV);
+  for (size_t i = 0; i < done.size(); ++i) {
+    const int slot = done[i];
+    BatchResult res;
+    int64_t ticket;
+    {
+      std::lock_guard<std::mutex> lock(m_);
+      ticket = slotTicket_.at(slot);
+      res = reqs_.at(ticket).result;
+    }
+    const CompiledSpot& cs = F.spot(slot);
+    const Tree& t = cs.tree;
+    res.status = PPS_GB_OK;
+    res.iterations = F.iterations(slot);
+    res.expl = doneExpl[i];
+    res.converged = res.target > 0.0 && res.expl <= res.target;
+    res.ev0 = ev0[i];
+    res.ev1 = ev1[i];
+    res.pairMass = (int64_t)(cs.pairMass * (double)(1LL << 20));
+    const Node& root = t.nodes[0];
+    if (root.kind == kDecide) {
+      res.rootRows = F.rootRows(slot);
+      res.rootCombos = t.n(0, root.player);
+      res.rootFreqs = aggregate(res.rootRows, root.na, res.rootCombos, t.side[root.player].w);
+      res.rootActions.assign(t.actions.begin() + root.actBase,
+                             t.actions.begin() + root.actBase + root.na);
+    }
+    F.retire(slot);
+    res.finishMs = nowMs();
+    {
+      std::lock_guard<std::mutex> lock(m_);
+      slotTicket_.erase(slot);
+      --stats_.active;
+      stats_.usedBytes = (int64_t)F.usedBytes();
+    }
+    finish(ticket, std::move(res));
+  }
+  std::lock_guard<std::mutex> lock(m_);
+  stats_.retireMs += nowMs() - tChecked;
+  return true;
+}
+
+bool BatchServer::run(double timeoutS) {
+  std::unique_lock<std::mutex> driver(driverMutex_, std::try_to_lock);
+  if (!driver.owns_lock() || serving_)
+    throw Error{PPS_GB_E_STATE, "batch: another driver (run or the serve thread) is active"};
+  cudaCheck(cudaSetDevice(device_), "cudaSetDevice");
+  const double deadline = timeoutS > 0.0 ? nowMs() + 1000.0 * timeoutS : 0.0;
+  for (;;) {
+    {
+      std::lock_guard<std::mutex> lock(m_);
+      if (pending_ == 0) return true;
+    }
+    if (deadline > 0.0 && nowMs() > deadline) return false;
+    if (!epoch()) {
+      // Nothing resident: wait for a compile to finish.
+      const double t = nowMs();
+      std::unique_lock<std::mutex> lock(m_);
+      cvReady_.wait_for(lock, std::chrono::milliseconds(20),
+                        [&] { return !ready_.empty() || pending_ == 0; });
+      stats_.idleMs += nowMs() - t;
+    }
+  }
+}
+
+void BatchServer::start() {
+  if (serving_.exchange(true)) return;
+  serveThread_ = std::thread([this] {
+    std::lock_guard<std::mutex> driver(driverMutex_);
+    try {
+      cudaCheck(cudaSetDevice(device_), "cudaSetDevice");
+      while (serving_) {
+        if (!epoch()) {
+          const double t = nowMs();
+          std::unique_lock<std::mutex> lock(m_);
+          cvReady_.wait_for(lock, std::chrono::milliseconds(5),
+                            [&] { return !ready_.empty() || !serving_; });
+          stats_.idleMs += nowMs() - t;
+        }
+      }
+    } catch (const Error& e) {
+      // A device error ends serving: fail everything still pending.
+      std::lock_guard<std::mutex> lock(m_);
+      for (auto& kv : reqs_)
+        if (kv.second.state != kDone) {
+          kv.second.state = kDone;
+          kv.second.result.status = e.code;
+          kv.second.result.error = e.msg;
+          ++stats_.failed;
+          ++stats_.done;
+          --pending_;
+        }
+      serving_ = false;
+      cvDone_.notify_all();
+    }
+  });
+}
+
+void BatchServer::stop() {
+  serving_ = false;
+  cvReady_.notify_all();
+  if (serveThread_.joinable()) serveThread_.join();
+}
+
+bool BatchServer::poll(int64_t ticket, BatchResult* out) const {
+  std::lock_guard<std::mutex> lock(m_);
+  auto it = reqs_.find(ticket);
+  if (it == reqs_.end()) throw Error{PPS_GB_E_INDEX, "batch: unknown or collected ticket"};
+  if (it->second.state != kDone) return false;
+  if (out) *out = it->second.result;
+  return true;
+}
+
+bool BatchServer::wait(int64_t ticket, double timeoutS, BatchResult* out) {
+  std::unique_lock<std::mutex> lock(m_);
+  auto done = [&] {
+    auto it = reqs_.find(ticket);
+    return it == reqs_.end() || it->second.state == kDone;
+  };
+  if (timeoutS > 0.0)
+    cvDone_.wait_for(lock, std::chrono::duration<double>(timeoutS), done);
+  else
+    cvDone_.wait(lock, done);
+  auto it = reqs_.find(ticket);
+  if (it == reqs_.end()) throw Error{PPS_GB_E_INDEX, "batch: unknown or collected ticket"};
+  if (it->second.state != kDone) return false;
+  if (out) *out = it->second.result;
+  return true;
+}
+
+std::vector<BatchResult> BatchServer::collect(size_t max) {
+  std::lock_guard<std::mutex> lock(m_);
+  std::vector<BatchResult> out;
+  for (auto it = reqs_.begin(); it != reqs_.end() && out.size() < max;) {
+    if (it->second.state == kDone) {
+      out.push_back(std::move(it->second.result));
+      it = reqs_.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  return out;
+}
+
+BatchInfo BatchServer::info() const {
+  std::lock_guard<std::mutex> lock(m_);
+  BatchInfo b = stats_;
+  b.budget = budget_;
+  return b;
+}
+
+}  // namespace gb
+}  // namespace pps

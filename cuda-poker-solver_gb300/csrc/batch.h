@@ -1,0 +1,133 @@
+// Batched and served solving: a request queue in front of a Forest.
+//
+// submit() hands a spot to a pool of compile threads; compiled spots wait
+// in ticket order and are admitted into the forest while the sum of the
+// resident spots' device footprints stays within the HBM budget. A driver
+// (run() on the caller's thread, or the thread start() launches) repeats
+// epochs: admit, run `checkEvery` DCFR iterations of every resident spot
+// in one graph, run the FP64 best-response walks, and retire each spot
+// whose exploitability reached its target (or whose iteration cap was
+// reached) after its FP64 EV walks. Spots admitted while others are
+// resident share the same launches, so work of requests that arrive at
+// different times overlaps on the device. Every spot is checked at
+// multiples of `checkEvery` iterations from its admission and its rows
+// depend on nothing but its own inputs, so a result does not depend on
+// which other spots were resident.
+#pragma once
+
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "forest.h"
+#include "gpu_cfr.h"
+#include "postflop_cfr.h"
+
+namespace pps {
+namespace gb {
+
+struct BatchConfig {
+  int64_t budget = 0;        // device bytes for resident spots (0: 80% of free memory)
+  int checkEvery = 64;       // iterations between exploitability checks
+  int maxIterations = 4096;  // per spot, rounded up to a multiple of checkEvery
+  int threads = 0;           // compile threads (0: hardware threads, at most 16)
+  std::string algo = "dcfr";
+};
+
+struct BatchResult {
+  int64_t ticket = 0;
+  int status = 0;  // PPS_GB_OK or a PPS_GB_E_* code
+  std::string error;
+  bool converged = false;
+  int iterations = 0;
+  double ev0 = 0.0, ev1 = 0.0, expl = 0.0, target = 0.0;
+  int64_t pairMass = 0;
+  double submitMs = 0.0, admitMs = 0.0, finishMs = 0.0;
+  int numNodes = 0;
+  size_t deviceBytes = 0;
+  std::vector<pf::TreeAction> rootActions;
+  std::vector<double> rootFreqs;
+  int rootCombos = 0;
+  std::vector<float> rootRows;  // na x n cumulative root strategy rows
+};
+
+struct BatchInfo {
+  int64_t submitted = 0, compiling = 0, waiting = 0, active = 0, done = 0, failed = 0;
+  int64_t usedBytes = 0, deviceBytes = 0, budget = 0;
+  int64_t epochs = 0, spotIterations = 0, captures = 0, peakActive = 0, peakUsed = 0;
+  int checkEvery = 0, maxIterations = 0;
+  double admitMs = 0.0, iterateMs = 0.0, checkMs = 0.0, retireMs = 0.0, idleMs = 0.0;
+};
+
+class BatchServer {
+ public:
+  explicit BatchServer(const BatchConfig& cfg);
+  ~BatchServer();
+  BatchServer(const BatchServer&) = delete;
+  BatchServer& operator=(const BatchServer&) = delete;
+
+  // Queues a spot; target = exploitability in chips (<= 0: run to the cap).
+  int64_t submit(const gpu::PostflopSpot& spot, const gpu::StreetBetConfigs& cfgs,
+                 bool perStreet, double target);
+  void setBudget(int64_t bytes);
+  // Drives epochs on the calling thread until every submitted request has
+  // finished; false if timeoutS (> 0) passed first.
+  bool run(double timeoutS);
+  void start();
+  void stop();
+  // True (and *out filled) once the request finished.
+  bool poll(int64_t ticket, BatchResult* out) const;
+  bool wait(int64_t ticket, double timeoutS, BatchResult* out);
+  // Finished results not collected before, in ticket order (at most max).
+  std::vector<BatchResult> collect(size_t max);
+  BatchInfo info() const;
+  double nowMs() const;
+
+ private:
+  enum ReqState { kCompiling, kWaiting, kActive, kDone };
+  struct Request {
+    ReqState state = kCompiling;
+    gpu::PostflopSpot spot;
+    gpu::StreetBetConfigs cfgs;
+    bool perStreet = false;
+    double target = 0.0;
+    BatchResult result;
+  };
+
+  BatchConfig cfg_;
+  int device_ = 0;
+  std::unique_ptr<Forest> forest_;
+  std::chrono::steady_clock::time_point t0_;
+
+  mutable std::mutex m_;
+  std::condition_variable cvCompile_, cvReady_, cvDone_;
+  std::map<int64_t, Request> reqs_;
+  std::vector<int64_t> compileQueue_;  // FIFO of tickets to compile
+  size_t compileHead_ = 0;
+  std::map<int64_t, std::unique_ptr<CompiledSpot>> ready_;
+  std::map<int, int64_t> slotTicket_;
+  int64_t nextTicket_ = 1;
+  int64_t budget_ = 0;
+  int64_t pending_ = 0;  // submitted, not finished
+  BatchInfo stats_;
+  bool closing_ = false;
+  std::vector<std::thread> compilers_;
+
+  std::mutex driverMutex_;  // one driver at a time
+  std::thread serveThread_;
+  std::atomic<bool> serving_{false};
+
+  void compileLoop();
+  bool epoch();  // one admission / iterate / check / retire round
+  void finish(int64_t ticket, BatchResult&& r);
+};
+
+}  // namespace gb
+}  // namespace pps

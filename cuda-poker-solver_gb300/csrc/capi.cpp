@@ -8,8 +8,10 @@
 #include <new>
 #include <string>
 
+#include "batch.h"
 #include "compiler.h"
 #include "engine.h"
+#include "forest.h"
 #include "noalloc.h"
 #include "solver.h"
 
@@ -18,6 +20,10 @@ using pps::gb::SolverCore;
 
 struct pps_gb_solver {
   std::unique_ptr<SolverCore> core;
+};
+
+struct pps_gb_batch {
+  std::unique_ptr<pps::gb::BatchServer> server;
 };
 
 namespace {
@@ -79,6 +85,44 @@ pps_gb_action toAction(const pps::gpu::ActionLabel& a) {
   o.kind = (int32_t)a.kind;
   o.amount = a.amount;
   return o;
+}
+
+pps::gpu::StreetBetConfigs toConfigs(const pps_gb_bet_config* cfgs, int n) {
+  if (!cfgs || (n != 1 && n != 3)) throw Error{PPS_GB_E_ARG, "cfgs must hold 1 or 3 configs"};
+  pps::gpu::StreetBetConfigs c;
+  for (int k = 0; k < 3; ++k) c.street[k] = toConfig(cfgs[n == 3 ? k : 0]);
+  return c;
+}
+
+pps::gb::BatchServer& server(pps_gb_batch* b) {
+  if (!b || !b->server) throw Error{PPS_GB_E_ARG, "null batch handle"};
+  return *b->server;
+}
+
+void toResult(const pps::gb::BatchResult& r, pps_gb_batch_result* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->ticket = r.ticket;
+  o->status = r.status;
+  o->converged = r.converged ? 1 : 0;
+  o->iterations = r.iterations;
+  o->num_nodes = r.numNodes;
+  o->ev0 = r.ev0;
+  o->ev1 = r.ev1;
+  o->exploitability = r.expl;
+  o->target = r.target;
+  o->pair_mass = r.pairMass;
+  o->submit_ms = r.submitMs;
+  o->admit_ms = r.admitMs;
+  o->finish_ms = r.finishMs;
+  o->device_bytes = (int64_t)r.deviceBytes;
+  o->root_actions = (int32_t)r.rootActions.size();
+  o->root_combos = r.rootCombos;
+  for (size_t a = 0; a < r.rootActions.size() && a < PPS_GB_MAX_ACTIONS; ++a) {
+    o->root_action[a].kind = (int32_t)r.rootActions[a].kind;
+    o->root_action[a].amount = r.rootActions[a].amount;
+    o->root_freqs[a] = a < r.rootFreqs.size() ? r.rootFreqs[a] : 0.0;
+  }
+  std::strncpy(o->error, r.error.c_str(), sizeof(o->error) - 1);
 }
 
 SolverCore& core(pps_gb_solver* h) {
@@ -433,6 +477,144 @@ int pps_gb_solve_noalloc(const pps_gb_spot* spot, const pps_gb_bet_config* cfg,
                                             row_capacity, first_iteration, iterations,
                                             static_cast<cudaStream_t>(stream));
     if (n_rows) *n_rows = n;
+  });
+}
+
+void pps_gb_batch_config_default(pps_gb_batch_config* cfg) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  const pps::gb::BatchConfig d;
+  cfg->hbm_budget = d.budget;
+  cfg->check_every = d.checkEvery;
+  cfg->max_iterations = d.maxIterations;
+  cfg->compile_threads = d.threads;
+  std::strncpy(cfg->algo, d.algo.c_str(), sizeof(cfg->algo) - 1);
+}
+
+int pps_gb_batch_create(const pps_gb_batch_config* cfg, pps_gb_batch** out) {
+  return guarded([&] {
+    if (!out) throw Error{PPS_GB_E_ARG, "null argument"};
+    *out = nullptr;
+    pps::gb::BatchConfig c;
+    if (cfg) {
+      c.budget = cfg->hbm_budget;
+      c.checkEvery = cfg->check_every;
+      c.maxIterations = cfg->max_iterations;
+      c.threads = cfg->compile_threads;
+      const size_t n = strnlen(cfg->algo, sizeof(cfg->algo));
+      if (n) c.algo.assign(cfg->algo, n);
+    }
+    auto* b = new pps_gb_batch();
+    try {
+      b->server.reset(new pps::gb::BatchServer(c));
+    } catch (...) {
+      delete b;
+      throw;
+    }
+    *out = b;
+  });
+}
+
+void pps_gb_batch_destroy(pps_gb_batch* b) { delete b; }
+
+int pps_gb_batch_set_budget(pps_gb_batch* b, int64_t bytes) {
+  return guarded([&] { server(b).setBudget(bytes); });
+}
+
+int pps_gb_batch_submit(pps_gb_batch* b, const pps_gb_spot* spot, const pps_gb_bet_config* cfgs,
+                        int n_cfgs, double target, int64_t* ticket) {
+  return guarded([&] {
+    if (!spot || !ticket) throw Error{PPS_GB_E_ARG, "null argument"};
+    *ticket = server(b).submit(toSpot(*spot), toConfigs(cfgs, n_cfgs), n_cfgs == 3, target);
+  });
+}
+
+int pps_gb_batch_run(pps_gb_batch* b, double timeout_s) {
+  bool all = false;
+  const int rc = guarded([&] { all = server(b).run(timeout_s); });
+  return rc != PPS_GB_OK ? rc : all ? PPS_GB_OK : PPS_GB_PENDING;
+}
+
+int pps_gb_batch_start(pps_gb_batch* b) { return guarded([&] { server(b).start(); }); }
+int pps_gb_batch_stop(pps_gb_batch* b) { return guarded([&] { server(b).stop(); }); }
+
+int pps_gb_batch_poll(pps_gb_batch* b, int64_t ticket, pps_gb_batch_result* out) {
+  bool done = false;
+  const int rc = guarded([&] {
+    pps::gb::BatchResult r;
+    done = server(b).poll(ticket, &r);
+    if (done && out) toResult(r, out);
+  });
+  return rc != PPS_GB_OK ? rc : done ? PPS_GB_OK : PPS_GB_PENDING;
+}
+
+int pps_gb_batch_wait(pps_gb_batch* b, int64_t ticket, double timeout_s,
+                      pps_gb_batch_result* out) {
+  bool done = false;
+  const int rc = guarded([&] {
+    pps::gb::BatchResult r;
+    done = server(b).wait(ticket, timeout_s, &r);
+    if (done && out) toResult(r, out);
+  });
+  return rc != PPS_GB_OK ? rc : done ? PPS_GB_OK : PPS_GB_PENDING;
+}
+
+int pps_gb_batch_collect(pps_gb_batch* b, pps_gb_batch_result* out, int cap, int* n_out) {
+  return guarded([&] {
+    if (!n_out || (cap > 0 && !out)) throw Error{PPS_GB_E_ARG, "null argument"};
+    const auto rs = server(b).collect(cap > 0 ? (size_t)cap : 0);
+    for (size_t i = 0; i < rs.size(); ++i) toResult(rs[i], &out[i]);
+    *n_out = (int)rs.size();
+  });
+}
+
+int pps_gb_batch_root_rows(pps_gb_batch* b, int64_t ticket, float* out, int64_t cap,
+                           int64_t* n_out) {
+  return guarded([&] {
+    if (!n_out) throw Error{PPS_GB_E_ARG, "null argument"};
+    pps::gb::BatchResult r;
+    if (!server(b).poll(ticket, &r)) throw Error{PPS_GB_E_STATE, "request not finished"};
+    *n_out = (int64_t)r.rootRows.size();
+    if ((int64_t)r.rootRows.size() > cap || (!out && !r.rootRows.empty()))
+      throw Error{PPS_GB_E_ARG, "buffer too small: need " + std::to_string(r.rootRows.size())};
+    std::copy(r.rootRows.begin(), r.rootRows.end(), out);
+  });
+}
+
+int pps_gb_batch_get_info(pps_gb_batch* b, pps_gb_batch_info* out) {
+  return guarded([&] {
+    if (!out) throw Error{PPS_GB_E_ARG, "null argument"};
+    const pps::gb::BatchInfo i = server(b).info();
+    out->submitted = i.submitted;
+    out->compiling = i.compiling;
+    out->waiting = i.waiting;
+    out->active = i.active;
+    out->done = i.done;
+    out->failed = i.failed;
+    out->used_bytes = i.usedBytes;
+    out->device_bytes = i.deviceBytes;
+    out->budget = i.budget;
+    out->epochs = i.epochs;
+    out->spot_iterations = i.spotIterations;
+    out->captures = i.captures;
+    out->peak_active = i.peakActive;
+    out->peak_used_bytes = i.peakUsed;
+    out->check_every = i.checkEvery;
+    out->admit_ms = i.admitMs;
+    out->iterate_ms = i.iterateMs;
+    out->check_ms = i.checkMs;
+    out->retire_ms = i.retireMs;
+    out->idle_ms = i.idleMs;
+    out->max_iterations = i.maxIterations;
+  });
+}
+
+int pps_gb_batch_footprint(const pps_gb_spot* spot, const pps_gb_bet_config* cfgs, int n_cfgs,
+                           int64_t* bytes) {
+  return guarded([&] {
+    if (!spot || !bytes) throw Error{PPS_GB_E_ARG, "null argument"};
+    const auto cs = pps::gb::compileSpot(toSpot(*spot), toConfigs(cfgs, n_cfgs), n_cfgs == 3);
+    *bytes = (int64_t)cs->bytes;
   });
 }
 

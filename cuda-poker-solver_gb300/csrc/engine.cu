@@ -12,24 +12,27 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "kernels.cuh"
 #include "leaf_kernel.cuh"
+#include "plan.cuh"
 #include "pps_gb.h"
 
 namespace pps {
 namespace gb {
 
-#define GB_CK(call)                                                          \
-  do {                                                                       \
-    cudaError_t e_ = (call);                                                 \
-    if (e_ != cudaSuccess)                                                   \
-      throw Error{e_ == cudaErrorMemoryAllocation ? PPS_GB_E_MEMORY          \
-                                                  : PPS_GB_E_CUDA,           \
-                  std::string("CUDA error: ") + cudaGetErrorString(e_) +     \
-                      " (" #call ")"};                                       \
-  } while (0)
+void raiseSmemLimit(const void* kernel, size_t bytes) {
+  static std::mutex m;
+  static std::map<const void*, size_t> limit;
+  std::lock_guard<std::mutex> lock(m);
+  size_t& cur = limit[kernel];
+  if (bytes <= cur) return;
+  GB_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
+}
 
 namespace {
 
@@ -41,24 +44,11 @@ V* alloc(size_t count, size_t& bytes) {
   return p;
 }
 
-enum LaunchKind { kFwd, kBwd, kBwdTerm, kBwdInt, kLeafSweep, kCounter };
-const char* kLaunchName[] = {"fwd_level", "bwd_level", "bwd_terminal", "bwd_interior",
-                             "leaf_street", "counter"};
-
-struct Launch {
-  LaunchKind kind;
-  int tr;
-  ListRef list;
-  double bytes;           // algorithmic bytes of this launch (f32 rows)
-  bool withNext = false;  // independent of the next launch: run both at once
-};
-
 }  // namespace
 
 struct Engine::Dev {
   cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;                  // second graph branch
-  cudaEvent_t fork = nullptr, join = nullptr;  // branch fork / join
+  Branches br;  // main = stream, plus the side branch
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<void*> owned;
@@ -97,53 +87,14 @@ V* upload(Engine::Dev& d, const std::vector<V>& v, size_t& bytes, int64_t& h2d) 
   return d.own(p);
 }
 
-unsigned gridOf(int count) { return (unsigned)std::min(count, 1 << 20); }
+PlanArgs planArgs(const Engine::Dev& d) {
+  return PlanArgs{d.tree, d.rowsF, d.tasks, d.counter, 1, d.maxN, d.smemF};
+}
 
 // Issues one planned launch (CFR mode, f32 rows) on stream s.
 void issue(Engine::Dev& d, const Launch& l, cudaStream_t s) {
-  const unsigned g = gridOf(l.list.count);
-  const int* tk = d.tasks + l.list.off;
-  switch (l.kind) {
-    case kFwd:
-      fwdLevelK<float><<<g, kThreads, 0, s>>>(d.tree, d.rowsF, tk, l.list.count, l.tr, 0);
-      break;
-    case kBwd:
-      bwdLevelK<float><<<g, kThreads, d.smemF, s>>>(d.tree, d.rowsF, tk, l.list.count, l.tr,
-                                                    kModeCFR, d.maxN);
-      break;
-    case kBwdTerm:
-      bwdTerminalK<float><<<g, kThreads, d.smemF, s>>>(d.tree, d.rowsF, tk, l.list.count, l.tr,
-                                                       d.maxN);
-      break;
-    case kBwdInt:
-      bwdInteriorK<float><<<g, kThreads, 0, s>>>(d.tree, d.rowsF, tk, l.list.count, l.tr,
-                                                 kModeCFR);
-      break;
-    case kLeafSweep:
-      launchLeaf(d.leaf, d.tree, d.rowsF, l.tr, s);
-      break;
-    case kCounter:
-      advanceCounterK<<<1, 32, 0, s>>>(d.counter);
-      break;
-  }
-}
-
-// Issues a plan; launches marked withNext run on a side branch forked from
-// and joined back into the main stream (graph branches under capture).
-void issuePlan(Engine::Dev& d, const std::vector<Launch>& P) {
-  for (size_t i = 0; i < P.size(); ++i) {
-    if (P[i].withNext && i + 1 < P.size()) {
-      GB_CK(cudaEventRecord(d.fork, d.stream));
-      GB_CK(cudaStreamWaitEvent(d.side, d.fork, 0));
-      issue(d, P[i], d.stream);
-      issue(d, P[i + 1], d.side);
-      GB_CK(cudaEventRecord(d.join, d.side));
-      GB_CK(cudaStreamWaitEvent(d.stream, d.join, 0));
-      ++i;
-    } else {
-      issue(d, P[i], d.stream);
-    }
-  }
+  if (l.kind == kLeafSweep) launchLeaf(d.leaf, d.tree, d.rowsF, l.tr, s);
+  else issueLaunch(planArgs(d), l, s);
 }
 
 }  // namespace
@@ -153,9 +104,10 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
   Dev& d = *d_;
   size_t& B = deviceBytes_;
   GB_CK(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
-  GB_CK(cudaStreamCreateWithFlags(&d.side, cudaStreamNonBlocking));
-  GB_CK(cudaEventCreateWithFlags(&d.fork, cudaEventDisableTiming));
-  GB_CK(cudaEventCreateWithFlags(&d.join, cudaEventDisableTiming));
+  d.br.main = d.stream;
+  GB_CK(cudaStreamCreateWithFlags(&d.br.side, cudaStreamNonBlocking));
+  GB_CK(cudaEventCreateWithFlags(&d.br.fork, cudaEventDisableTiming));
+  GB_CK(cudaEventCreateWithFlags(&d.br.join, cudaEventDisableTiming));
   d.tree.nodes = upload(d, L_.nodes, B, h2d_);
   d.tree.rows = upload(d, L_.rows, B, h2d_);
   d.tree.termVal = upload(d, L_.termVal, B, h2d_);
@@ -207,12 +159,9 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
   d.maxN = L_.maxN;
   d.smemF = bwdScratchBytes<float>(d.maxN);
   d.smemD = bwdScratchBytes<double>(d.maxN);
-  GB_CK(cudaFuncSetAttribute(bwdLevelK<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)d.smemF));
-  GB_CK(cudaFuncSetAttribute(bwdLevelK<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)d.smemD));
-  GB_CK(cudaFuncSetAttribute(bwdTerminalK<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)d.smemF));
+  raiseSmemLimit((const void*)bwdLevelK<float>, d.smemF);
+  raiseSmemLimit((const void*)bwdLevelK<double>, d.smemD);
+  raiseSmemLimit((const void*)bwdTerminalK<float>, d.smemF);
   if (d.leaf.ok) GB_CK(prepareLeaf(d.leaf));
   buildPlans();
   engineKind_ = d.leaf.ok ? 1 : 0;
@@ -226,9 +175,9 @@ Engine::~Engine() {
   if (d_->stream) cudaStreamSynchronize(d_->stream);
   for (void* p : d_->owned) cudaFree(p);
   if (d_->stream) cudaStreamDestroy(d_->stream);
-  if (d_->side) cudaStreamDestroy(d_->side);
-  if (d_->fork) cudaEventDestroy(d_->fork);
-  if (d_->join) cudaEventDestroy(d_->join);
+  if (d_->br.side) cudaStreamDestroy(d_->br.side);
+  if (d_->br.fork) cudaEventDestroy(d_->br.fork);
+  if (d_->br.join) cudaEventDestroy(d_->br.join);
 }
 
 void* Engine::stream() const { return (void*)d_->stream; }
@@ -237,7 +186,7 @@ void* Engine::stream() const { return (void*)d_->stream; }
 // write once (index tables excluded).
 double Engine::taskBytes(int task, int tr, bool fwd) const {
   const Tree& t = t_;
-  const int u = task >> 8, sub = (task >> 2) & 63, kind = task & 3;
+  const int u = (int)((unsigned)task >> 8), sub = (task >> 2) & 63, kind = task & 3;
   const Node& nd = t.nodes[u];
   auto share = [&](int n) {  // the quads of this task's chunk
     const int q = (int)quads(n), q0 = sub * kChunkQuads, q1 = std::min(q, q0 + kChunkQuads);
@@ -298,8 +247,7 @@ void Engine::buildPlans() {
         // write their own cfv rows; interior tasks read child cfv rows of
         // deeper levels, so both halves of a level run at once.
         const std::vector<int>& v = bw[dd];
-        int nt = 0;
-        while (nt < (int)v.size() && (v[nt] & 3) >= 2) ++nt;
+        const int nt = terminalCount(v);
         const std::vector<int> vt(v.begin(), v.begin() + nt), vi(v.begin() + nt, v.end());
         const ListRef lt{brf[dd].off, nt}, li{brf[dd].off + nt, brf[dd].count - nt};
         if (nt) P.push_back({kBwdTerm, tr, lt, listBytes(vt, tr, false), li.count > 0});
@@ -365,7 +313,7 @@ void Engine::capture() {
   const std::vector<Launch>& P = d.plan[engineKind_];
   GB_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t launchErr = cudaSuccess;
-  issuePlan(d, P);
+  issuePlan(P, d.br, [&](const Launch& l, cudaStream_t s) { issue(d, l, s); });
   launchErr = cudaGetLastError();
   cudaGraph_t g = nullptr;
   const cudaError_t endErr = cudaStreamEndCapture(d.stream, &g);
@@ -420,7 +368,7 @@ std::vector<Engine::KernelStat> Engine::profile(int n, bool splitKinds) {
   for (const Launch& l : d.plan[engineKind_]) {
     const bool bwd = l.kind == kBwd || l.kind == kBwdTerm || l.kind == kBwdInt;
     if (!bwd || !splitKinds) {
-      P.push_back({l, kLaunchName[l.kind]});
+      P.push_back({l, launchName(l.kind)});
       continue;
     }
     int i = l.list.off;

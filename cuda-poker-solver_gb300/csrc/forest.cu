@@ -1,0 +1,690 @@
+// Forest (see forest.h): shared device pools, relocation of spot layouts,
+// the all-spots iteration graph and the FP64 check walks.
+#include "forest.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <string>
+
+#include "kernels.cuh"
+#include "plan.cuh"
+#include "pps_gb.h"
+
+namespace pps {
+namespace gb {
+
+double pairMassOf(const Tree& t) {
+  const Side& s0 = t.side[0];
+  const Side& s1 = t.side[1];
+  double total1 = 0.0, cardSum[52] = {0.0};
+  for (int j = 0; j < s1.n; ++j) {
+    total1 += s1.w[j];
+    cardSum[s1.cards[2 * j]] += s1.w[j];
+    cardSum[s1.cards[2 * j + 1]] += s1.w[j];
+  }
+  double Z = 0.0;
+  for (int i = 0; i < s0.n; ++i) {
+    double w = total1 - cardSum[s0.cards[2 * i]] - cardSum[s0.cards[2 * i + 1]];
+    if (s0.sameOther[i] >= 0) w += s1.w[s0.sameOther[i]];
+    if (w > 0.0) Z += s0.w[i] * w;
+  }
+  return Z;
+}
+
+namespace {
+
+// Pools. A region is one index space (node ids, row quads, ...); arrays
+// are the device buffers indexed by it.
+enum Region { rNode, rChild, rState, rU8, rU16, rI16, rSd, rReg, rCfv, rReach0, rReach1, rW,
+              kRegions };
+// Allocation granule per region, in entries: every range starts on a
+// 16-byte boundary (u16 tables are staged with 16-byte loads).
+constexpr size_t kGranule[kRegions] = {1, 4, 1, 16, 8, 8, 1, 1, 1, 1, 1, 2};
+
+enum Array { aNodes, aRows, aTerm, aChild, aState, aU8, aU16, aI16, aSd, aReg, aStr, aCfvF,
+             aCfvD, aReachF0, aReachD0, aReachF1, aReachD1, aW, kArrays };
+struct ArrayDef {
+  Region region;
+  size_t entryBytes;
+};
+const ArrayDef kArray[kArrays] = {
+    {rNode, sizeof(NodeDev)}, {rNode, sizeof(RowDev)}, {rNode, 8 * sizeof(float)},
+    {rChild, sizeof(int)},    {rState, sizeof(StateDev)}, {rU8, 1},
+    {rU16, 2},                {rI16, 2},                  {rSd, sizeof(ShowdownInfo)},
+    {rReg, 16},               {rReg, 16},                 {rCfv, 16},
+    {rCfv, 32},               {rReach0, 16},              {rReach0, 32},
+    {rReach1, 16},            {rReach1, 32},              {rW, 8}};
+
+size_t roundUp(size_t n, size_t g) { return (n + g - 1) / g * g; }
+
+void regionSizes(const Tree& t, const HostLayout& L, size_t out[kRegions]) {
+  out[rNode] = L.nodes.size();
+  out[rChild] = L.children.size();
+  out[rState] = L.states.size();
+  out[rU8] = L.poolU8.size();
+  out[rU16] = L.poolU16.size();
+  out[rI16] = L.poolI16.size();
+  out[rSd] = L.poolSd.size();
+  out[rReg] = L.regQuads;
+  out[rCfv] = L.cfvQuads;
+  out[rReach0] = L.reachQuads[0];
+  out[rReach1] = L.reachQuads[1];
+  out[rW] = (size_t)t.side[0].n + (size_t)t.side[1].n;  // w0 then w1
+}
+
+size_t footprintOf(const Tree& t, const HostLayout& L) {
+  size_t sz[kRegions];
+  regionSizes(t, L, sz);
+  size_t bytes = 0;
+  for (int a = 0; a < kArrays; ++a) {
+    const Region r = kArray[a].region;
+    bytes += roundUp(sz[r], kGranule[r]) * kArray[a].entryBytes;
+  }
+  return bytes;
+}
+
+// First-fit range allocator over one index space: holes by offset, a bump
+// pointer at the top; ranges are multiples of the region's granule.
+class RangeAlloc {
+ public:
+  size_t alloc(size_t n, size_t g) {
+    n = roundUp(n, g);
+    if (n == 0) return 0;
+    for (auto it = holes_.begin(); it != holes_.end(); ++it) {
+      if (it->second < n) continue;
+      const size_t off = it->first, rest = it->second - n;
+      holes_.erase(it);
+      if (rest) holes_[off + n] = rest;
+      return off;
+    }
+    const size_t off = top_;
+    top_ += n;
+    return off;
+  }
+  void release(size_t off, size_t n, size_t g) {
+    n = roundUp(n, g);
+    if (n == 0) return;
+    auto next = holes_.lower_bound(off);
+    if (next != holes_.begin()) {
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == off) {
+        off = prev->first;
+        n += prev->second;
+        holes_.erase(prev);
+      }
+    }
+    if (next != holes_.end() && off + n == next->first) {
+      n += next->second;
+      holes_.erase(next);
+    }
+    if (off + n == top_) {
+      top_ = off;
+      // A hole may now end at the new top.
+      if (!holes_.empty()) {
+        auto last = std::prev(holes_.end());
+        if (last->first + last->second == top_) {
+          top_ = last->first;
+          holes_.erase(last);
+        }
+      }
+    } else {
+      holes_[off] = n;
+    }
+  }
+  size_t top() const { return top_; }
+
+ private:
+  std::map<size_t, size_t> holes_;
+  size_t top_ = 0;
+};
+
+struct RootInfo {
+  uint32_t cfvQ;  // root value row (quads)
+  int wOff;       // traverser weights in the weight pool
+  int n;          // traverser combos
+  int pad;
+};
+
+// Root value of each listed spot: sum_j w[j] * cfv[j] in a fixed order
+// (one CTA per spot, strided partial sums, then a tree reduction).
+__global__ void __launch_bounds__(128) rootValueK(const double* __restrict__ cfv,
+                                                  const double* __restrict__ w,
+                                                  const RootInfo* __restrict__ info,
+                                                  double* __restrict__ out) {
+  __shared__ double part[128];
+  const RootInfo r = info[blockIdx.x];
+  double acc = 0.0;
+  for (int j = threadIdx.x; j < r.n; j += blockDim.x)
+    acc += w[r.wOff + j] * cfv[(size_t)r.cfvQ * 4 + j];
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = 64; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) part[threadIdx.x] += part[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = part[0];
+}
+
+template <typename V>
+void ensureBuf(V*& p, size_t& cap, size_t need) {
+  if (need <= cap) return;
+  const size_t n = std::max(need, cap + cap / 2);
+  if (p) GB_CK(cudaFree(p));
+  p = nullptr;
+  GB_CK(cudaMalloc(&p, n * sizeof(V)));
+  cap = n;
+}
+
+}  // namespace
+
+std::unique_ptr<CompiledSpot> compileSpot(const gpu::PostflopSpot& spot,
+                                          const gpu::StreetBetConfigs& cfgs, bool perStreet) {
+  std::unique_ptr<CompiledSpot> s(new CompiledSpot);
+  s->tree = compileTree(spot, cfgs, perStreet);
+  if (!s->tree.empty) {
+    s->layout = buildLayout(s->tree);
+    s->pairMass = pairMassOf(s->tree);
+    s->bytes = footprintOf(s->tree, s->layout);
+  }
+  return s;
+}
+
+struct SlotRec {
+  std::unique_ptr<CompiledSpot> spot;
+  size_t off[kRegions] = {};
+  size_t size[kRegions] = {};
+  int iters = 0;
+  uint32_t rootCfvQ = 0, rootRegQ = 0;
+  int depth = 0;
+  // Task lists per traverser and depth, node ids relocated; backward lists
+  // keep the layout's order (terminal tasks first).
+  std::vector<std::vector<int>> fwd[2], bwd[2];
+};
+
+struct Forest::Dev {
+  cudaStream_t stream = nullptr;
+  Branches br;
+  cudaEvent_t evA = nullptr, evB = nullptr;  // around the last iterate()
+  bool timed = false;
+  RangeAlloc regions[kRegions];
+  void* arr[kArrays] = {};
+  size_t arrBytes[kArrays] = {};
+  float* coef = nullptr;
+  int coefEntries = 0;
+  int* counter = nullptr;
+  size_t counterCap = 0;
+  std::vector<int> freeSlots;
+  int nextSlot = 0;
+  std::map<int, SlotRec> live;
+  size_t used = 0;
+  // Iteration graph.
+  int* tasks = nullptr;
+  size_t tasksCap = 0;
+  std::vector<Launch> plan;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool dirty = true;
+  int captures = 0;
+  // Walk scratch.
+  int* wTasks = nullptr;
+  size_t wTasksCap = 0;
+  RootInfo* info = nullptr;
+  size_t infoCap = 0;
+  double* vals = nullptr;
+  size_t valsCap = 0;
+
+  template <typename V>
+  V* at(int a, size_t entry) const {
+    return reinterpret_cast<V*>(static_cast<char*>(arr[a]) + entry * kArray[a].entryBytes);
+  }
+  DevTree tree() const {
+    DevTree t{};
+    t.nodes = static_cast<const NodeDev*>(arr[aNodes]);
+    t.rows = static_cast<const RowDev*>(arr[aRows]);
+    t.termVal = static_cast<const float*>(arr[aTerm]);
+    t.children = static_cast<const int*>(arr[aChild]);
+    t.states = static_cast<const StateDev*>(arr[aState]);
+    t.poolU8 = static_cast<const uint8_t*>(arr[aU8]);
+    t.poolU16 = static_cast<const uint16_t*>(arr[aU16]);
+    t.poolI16 = static_cast<const int16_t*>(arr[aI16]);
+    t.poolSd = static_cast<const ShowdownInfo*>(arr[aSd]);
+    t.regret = static_cast<float*>(arr[aReg]);
+    t.strat = static_cast<float*>(arr[aStr]);
+    t.coef = coef;
+    t.counter = counter;
+    return t;
+  }
+  template <typename T>
+  DevRows<T> rows(int fArr0, int fArr1, int cArr) const {
+    DevRows<T> r{};
+    r.reach[0] = static_cast<T*>(arr[fArr0]);
+    r.reach[1] = static_cast<T*>(arr[fArr1]);
+    r.cfv = static_cast<T*>(arr[cArr]);
+    return r;
+  }
+  void dropGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    dirty = true;
+  }
+  // Grows array a to cover its region, keeping the contents.
+  void grow(int a) {
+    const size_t need = regions[kArray[a].region].top() * kArray[a].entryBytes;
+    if (need <= arrBytes[a]) return;
+    const size_t nb = roundUp(std::max(need, arrBytes[a] + arrBytes[a] / 2), (size_t)1 << 16);
+    void* p = nullptr;
+    GB_CK(cudaMalloc(&p, nb));
+    if (arr[a]) {
+      GB_CK(cudaMemcpyAsync(p, arr[a], arrBytes[a], cudaMemcpyDeviceToDevice, stream));
+      GB_CK(cudaStreamSynchronize(stream));
+      GB_CK(cudaFree(arr[a]));
+    }
+    arr[a] = p;
+    arrBytes[a] = nb;
+    dropGraph();
+  }
+  int maxN(const std::vector<int>& slots) const {
+    int m = 1;
+    for (int s : slots) m = std::max(m, live.at(s).spot->layout.maxN);
+    return m;
+  }
+};
+
+Forest::Forest(const std::vector<float>& coef) : d_(new Dev()) {
+  Dev& d = *d_;
+  GB_CK(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
+  d.br.main = d.stream;
+  GB_CK(cudaStreamCreateWithFlags(&d.br.side, cudaStreamNonBlocking));
+  GB_CK(cudaEventCreateWithFlags(&d.br.fork, cudaEventDisableTiming));
+  GB_CK(cudaEventCreateWithFlags(&d.br.join, cudaEventDisableTiming));
+  GB_CK(cudaEventCreate(&d.evA));
+  GB_CK(cudaEventCreate(&d.evB));
+  d.coefEntries = (int)(coef.size() / 3);
+  GB_CK(cudaMalloc(&d.coef, std::max<size_t>(coef.size(), 3) * sizeof(float)));
+  if (!coef.empty())
+    GB_CK(cudaMemcpy(d.coef, coef.data(), coef.size() * sizeof(float), cudaMemcpyHostToDevice));
+}
+
+Forest::~Forest() {
+  if (!d_) return;
+  Dev& d = *d_;
+  if (d.stream) cudaStreamSynchronize(d.stream);
+  if (d.exec) cudaGraphExecDestroy(d.exec);
+  if (d.graph) cudaGraphDestroy(d.graph);
+  for (void* p : d.arr) cudaFree(p);
+  cudaFree(d.coef);
+  cudaFree(d.counter);
+  cudaFree(d.tasks);
+  cudaFree(d.wTasks);
+  cudaFree(d.info);
+  cudaFree(d.vals);
+  if (d.br.side) cudaStreamDestroy(d.br.side);
+  if (d.br.fork) cudaEventDestroy(d.br.fork);
+  if (d.br.join) cudaEventDestroy(d.br.join);
+  if (d.evA) cudaEventDestroy(d.evA);
+  if (d.evB) cudaEventDestroy(d.evB);
+  if (d.stream) cudaStreamDestroy(d.stream);
+}
+
+int Forest::admit(std::unique_ptr<CompiledSpot> s) {
+  Dev& d = *d_;
+  if (!s || s->tree.empty) throw Error{PPS_GB_E_ARG, "forest: spot compiled to empty ranges"};
+  const Tree& t = s->tree;
+  HostLayout& L = s->layout;
+  int slot;
+  if (!d.freeSlots.empty()) {
+    slot = d.freeSlots.back();
+    d.freeSlots.pop_back();
+  } else {
+    if (d.nextSlot > 0xffff) throw Error{PPS_GB_E_BUDGET, "forest: more than 65536 spots"};
+    slot = d.nextSlot++;
+  }
+  SlotRec rec;
+  regionSizes(t, L, rec.size);
+  for (int r = 0; r < kRegions; ++r) rec.off[r] = d.regions[r].alloc(rec.size[r], kGranule[r]);
+  const size_t N = rec.size[rNode];
+  // Index widths: 24-bit task node ids, 32-bit row quads, 31-bit pools.
+  bool fits = rec.off[rNode] + N < ((size_t)1 << 24);
+  for (int r : {rReg, rCfv, rReach0, rReach1})
+    fits = fits && rec.off[r] + rec.size[r] <= 0xffffffffull;
+  for (int r : {rChild, rState, rU8, rU16, rI16, rSd, rW})
+    fits = fits && rec.off[r] + rec.size[r] < ((size_t)1 << 31);
+  if (!fits) {
+    for (int r = 0; r < kRegions; ++r) d.regions[r].release(rec.off[r], rec.size[r], kGranule[r]);
+    d.freeSlots.push_back(slot);
+    throw Error{PPS_GB_E_BUDGET, "forest: resident spots exceed the 32-bit row / 24-bit node "
+                                 "index space"};
+  }
+  for (int a = 0; a < kArrays; ++a) d.grow(a);
+  if ((size_t)slot >= d.counterCap) {
+    const size_t cap = std::max<size_t>(64, (size_t)slot * 2);
+    int* p = nullptr;
+    GB_CK(cudaMalloc(&p, cap * sizeof(int)));
+    GB_CK(cudaMemsetAsync(p, 0, cap * sizeof(int), d.stream));
+    if (d.counter) {
+      GB_CK(cudaMemcpyAsync(p, d.counter, d.counterCap * sizeof(int), cudaMemcpyDeviceToDevice,
+                            d.stream));
+      GB_CK(cudaStreamSynchronize(d.stream));
+      GB_CK(cudaFree(d.counter));
+    }
+    d.counter = p;
+    d.counterCap = cap;
+    d.dropGraph();
+  }
+
+  // Relocate the layout into the pools.
+  const size_t* off = rec.off;
+  for (NodeDev& nd : L.nodes) {
+    nd.meta = (int)(((unsigned)nd.meta & 0xffffu) | ((unsigned)slot << 16));
+    nd.state += (int)off[rState];
+    nd.childBase += (int)off[rChild];
+    nd.regQ += (uint32_t)off[rReg];
+  }
+  for (RowDev& rw : L.rows) {
+    rw.reachQ[0] += (uint32_t)off[rReach0];
+    rw.reachQ[1] += (uint32_t)off[rReach1];
+    rw.cfvQ += (uint32_t)off[rCfv];
+  }
+  for (int& c : L.children) c += (int)off[rNode];
+  auto shift = [](int& v, size_t by) {
+    if (v >= 0) v += (int)by;
+  };
+  for (StateDev& st : L.states)
+    for (int p = 0; p < 2; ++p) {
+      shift(st.cardsOff[p], off[rU8]);
+      shift(st.csrOff[p], off[rU16]);
+      shift(st.sameOff[p], off[rI16]);
+      shift(st.upOff[p], off[rU16]);
+      shift(st.downOff[p], off[rI16]);
+      shift(st.sdOff[p], off[rU16]);
+      shift(st.sdInfoOff[p], off[rSd]);
+    }
+  auto put = [&](int a, size_t entry, const void* src, size_t bytes) {
+    if (bytes)
+      GB_CK(cudaMemcpyAsync(d.at<char>(a, entry), src, bytes, cudaMemcpyHostToDevice, d.stream));
+  };
+  put(aNodes, off[rNode], L.nodes.data(), L.nodes.size() * sizeof(NodeDev));
+  put(aRows, off[rNode], L.rows.data(), L.rows.size() * sizeof(RowDev));
+  put(aTerm, off[rNode], L.termVal.data(), L.termVal.size() * sizeof(float));
+  put(aChild, off[rChild], L.children.data(), L.children.size() * sizeof(int));
+  put(aState, off[rState], L.states.data(), L.states.size() * sizeof(StateDev));
+  put(aU8, off[rU8], L.poolU8.data(), L.poolU8.size());
+  put(aU16, off[rU16], L.poolU16.data(), L.poolU16.size() * 2);
+  put(aI16, off[rI16], L.poolI16.data(), L.poolI16.size() * 2);
+  put(aSd, off[rSd], L.poolSd.data(), L.poolSd.size() * sizeof(ShowdownInfo));
+  for (int a : {aReg, aStr, aCfvF, aCfvD, aReachF0, aReachD0, aReachF1, aReachD1}) {
+    const Region r = kArray[a].region;
+    const size_t bytes = rec.size[r] * kArray[a].entryBytes;
+    if (bytes) GB_CK(cudaMemsetAsync(d.at<char>(a, off[r]), 0, bytes, d.stream));
+  }
+  // Root reach rows (the opponent's weights) and the weight rows.
+  std::vector<double> w(t.side[0].w);
+  w.insert(w.end(), t.side[1].w.begin(), t.side[1].w.end());
+  put(aW, off[rW], w.data(), w.size() * sizeof(double));
+  for (int tr = 0; tr < 2; ++tr) {
+    const Side& opp = t.side[1 - tr];
+    std::vector<float> rf(opp.w.begin(), opp.w.end());
+    const size_t q = L.rows[0].reachQ[tr];
+    put(tr ? aReachF1 : aReachF0, q, rf.data(), rf.size() * sizeof(float));
+    put(tr ? aReachD1 : aReachD0, q, opp.w.data(), opp.w.size() * sizeof(double));
+  }
+  GB_CK(cudaMemsetAsync(d.counter + slot, 0, sizeof(int), d.stream));
+
+  rec.rootCfvQ = L.rows[0].cfvQ;
+  rec.rootRegQ = L.nodes[0].regQ;
+  rec.depth = (int)L.fwdTasks[0].size();
+  const unsigned nodeShift = (unsigned)off[rNode] << 8;
+  for (int tr = 0; tr < 2; ++tr) {
+    rec.fwd[tr] = std::move(L.fwdTasks[tr]);
+    rec.bwd[tr] = std::move(L.bwdTasks[tr]);
+    for (auto* lists : {&rec.fwd[tr], &rec.bwd[tr]})
+      for (auto& v : *lists)
+        for (int& task : v) task = (int)((unsigned)task + nodeShift);
+  }
+  // The host tables are on the device now; keep only what queries need.
+  GB_CK(cudaStreamSynchronize(d.stream));
+  L.termVal = {};
+  L.children = {};
+  L.poolU8 = {};
+  L.poolU16 = {};
+  L.poolI16 = {};
+  L.poolSd = {};
+  L.states = {};
+  d.used += s->bytes;
+  rec.spot = std::move(s);
+  d.live[slot] = std::move(rec);
+  d.dirty = true;
+  return slot;
+}
+
+std::unique_ptr<CompiledSpot> Forest::retire(int slot) {
+  Dev& d = *d_;
+  auto it = d.live.find(slot);
+  if (it == d.live.end()) throw Error{PPS_GB_E_INDEX, "forest: no spot in slot"};
+  SlotRec& rec = it->second;
+  for (int r = 0; r < kRegions; ++r) d.regions[r].release(rec.off[r], rec.size[r], kGranule[r]);
+  std::unique_ptr<CompiledSpot> s = std::move(rec.spot);
+  d.used -= s->bytes;
+  d.live.erase(it);
+  d.freeSlots.push_back(slot);
+  d.dirty = true;
+  return s;
+}
+
+std::vector<int> Forest::slots() const {
+  std::vector<int> out;
+  for (const auto& kv : d_->live) out.push_back(kv.first);
+  return out;
+}
+
+const CompiledSpot& Forest::spot(int slot) const { return *d_->live.at(slot).spot; }
+int Forest::iterations(int slot) const { return d_->live.at(slot).iters; }
+int Forest::maxIterations() const { return d_->coefEntries; }
+
+namespace {
+
+// Concatenates the listed spots' task lists: per traverser, forward lists
+// per depth and backward lists per depth (terminal head, interior tail
+// when `split`). Returns the refs into `all`.
+struct Lists {
+  std::vector<int> all;
+  std::vector<ListRef> fwd[2], term[2], inner[2], bwd[2];
+};
+
+Lists gather(const std::map<int, SlotRec>& live, const std::vector<int>& slots) {
+  Lists out;
+  int D = 0;
+  for (int s : slots) D = std::max(D, live.at(s).depth);
+  for (int tr = 0; tr < 2; ++tr) {
+    out.fwd[tr].resize(D);
+    out.term[tr].resize(D);
+    out.inner[tr].resize(D);
+    out.bwd[tr].resize(D);
+    for (int dd = 0; dd < D; ++dd) {
+      const int f0 = (int)out.all.size();
+      for (int s : slots) {
+        const SlotRec& r = live.at(s);
+        if (dd < r.depth)
+          out.all.insert(out.all.end(), r.fwd[tr][dd].begin(), r.fwd[tr][dd].end());
+      }
+      out.fwd[tr][dd] = ListRef{f0, (int)out.all.size() - f0};
+      const int b0 = (int)out.all.size();
+      for (int s : slots) {
+        const SlotRec& r = live.at(s);
+        if (dd >= r.depth) continue;
+        const auto& v = r.bwd[tr][dd];
+        out.all.insert(out.all.end(), v.begin(), v.begin() + terminalCount(v));
+      }
+      const int i0 = (int)out.all.size();
+      for (int s : slots) {
+        const SlotRec& r = live.at(s);
+        if (dd >= r.depth) continue;
+        const auto& v = r.bwd[tr][dd];
+        out.all.insert(out.all.end(), v.begin() + terminalCount(v), v.end());
+      }
+      const int e = (int)out.all.size();
+      out.term[tr][dd] = ListRef{b0, i0 - b0};
+      out.inner[tr][dd] = ListRef{i0, e - i0};
+      out.bwd[tr][dd] = ListRef{b0, e - b0};
+    }
+  }
+  return out;
+}
+
+}  // namespace
+
+void Forest::iterate(int n) {
+  Dev& d = *d_;
+  if (d.live.empty() || n <= 0) return;
+  for (const auto& kv : d.live)
+    if (kv.second.iters + n > d.coefEntries)
+      throw Error{PPS_GB_E_STATE, "forest: a spot would run past the schedule table"};
+  if (d.dirty || !d.exec) {
+    d.dropGraph();
+    const std::vector<int> all = slots();
+    Lists ls = gather(d.live, all);
+    ensureBuf(d.tasks, d.tasksCap, std::max<size_t>(ls.all.size(), 1));
+    if (!ls.all.empty())
+      GB_CK(cudaMemcpyAsync(d.tasks, ls.all.data(), ls.all.size() * sizeof(int),
+                            cudaMemcpyHostToDevice, d.stream));
+    d.plan.clear();
+    for (int tr = 0; tr < 2; ++tr) {
+      const int D = (int)ls.fwd[tr].size();
+      for (int dd = 0; dd < D; ++dd)
+        if (ls.fwd[tr][dd].count) d.plan.push_back({kFwd, tr, ls.fwd[tr][dd], 0.0});
+      for (int dd = D - 1; dd >= 0; --dd) {
+        const ListRef lt = ls.term[tr][dd], li = ls.inner[tr][dd];
+        if (lt.count) d.plan.push_back({kBwdTerm, tr, lt, 0.0, li.count > 0});
+        if (li.count) d.plan.push_back({kBwdInt, tr, li, 0.0});
+      }
+    }
+    d.plan.push_back({kCounter, 0, ListRef{}, 0.0});
+    const int maxN = d.maxN(all);
+    const size_t smem = bwdScratchBytes<float>(maxN);
+    raiseSmemLimit((const void*)bwdTerminalK<float>, smem);
+    const PlanArgs args{d.tree(), d.rows<float>(aReachF0, aReachF1, aCfvF), d.tasks, d.counter,
+                        (int)d.counterCap, maxN, smem};
+    GB_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
+    issuePlan(d.plan, d.br, [&](const Launch& l, cudaStream_t s) { issueLaunch(args, l, s); });
+    const cudaError_t launchErr = cudaGetLastError();
+    cudaGraph_t g = nullptr;
+    const cudaError_t endErr = cudaStreamEndCapture(d.stream, &g);
+    if (launchErr != cudaSuccess || endErr != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      GB_CK(launchErr);
+      GB_CK(endErr);
+    }
+    d.graph = g;
+    GB_CK(cudaGraphInstantiate(&d.exec, d.graph, 0));
+    d.dirty = false;
+    ++d.captures;
+  }
+  GB_CK(cudaEventRecord(d.evA, d.stream));
+  for (int i = 0; i < n; ++i) GB_CK(cudaGraphLaunch(d.exec, d.stream));
+  GB_CK(cudaEventRecord(d.evB, d.stream));
+  d.timed = true;
+  for (auto& kv : d.live) kv.second.iters += n;
+}
+
+double Forest::lastIterateMs() {
+  Dev& d = *d_;
+  if (!d.timed) return 0.0;
+  GB_CK(cudaEventSynchronize(d.evB));
+  float ms = 0.0f;
+  GB_CK(cudaEventElapsedTime(&ms, d.evA, d.evB));
+  return ms;
+}
+
+std::vector<double> Forest::walkValues(const std::vector<int>& slots, int tr, int mode) {
+  Dev& d = *d_;
+  std::vector<double> out(slots.size(), 0.0);
+  if (slots.empty()) return out;
+  Lists ls = gather(d.live, slots);
+  ensureBuf(d.wTasks, d.wTasksCap, std::max<size_t>(ls.all.size(), 1));
+  if (!ls.all.empty())
+    GB_CK(cudaMemcpyAsync(d.wTasks, ls.all.data(), ls.all.size() * sizeof(int),
+                          cudaMemcpyHostToDevice, d.stream));
+  const int maxN = d.maxN(slots);
+  const size_t smem = bwdScratchBytes<double>(maxN);
+  raiseSmemLimit((const void*)bwdLevelK<double>, smem);
+  const DevTree tree = d.tree();
+  const DevRows<double> rows = d.rows<double>(aReachD0, aReachD1, aCfvD);
+  const int D = (int)ls.fwd[tr].size();
+  for (int dd = 0; dd < D; ++dd) {
+    const ListRef a = ls.fwd[tr][dd];
+    if (a.count)
+      fwdLevelK<double><<<gridOf(a.count), kThreads, 0, d.stream>>>(tree, rows, d.wTasks + a.off,
+                                                                   a.count, tr, 1);
+  }
+  for (int dd = D - 1; dd >= 0; --dd) {
+    const ListRef b = ls.bwd[tr][dd];
+    if (b.count)
+      bwdLevelK<double><<<gridOf(b.count), kThreads, smem, d.stream>>>(
+          tree, rows, d.wTasks + b.off, b.count, tr, mode, maxN);
+  }
+  std::vector<RootInfo> info(slots.size());
+  for (size_t i = 0; i < slots.size(); ++i) {
+    const SlotRec& r = d.live.at(slots[i]);
+    info[i].cfvQ = r.rootCfvQ;
+    info[i].wOff = (int)r.off[rW] + (tr == 0 ? 0 : r.spot->tree.side[0].n);
+    info[i].n = r.spot->tree.side[tr].n;
+    info[i].pad = 0;
+  }
+  ensureBuf(d.info, d.infoCap, info.size());
+  ensureBuf(d.vals, d.valsCap, info.size());
+  GB_CK(cudaMemcpyAsync(d.info, info.data(), info.size() * sizeof(RootInfo),
+                        cudaMemcpyHostToDevice, d.stream));
+  rootValueK<<<(unsigned)info.size(), 128, 0, d.stream>>>(
+      static_cast<const double*>(d.arr[aCfvD]), static_cast<const double*>(d.arr[aW]), d.info,
+      d.vals);
+  GB_CK(cudaGetLastError());
+  GB_CK(cudaMemcpyAsync(out.data(), d.vals, out.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                        d.stream));
+  GB_CK(cudaStreamSynchronize(d.stream));
+  for (size_t i = 0; i < slots.size(); ++i) {
+    const double Z = d.live.at(slots[i]).spot->pairMass;
+    out[i] = Z > 0.0 ? out[i] / Z : 0.0;
+  }
+  return out;
+}
+
+std::vector<float> Forest::rootRows(int slot) {
+  Dev& d = *d_;
+  const SlotRec& r = d.live.at(slot);
+  const Tree& t = r.spot->tree;
+  const Node& root = t.nodes[0];
+  if (root.kind != kDecide) return {};
+  const int n = t.n(0, root.player);
+  const size_t stride = quads(n) * 4;
+  std::vector<float> padded(stride * root.na), out((size_t)n * root.na);
+  GB_CK(cudaMemcpyAsync(padded.data(), d.at<float>(aStr, r.rootRegQ),
+                        padded.size() * sizeof(float), cudaMemcpyDeviceToHost, d.stream));
+  GB_CK(cudaStreamSynchronize(d.stream));
+  for (int a = 0; a < root.na; ++a)
+    std::copy(padded.begin() + a * stride, padded.begin() + a * stride + n,
+              out.begin() + (size_t)a * n);
+  return out;
+}
+
+void Forest::sync() { GB_CK(cudaStreamSynchronize(d_->stream)); }
+
+size_t Forest::deviceBytes() const {
+  const Dev& d = *d_;
+  size_t b = (size_t)d.coefEntries * 3 * sizeof(float) + d.counterCap * sizeof(int) +
+             d.tasksCap * sizeof(int) + d.wTasksCap * sizeof(int) +
+             d.infoCap * sizeof(RootInfo) + d.valsCap * sizeof(double);
+  for (size_t x : d.arrBytes) b += x;
+  return b;
+}
+
+size_t Forest::usedBytes() const { return d_->used; }
+int Forest::captures() const { return d_->captures; }
+int Forest::launchesPerIteration() const { return (int)d_->plan.size(); }
+
+}  // namespace gb
+}  // namespace pps

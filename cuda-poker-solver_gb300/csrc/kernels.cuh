@@ -44,7 +44,8 @@ struct DevTree {
   float* regret;
   float* strat;
   const float* coef;     // 3 floats per iteration: pos, neg, avg
-  const int* counter;    // current iteration index
+  const int* counter;    // current iteration index, per spot (node meta
+                         // bits 16-31; a lone spot is spot 0)
 };
 
 template <typename T>
@@ -56,6 +57,7 @@ struct DevRows {
 __device__ __forceinline__ int nodeKind(int meta) { return meta & 3; }
 __device__ __forceinline__ int nodePlayer(int meta) { return (meta >> 2) & 1; }
 __device__ __forceinline__ int nodeCount(int meta) { return (meta >> 8) & 0xff; }
+__device__ __forceinline__ int nodeSpot(int meta) { return (int)((unsigned)meta >> 16); }
 __device__ __forceinline__ int quadsOf(int n) { return (n + 3) >> 2; }
 
 // ---- quad load/store ----
@@ -221,7 +223,7 @@ fwdLevelK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int count, 
           int sigSrc) {
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
     const int w = tasks[i];
-    const int node = w >> 8, sub = (w >> 2) & 63;
+    const int node = (int)((unsigned)w >> 8), sub = (w >> 2) & 63;
     if ((w & 3) == kTaskDecide) fwdDecideChunk<T>(t, rows, node, sub, tr, sigSrc);
     else fwdChanceBranch<T>(t, rows, node, sub, tr);
   }
@@ -563,7 +565,7 @@ __device__ void decideChunk(const DevTree& t, const DevRows<T>& rows, int u, int
   const T uniform = T(1) / T(na);
   float pos = 0.f, neg = 0.f, avg = 0.f;
   if (mode == kModeCFR) {
-    const float* c = t.coef + (size_t)(*t.counter) * 3;
+    const float* c = t.coef + (size_t)t.counter[nodeSpot(nd.meta)] * 3;
     pos = c[0];
     neg = c[1];
     avg = c[2];
@@ -642,7 +644,7 @@ bwdLevelK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int count, 
   const Scratch<T> ws = scratchOf<T>(smem, maxN);
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
     const int w = tasks[i];
-    const int node = w >> 8, sub = (w >> 2) & 63;
+    const int node = (int)((unsigned)w >> 8), sub = (w >> 2) & 63;
     switch (w & 3) {
       case kTaskShowdown: showdownNode<T>(t, rows, node, tr, ws); break;
       case kTaskFold: foldNode<T>(t, rows, node, tr, ws); break;
@@ -666,8 +668,8 @@ bwdTerminalK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int coun
   const Scratch<T> ws = scratchOf<T>(smem, maxN);
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
     const int w = tasks[i];
-    if ((w & 3) == kTaskShowdown) showdownNode<T>(t, rows, w >> 8, tr, ws);
-    else foldNode<T>(t, rows, w >> 8, tr, ws);
+    if ((w & 3) == kTaskShowdown) showdownNode<T>(t, rows, (int)((unsigned)w >> 8), tr, ws);
+    else foldNode<T>(t, rows, (int)((unsigned)w >> 8), tr, ws);
     __syncthreads();
   }
 }
@@ -679,7 +681,7 @@ bwdInteriorK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int coun
   __shared__ __align__(16) unsigned char smem[kChanceScratchBytes];
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
     const int w = tasks[i];
-    const int node = w >> 8, sub = (w >> 2) & 63;
+    const int node = (int)((unsigned)w >> 8), sub = (w >> 2) & 63;
     if ((w & 3) == kTaskChance) chanceChunk<T>(t, rows, node, sub, tr, smem);
     else decideChunk<T>(t, rows, node, sub, tr, mode);
     __syncthreads();
@@ -687,8 +689,9 @@ bwdInteriorK(DevTree t, DevRows<T> rows, const int* __restrict__ tasks, int coun
 }
 
 // Internal linkage: this header is included by more than one translation unit.
-static __global__ void advanceCounterK(int* counter) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) ++(*counter);
+static __global__ void advanceCounterK(int* counter, int spots) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < spots; i += gridDim.x * blockDim.x)
+    ++counter[i];
 }
 
 }  // namespace gb

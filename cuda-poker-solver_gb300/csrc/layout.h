@@ -28,7 +28,8 @@ namespace gb {
 enum WalkMode : int { kModeCFR = 0, kModeEV = 1, kModeBR = 2 };
 
 // Packed node word: kind (bits 0-1), player (bit 2), foldBy (bit 3),
-// na or branch count (bits 8-15).
+// na or branch count (bits 8-15); a forest stores the spot's slot in bits
+// 16-31 (its iteration counter).
 inline int packNode(int kind, int player, int foldBy, int na) {
   return kind | (player << 2) | (foldBy << 3) | (na << 8);
 }

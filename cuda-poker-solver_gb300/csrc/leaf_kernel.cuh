@@ -11,13 +11,10 @@
 #include "compiler.h"
 #include "kernels.cuh"
 #include "layout.h"
+#include "plan.cuh"
 
 namespace pps {
 namespace gb {
-
-struct ListRef {
-  int off = 0, count = 0;
-};
 
 struct LeafPlan {
   bool ok = false;

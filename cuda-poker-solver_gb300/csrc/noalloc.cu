@@ -29,6 +29,7 @@
 #include "kernels.cuh"
 #include "layout.h"
 #include "noalloc.h"
+#include "plan.cuh"
 #include "pps_gb.h"
 #include "solver.h"
 
@@ -224,8 +225,7 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
   const int* dTasks = reinterpret_cast<const int*>(base + oTasks);
 
   const size_t smem = bwdScratchBytes<float>(L.maxN);
-  NA_CK(cudaFuncSetAttribute(bwdLevelK<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem));
+  raiseSmemLimit((const void*)bwdLevelK<float>, smem);
   auto grid = [](int count) { return (unsigned)std::min(count, 1 << 20); };
   for (int it = 0; it < iterations; ++it) {
     for (int tr = 0; tr < 2; ++tr) {
@@ -238,7 +238,7 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
           bwdLevelK<float><<<grid(bwd[tr][d].second), kThreads, smem, stream>>>(
               tree, rows, dTasks + bwd[tr][d].first, bwd[tr][d].second, tr, kModeCFR, L.maxN);
     }
-    advanceCounterK<<<1, 32, 0, stream>>>(counter);
+    advanceCounterK<<<1, 32, 0, stream>>>(counter, 1);
     NA_CK(cudaGetLastError());
   }
   repackK<<<gMap, 128, 0, stream>>>(map, nMap, reg, dRegret, 0);

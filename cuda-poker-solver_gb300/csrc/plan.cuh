@@ -1,0 +1,131 @@
+// Launch plans shared by the single-spot engine and the forest: a DCFR
+// iteration is a list of level launches (kernel, task list, traverser,
+// algorithmic bytes), issued on a main stream with independent pairs forked
+// onto a side stream (graph branches when captured).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "compiler.h"
+#include "kernels.cuh"
+#include "pps_gb.h"
+
+namespace pps {
+namespace gb {
+
+#define GB_CK(call)                                                          \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      throw Error{e_ == cudaErrorMemoryAllocation ? PPS_GB_E_MEMORY          \
+                                                  : PPS_GB_E_CUDA,           \
+                  std::string("CUDA error: ") + cudaGetErrorString(e_) +     \
+                      " (" #call ")"};                                       \
+  } while (0)
+
+struct ListRef {
+  int off = 0, count = 0;
+};
+
+enum LaunchKind { kFwd, kBwd, kBwdTerm, kBwdInt, kLeafSweep, kCounter };
+inline const char* launchName(LaunchKind k) {
+  static const char* names[] = {"fwd_level", "bwd_level", "bwd_terminal", "bwd_interior",
+                                "leaf_street", "counter"};
+  return names[k];
+}
+
+struct Launch {
+  LaunchKind kind;
+  int tr;
+  ListRef list;
+  double bytes;           // algorithmic bytes of this launch (f32 rows)
+  bool withNext = false;  // independent of the next launch: run both at once
+};
+
+// What the level launches of a plan read: the tree, the f32 rows, the
+// concatenated task lists, the per-spot counters.
+struct PlanArgs {
+  DevTree tree;
+  DevRows<float> rows;
+  const int* tasks;
+  int* counter;
+  int spots;    // counters advanced per iteration
+  int maxN;     // largest combo list (shared scratch layout)
+  size_t smem;  // bwdScratchBytes<float>(maxN)
+};
+
+inline unsigned gridOf(int count) { return (unsigned)std::min(count, 1 << 20); }
+
+// One CFR-mode launch of the plan on stream s (kLeafSweep is issued by the
+// engine that owns a leaf plan).
+inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t s) {
+  const unsigned g = gridOf(l.list.count);
+  const int* tk = a.tasks + l.list.off;
+  switch (l.kind) {
+    case kFwd:
+      fwdLevelK<float><<<g, kThreads, 0, s>>>(a.tree, a.rows, tk, l.list.count, l.tr, 0);
+      break;
+    case kBwd:
+      bwdLevelK<float><<<g, kThreads, a.smem, s>>>(a.tree, a.rows, tk, l.list.count, l.tr,
+                                                   kModeCFR, a.maxN);
+      break;
+    case kBwdTerm:
+      bwdTerminalK<float><<<g, kThreads, a.smem, s>>>(a.tree, a.rows, tk, l.list.count, l.tr,
+                                                      a.maxN);
+      break;
+    case kBwdInt:
+      bwdInteriorK<float><<<g, kThreads, 0, s>>>(a.tree, a.rows, tk, l.list.count, l.tr,
+                                                 kModeCFR);
+      break;
+    case kCounter:
+      advanceCounterK<<<(a.spots + 255) / 256, 256, 0, s>>>(a.counter, a.spots);
+      break;
+    case kLeafSweep:
+      break;
+  }
+}
+
+// Streams and events of a two-branch plan.
+struct Branches {
+  cudaStream_t main = nullptr, side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+// Issues a plan; a launch marked withNext runs beside the next one on the
+// side stream, forked from and joined back into the main stream. `one`
+// issues a single launch (so callers can add launch kinds of their own).
+template <typename IssueOne>
+void issuePlan(const std::vector<Launch>& P, const Branches& b, IssueOne&& one) {
+  for (size_t i = 0; i < P.size(); ++i) {
+    if (P[i].withNext && i + 1 < P.size()) {
+      GB_CK(cudaEventRecord(b.fork, b.main));
+      GB_CK(cudaStreamWaitEvent(b.side, b.fork, 0));
+      one(P[i], b.main);
+      one(P[i + 1], b.side);
+      GB_CK(cudaEventRecord(b.join, b.side));
+      GB_CK(cudaStreamWaitEvent(b.main, b.join, 0));
+      ++i;
+    } else {
+      one(P[i], b.main);
+    }
+  }
+}
+
+// Splits a backward level list (sorted showdown, fold, chance, decide) into
+// its terminal head and interior tail.
+inline int terminalCount(const std::vector<int>& v) {
+  int nt = 0;
+  while (nt < (int)v.size() && (v[nt] & 3) >= 2) ++nt;
+  return nt;
+}
+
+// Raises the dynamic shared-memory limit of a kernel to at least `bytes`
+// (never lowers it: graphs captured earlier keep their launch sizes valid).
+void raiseSmemLimit(const void* kernel, size_t bytes);
+
+}  // namespace gb
+}  // namespace pps

@@ -278,8 +278,6 @@ pf::NodeStats SolverCore::stats() {
 // Strategy queries.
 // ---------------------------------------------------------------------------
 
-namespace {
-
 // Range-weighted average frequencies over a first-street node's rows.
 std::vector<double> aggregate(const std::vector<float>& rows, int na, int nC,
                               const std::vector<double>& w) {
@@ -299,6 +297,8 @@ std::vector<double> aggregate(const std::vector<float>& rows, int na, int nC,
   }
   return freq;
 }
+
+namespace {
 
 gpu::ActionLabel label(const pf::TreeAction& a) { return {a.kind, a.amount}; }
 

@@ -26,6 +26,11 @@ struct Schedule {
   void coefs(int t, int iters, double out[3]) const;
 };
 
+// Range-weighted average action frequencies of a decide node whose rows
+// (na x nC, dense, cumulative strategy) belong to combos weighted w.
+std::vector<double> aggregate(const std::vector<float>& rows, int na, int nC,
+                              const std::vector<double>& w);
+
 class SolverCore {
  public:
   SolverCore(const gpu::PostflopSpot& spot, const gpu::StreetBetConfigs& cfgs,

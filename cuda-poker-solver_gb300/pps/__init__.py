@@ -2,6 +2,7 @@
 
 The same programmatic surface as the reference's ``pps`` package
 (python/pps/__init__.py:22-31): ``pps.Solver`` is ``pps.pps_native.Solver``.
+``pps.Batch`` (an extension) solves many spots at once on one GPU.
 
     import pps
     s = pps.Solver(board="Qs9h2d", oop="TT+,AKo", ip="AQ+,KQs",
@@ -14,10 +15,12 @@ The native library (libpps_gb.so, sm_103a) is built in-tree by
 raises ImportError.
 """
 
-__all__ = ["Solver", "__version__"]
+__all__ = ["Solver", "Batch", "__version__"]
 
 __version__ = "0.1.0"
 
 from . import pps_native as _native  # noqa: E402
 
 Solver = _native.Solver
+
+from .batch import Batch  # noqa: E402

@@ -16,7 +16,7 @@ COMBOS = 1326
 MAX_SIZES = 16
 
 E_OK, E_ARG, E_INDEX, E_STATE, E_IO, E_FORMAT, E_CUDA, E_MEMORY, E_DEVICE, E_BUDGET, \
-    E_TOO_WIDE = range(11)
+    E_TOO_WIDE, PENDING = range(12)
 
 
 class BetConfig(C.Structure):
@@ -60,6 +60,32 @@ class DecideInfo(C.Structure):
     _fields_ = [("node_id", C.c_int32), ("player", C.c_int32), ("depth", C.c_int32),
                 ("n_board", C.c_int32), ("n_combos", C.c_int32), ("n_actions", C.c_int32),
                 ("actions", Action * MAX_ACTIONS), ("children", C.c_int32 * MAX_ACTIONS)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("hbm_budget", C.c_int64), ("check_every", C.c_int32),
+                ("max_iterations", C.c_int32), ("compile_threads", C.c_int32),
+                ("algo", C.c_char * 16)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("ticket", C.c_int64), ("status", C.c_int32), ("converged", C.c_int32),
+                ("iterations", C.c_int32), ("num_nodes", C.c_int32), ("ev0", C.c_double),
+                ("ev1", C.c_double), ("exploitability", C.c_double), ("target", C.c_double),
+                ("pair_mass", C.c_int64), ("submit_ms", C.c_double), ("admit_ms", C.c_double),
+                ("finish_ms", C.c_double), ("device_bytes", C.c_int64),
+                ("root_actions", C.c_int32), ("root_combos", C.c_int32),
+                ("root_action", Action * MAX_ACTIONS), ("root_freqs", C.c_double * MAX_ACTIONS),
+                ("error", C.c_char * 160)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in (
+        "submitted", "compiling", "waiting", "active", "done", "failed", "used_bytes",
+        "device_bytes", "budget", "epochs", "spot_iterations", "captures", "peak_active",
+        "peak_used_bytes")] + \
+        [("check_every", C.c_int32), ("max_iterations", C.c_int32)] + \
+        [(k, C.c_double) for k in ("admit_ms", "iterate_ms", "check_ms", "retire_ms", "idle_ms")]
 
 
 ARRAY_CB = C.CFUNCTYPE(None, C.c_void_p, C.c_char_p, C.c_char, C.c_void_p, C.c_int64)
@@ -106,6 +132,22 @@ _SIGS = {
     "pps_gb_profile": (C.c_int, [H, C.c_int, C.c_int, P(KernelStat), C.c_int, P(C.c_int)]),
     "pps_gb_solve_noalloc": (C.c_int, [P(Spot), P(BetConfig), C.c_void_p, C.c_void_p, C.c_int64,
                                        C.c_int, C.c_int, C.c_void_p, P(C.c_int64)]),
+    "pps_gb_batch_config_default": (None, [P(BatchConfig)]),
+    "pps_gb_batch_create": (C.c_int, [P(BatchConfig), P(H)]),
+    "pps_gb_batch_destroy": (None, [H]),
+    "pps_gb_batch_set_budget": (C.c_int, [H, C.c_int64]),
+    "pps_gb_batch_submit": (C.c_int, [H, P(Spot), P(BetConfig), C.c_int, C.c_double,
+                                      P(C.c_int64)]),
+    "pps_gb_batch_run": (C.c_int, [H, C.c_double]),
+    "pps_gb_batch_start": (C.c_int, [H]),
+    "pps_gb_batch_stop": (C.c_int, [H]),
+    "pps_gb_batch_poll": (C.c_int, [H, C.c_int64, P(BatchResult)]),
+    "pps_gb_batch_wait": (C.c_int, [H, C.c_int64, C.c_double, P(BatchResult)]),
+    "pps_gb_batch_collect": (C.c_int, [H, P(BatchResult), C.c_int, P(C.c_int)]),
+    "pps_gb_batch_root_rows": (C.c_int, [H, C.c_int64, P(C.c_float), C.c_int64,
+                                         P(C.c_int64)]),
+    "pps_gb_batch_get_info": (C.c_int, [H, P(BatchInfo)]),
+    "pps_gb_batch_footprint": (C.c_int, [P(Spot), P(BetConfig), C.c_int, P(C.c_int64)]),
     "pps_gb_compile_export": (C.c_int, [P(Spot), P(BetConfig), C.c_int, ARRAY_CB, C.c_void_p]),
     "pps_gb_hand_keys": (C.c_int, [P(C.c_uint8), C.c_int, P(C.c_uint64)]),
     "pps_gb_bet_actions": (C.c_int, [C.c_int64, C.c_int64, P(BetConfig), C.c_int64, C.c_int64,

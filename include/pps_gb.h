@@ -37,7 +37,8 @@ enum {
   PPS_GB_E_MEMORY = 7,      /* host or device allocation failed */
   PPS_GB_E_DEVICE = 8,      /* a kernel raised its device error flag */
   PPS_GB_E_BUDGET = 9,      /* admission refused: over the HBM budget */
-  PPS_GB_E_TOO_WIDE = 10    /* more than PPS_GB_MAX_ACTIONS actions */
+  PPS_GB_E_TOO_WIDE = 10,   /* more than PPS_GB_MAX_ACTIONS actions */
+  PPS_GB_PENDING = 11       /* batch request not finished yet (not an error) */
 };
 
 typedef struct pps_gb_solver pps_gb_solver;
@@ -264,6 +265,99 @@ int pps_gb_solve_noalloc(const pps_gb_spot* spot, const pps_gb_bet_config* cfg,
                          float* d_regret, float* d_strat, int64_t row_capacity,
                          int first_iteration, int iterations, void* stream,
                          int64_t* n_rows);
+
+/* ---------------------------------------------------------------------
+ * Batched and served solving. No reference counterpart: the reference
+ * solves one spot per GpuPostflopSolver (cuda/gpu_cfr.h:141-264) and its
+ * API server serialises solves behind one lock (python/pps_api.py). Here
+ * many spots are resident on the GPU at once and share every launch:
+ * submit() queues a spot (compiled on host threads), a driver admits
+ * compiled spots in submission order while the sum of their device
+ * footprints fits the HBM budget, runs check_every DCFR iterations of all
+ * resident spots per epoch (one CUDA graph), checks each spot's
+ * exploitability with FP64 best-response walks and retires it once it is
+ * at or below its target (or at max_iterations), with FP64 EV walks.
+ * Requests submitted while others run are admitted as memory frees up, so
+ * their work overlaps on the device. A spot's result does not depend on the
+ * other resident spots (same rows, same checks, same iteration count).
+ * All pps_gb_batch_* calls may come from any thread.
+ * --------------------------------------------------------------------- */
+typedef struct pps_gb_batch pps_gb_batch;
+
+typedef struct {
+  int64_t hbm_budget;      /* device bytes resident spots may occupy (0: 80% of free) */
+  int32_t check_every;     /* DCFR iterations between checks (0: 64) */
+  int32_t max_iterations;  /* per spot, rounded up to a multiple of check_every (0: 4096) */
+  int32_t compile_threads; /* host compile threads (0: hardware threads, at most 16) */
+  char algo[16];           /* "dcfr" (default), "dcfr-g2", "dcfr-noreset", "dcfr-g2-noreset" */
+} pps_gb_batch_config;
+
+typedef struct {
+  int64_t ticket;
+  int32_t status;      /* PPS_GB_OK, or this request's error (pps_gb_batch_result.error) */
+  int32_t converged;   /* 1: exploitability <= target at the last check */
+  int32_t iterations;  /* DCFR iterations run */
+  int32_t num_nodes;
+  double ev0, ev1, exploitability, target; /* chips (pf::NodeStats fields) */
+  int64_t pair_mass;                        /* pf::NodeStats::pairMass */
+  double submit_ms, admit_ms, finish_ms;    /* ms since the batch was created */
+  int64_t device_bytes;                     /* the spot's device footprint */
+  int32_t root_actions; /* actions at the root decide node (0: root is no decision) */
+  int32_t root_combos;  /* root actor's combos (rows of pps_gb_batch_root_rows) */
+  pps_gb_action root_action[PPS_GB_MAX_ACTIONS];
+  double root_freqs[PPS_GB_MAX_ACTIONS];    /* range-weighted root strategy */
+  char error[160];
+} pps_gb_batch_result;
+
+typedef struct {
+  int64_t submitted, compiling, waiting, active, done, failed;
+  int64_t used_bytes;   /* footprints of the resident spots */
+  int64_t device_bytes; /* pool capacity held on the device */
+  int64_t budget;
+  int64_t epochs, spot_iterations, captures, peak_active;
+  int64_t peak_used_bytes; /* largest used_bytes seen (never above budget) */
+  int32_t check_every, max_iterations;
+  /* Driver time split (ms): admission (uploads), DCFR iterations (CUDA
+   * events), iterations plus best-response checks (wall), EV walks and
+   * retirement, waiting for compiles. */
+  double admit_ms, iterate_ms, check_ms, retire_ms, idle_ms;
+} pps_gb_batch_info;
+
+void pps_gb_batch_config_default(pps_gb_batch_config* cfg);
+/* Creates a batch on the current CUDA device. */
+int pps_gb_batch_create(const pps_gb_batch_config* cfg, pps_gb_batch** out);
+/* Stops the serve thread (if any) and frees everything. NULL is ignored. */
+void pps_gb_batch_destroy(pps_gb_batch* b);
+int pps_gb_batch_set_budget(pps_gb_batch* b, int64_t bytes);
+/* Queues a spot (target: exploitability in chips; <= 0 runs to
+ * max_iterations). cfgs holds 1 config (all streets) or 3 (per street). */
+int pps_gb_batch_submit(pps_gb_batch* b, const pps_gb_spot* spot,
+                        const pps_gb_bet_config* cfgs, int n_cfgs,
+                        double target, int64_t* ticket);
+/* Drives the batch on the calling thread until every submitted request has
+ * finished (PPS_GB_OK) or timeout_s (> 0) passed (PPS_GB_PENDING). */
+int pps_gb_batch_run(pps_gb_batch* b, double timeout_s);
+/* Serve mode: a library thread drives the batch until pps_gb_batch_stop. */
+int pps_gb_batch_start(pps_gb_batch* b);
+int pps_gb_batch_stop(pps_gb_batch* b);
+/* PPS_GB_OK with *out filled once the request finished, else PPS_GB_PENDING. */
+int pps_gb_batch_poll(pps_gb_batch* b, int64_t ticket, pps_gb_batch_result* out);
+/* Blocks until the request finished or timeout_s (> 0) passed. */
+int pps_gb_batch_wait(pps_gb_batch* b, int64_t ticket, double timeout_s,
+                      pps_gb_batch_result* out);
+/* Moves up to cap finished results (ticket order) into out; their tickets
+ * are forgotten afterwards. */
+int pps_gb_batch_collect(pps_gb_batch* b, pps_gb_batch_result* out, int cap,
+                         int* n_out);
+/* Cumulative root strategy rows of a finished, uncollected request
+ * (root_actions x root_combos floats, action-major). */
+int pps_gb_batch_root_rows(pps_gb_batch* b, int64_t ticket, float* out,
+                           int64_t cap, int64_t* n_out);
+int pps_gb_batch_get_info(pps_gb_batch* b, pps_gb_batch_info* out);
+/* Host only: the device bytes a spot occupies in a batch. */
+int pps_gb_batch_footprint(const pps_gb_spot* spot,
+                           const pps_gb_bet_config* cfgs, int n_cfgs,
+                           int64_t* bytes);
 
 /* Host-only compile (no device use): runs the tree compiler and reports
  * every artifact in the reference's own layout (cuda/gpu_cfr.cu:1331-1827)
