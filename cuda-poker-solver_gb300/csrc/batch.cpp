@@ -50,7 +50,10 @@ BatchServer::BatchServer(const BatchConfig& cfg) : cfg_(cfg), t0_(std::chrono::s
     cudaCheck(cudaMemGetInfo(&freeB, &totalB), "cudaMemGetInfo");
     budget_ = (int64_t)(0.8 * (double)freeB);
   }
-  forest_.reset(new Forest(scheduleTable(s, cfg_.maxIterations)));
+  size_t freeB = 0, totalB = 0;
+  cudaCheck(cudaMemGetInfo(&freeB, &totalB), "cudaMemGetInfo");
+  forest_.reset(new Forest(scheduleTable(s, cfg_.maxIterations),
+                           std::max<size_t>(totalB, (size_t)std::max<int64_t>(budget_, 0))));
   stats_.checkEvery = cfg_.checkEvery;
   stats_.maxIterations = cfg_.maxIterations;
   int n = cfg_.threads;
@@ -168,59 +171,58 @@ void BatchServer::finish(int64_t ticket, BatchResult&& r) {
 bool BatchServer::epoch() {
   Forest& F = *forest_;
   const double tStart = nowMs();
-  // Admission in ticket order while the budget allows.
-  std::vector<std::pair<int64_t, std::unique_ptr<CompiledSpot>>> admit;
-  {
-    std::lock_guard<std::mutex> lock(m_);
-    int64_t used = (int64_t)F.usedBytes();
-    bool resident = !F.slots().empty();
-    while (!ready_.empty()) {
-      auto it = ready_.begin();
-      const int64_t b = (int64_t)it->second->bytes;
-      if (b > budget_) {
-        Request& q = reqs_.at(it->first);
-        q.result.status = PPS_GB_E_BUDGET;
-        q.result.error = "spot needs " + std::to_string(b) + " device bytes, budget is " +
-                         std::to_string(budget_);
-        q.result.admitMs = q.result.finishMs = nowMs();
-        q.state = kDone;
-        ++stats_.failed;
-        ++stats_.done;
-        --stats_.waiting;
-        --pending_;
-        ready_.erase(it);
-        cvDone_.notify_all();
-        continue;
-      }
-      if (resident && used + b > budget_) break;
-      used += b;
-      resident = true;
-      admit.emplace_back(it->first, std::move(it->second));
-      ready_.erase(it);
-      --stats_.waiting;
-    }
-  }
-  for (auto& a : admit) {
-    const int64_t ticket = a.first;
-    try {
-      const int slot = F.admit(std::move(a.second));
+  // Admission in ticket order while the forest's device bytes stay within
+  // the budget; a spot that does not fit waits (or fails if it cannot fit
+  // even alone).
+  bool admitted = false;
+  for (;;) {
+    int64_t ticket;
+    std::unique_ptr<CompiledSpot> cs;
+    int64_t budget;
+    {
       std::lock_guard<std::mutex> lock(m_);
-      slotTicket_[slot] = ticket;
-      Request& q = reqs_.at(ticket);
-      q.state = kActive;
-      q.result.admitMs = nowMs();
-      ++stats_.active;
-    } catch (const Error& e) {
-      BatchResult res;
-      {
-        std::lock_guard<std::mutex> lock(m_);
-        res = reqs_.at(ticket).result;
-      }
-      res.status = e.code;
-      res.error = e.msg;
-      res.admitMs = res.finishMs = nowMs();
-      finish(ticket, std::move(res));
+      if (ready_.empty()) break;
+      auto it = ready_.begin();
+      ticket = it->first;
+      cs = std::move(it->second);
+      ready_.erase(it);
+      budget = budget_;
     }
+    int slot = -1;
+    int code = PPS_GB_OK;
+    std::string msg;
+    try {
+      slot = F.admit(cs, budget > 0 ? (size_t)budget : 0);
+    } catch (const Error& e) {
+      code = e.code;
+      msg = e.msg;
+    }
+    if (code == PPS_GB_OK && slot < 0 && F.slots().empty()) {
+      code = PPS_GB_E_BUDGET;
+      msg = "spot needs " + std::to_string(cs->bytes) + " device bytes, budget is " +
+            std::to_string(budget);
+    }
+    std::unique_lock<std::mutex> lock(m_);
+    if (code == PPS_GB_OK && slot < 0) {
+      ready_[ticket] = std::move(cs);  // waits for memory to free up
+      break;
+    }
+    --stats_.waiting;
+    if (code != PPS_GB_OK) {
+      BatchResult res = reqs_.at(ticket).result;
+      res.status = code;
+      res.error = msg;
+      res.admitMs = res.finishMs = nowMs();
+      lock.unlock();
+      finish(ticket, std::move(res));
+      continue;
+    }
+    slotTicket_[slot] = ticket;
+    Request& q = reqs_.at(ticket);
+    q.state = kActive;
+    q.result.admitMs = nowMs();
+    ++stats_.active;
+    admitted = true;
   }
   const std::vector<int> slots = F.slots();
   const double tAdmitted = nowMs();
@@ -232,7 +234,7 @@ bool BatchServer::epoch() {
     stats_.peakUsed = std::max(stats_.peakUsed, stats_.usedBytes);
     stats_.deviceBytes = (int64_t)F.deviceBytes();
   }
-  if (slots.empty()) return !admit.empty();
+  if (slots.empty()) return admitted;
 
   F.iterate(cfg_.checkEvery);
   const std::vector<double> br0 = F.walkValues(slots, 0, kModeBR);

@@ -1,8 +1,8 @@
 // Batched and served solving: a request queue in front of a Forest.
 //
 // submit() hands a spot to a pool of compile threads; compiled spots wait
-// in ticket order and are admitted into the forest while the sum of the
-// resident spots' device footprints stays within the HBM budget. A driver
+// in ticket order and are admitted into the forest while the device memory
+// the forest maps stays within the HBM budget. A driver
 // (run() on the caller's thread, or the thread start() launches) repeats
 // epochs: admit, run `checkEvery` DCFR iterations of every resident spot
 // in one graph, run the FP64 best-response walks, and retire each spot

@@ -2,12 +2,14 @@
 // the all-spots iteration graph and the FP64 check walks.
 #include "forest.h"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
 #include <map>
 #include <string>
+#include <type_traits>
 
 #include "kernels.cuh"
 #include "plan.cuh"
@@ -141,6 +143,58 @@ class RangeAlloc {
   size_t top_ = 0;
 };
 
+// Driver virtual-memory entry points, looked up through the runtime (the
+// library does not link the driver library directly).
+struct DriverVmm {
+  decltype(&::cuMemGetAllocationGranularity) granularity = nullptr;
+  decltype(&::cuMemAddressReserve) reserve = nullptr;
+  decltype(&::cuMemAddressFree) addressFree = nullptr;
+  decltype(&::cuMemCreate) create = nullptr;
+  decltype(&::cuMemRelease) release = nullptr;
+  decltype(&::cuMemMap) map = nullptr;
+  decltype(&::cuMemUnmap) unmap = nullptr;
+  decltype(&::cuMemSetAccess) setAccess = nullptr;
+};
+
+const DriverVmm& vmm() {
+  static const DriverVmm v = [] {
+    DriverVmm d;
+    auto get = [](const char* name, auto& fn) {
+      cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+      void* p = nullptr;
+      GB_CK(cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q));
+      if (q != cudaDriverEntryPointSuccess || !p)
+        throw Error{PPS_GB_E_CUDA, std::string("driver entry point missing: ") + name};
+      fn = reinterpret_cast<std::remove_reference_t<decltype(fn)>>(p);
+    };
+    get("cuMemGetAllocationGranularity", d.granularity);
+    get("cuMemAddressReserve", d.reserve);
+    get("cuMemAddressFree", d.addressFree);
+    get("cuMemCreate", d.create);
+    get("cuMemRelease", d.release);
+    get("cuMemMap", d.map);
+    get("cuMemUnmap", d.unmap);
+    get("cuMemSetAccess", d.setAccess);
+    return d;
+  }();
+  return v;
+}
+
+void cuCheck(CUresult r, const char* what) {
+  if (r != CUDA_SUCCESS)
+    throw Error{r == CUDA_ERROR_OUT_OF_MEMORY ? PPS_GB_E_MEMORY : PPS_GB_E_CUDA,
+                std::string("CUDA driver error ") + std::to_string((int)r) + " (" + what + ")"};
+}
+
+// A device array at a fixed virtual address range: physical memory is
+// mapped at its end as the array grows and unmapped as it shrinks, so the
+// base pointer never moves and growing copies nothing.
+struct VmArray {
+  CUdeviceptr base = 0;
+  size_t reserved = 0, mapped = 0;
+  std::vector<std::pair<CUmemGenericAllocationHandle, size_t>> chunks;  // address order
+};
+
 struct RootInfo {
   uint32_t cfvQ;  // root value row (quads)
   int wOff;       // traverser weights in the weight pool
@@ -210,8 +264,10 @@ struct Forest::Dev {
   cudaEvent_t evA = nullptr, evB = nullptr;  // around the last iterate()
   bool timed = false;
   RangeAlloc regions[kRegions];
-  void* arr[kArrays] = {};
-  size_t arrBytes[kArrays] = {};
+  VmArray va[kArrays];
+  void* arr[kArrays] = {};  // va[a].base
+  int device = 0;
+  size_t gran = 0;          // physical mapping granularity
   float* coef = nullptr;
   int coefEntries = 0;
   int* counter = nullptr;
@@ -272,21 +328,59 @@ struct Forest::Dev {
     graph = nullptr;
     dirty = true;
   }
-  // Grows array a to cover its region, keeping the contents.
+  // Bytes array a maps when its region's top is `top` entries.
+  size_t mappedFor(int a, size_t top) const {
+    return roundUp(top * kArray[a].entryBytes, gran);
+  }
+  // Maps physical memory so array a covers its region.
   void grow(int a) {
-    const size_t need = regions[kArray[a].region].top() * kArray[a].entryBytes;
-    if (need <= arrBytes[a]) return;
-    const size_t nb = roundUp(std::max(need, arrBytes[a] + arrBytes[a] / 2), (size_t)1 << 16);
-    void* p = nullptr;
-    GB_CK(cudaMalloc(&p, nb));
-    if (arr[a]) {
-      GB_CK(cudaMemcpyAsync(p, arr[a], arrBytes[a], cudaMemcpyDeviceToDevice, stream));
-      GB_CK(cudaStreamSynchronize(stream));
-      GB_CK(cudaFree(arr[a]));
+    VmArray& v = va[a];
+    const size_t need = mappedFor(a, regions[kArray[a].region].top());
+    if (need <= v.mapped) return;
+    if (need > v.reserved) throw Error{PPS_GB_E_BUDGET, "forest: pool address range exhausted"};
+    const DriverVmm& dv = vmm();
+    const size_t add = need - v.mapped;
+    CUmemAllocationProp prop{};
+    prop.type = CU_MEM_ALLOCATION_TYPE_PINNED;
+    prop.location.type = CU_MEM_LOCATION_TYPE_DEVICE;
+    prop.location.id = device;
+    CUmemGenericAllocationHandle h = 0;
+    cuCheck(dv.create(&h, add, &prop, 0), "cuMemCreate");
+    CUresult r = dv.map(v.base + v.mapped, add, 0, h, 0);
+    if (r != CUDA_SUCCESS) {
+      dv.release(h);
+      cuCheck(r, "cuMemMap");
     }
-    arr[a] = p;
-    arrBytes[a] = nb;
-    dropGraph();
+    CUmemAccessDesc acc{};
+    acc.location = prop.location;
+    acc.flags = CU_MEM_ACCESS_FLAGS_PROT_READWRITE;
+    r = dv.setAccess(v.base + v.mapped, add, &acc, 1);
+    if (r != CUDA_SUCCESS) {
+      dv.unmap(v.base + v.mapped, add);
+      dv.release(h);
+      cuCheck(r, "cuMemSetAccess");
+    }
+    v.chunks.emplace_back(h, add);
+    v.mapped = need;
+  }
+  // Unmaps whole trailing chunks above array a's region top (the stream is
+  // idle: callers synchronize first).
+  void trim(int a) {
+    VmArray& v = va[a];
+    const size_t need = mappedFor(a, regions[kArray[a].region].top());
+    const DriverVmm& dv = vmm();
+    while (!v.chunks.empty() && v.mapped - v.chunks.back().second >= need) {
+      const auto c = v.chunks.back();
+      v.mapped -= c.second;
+      cuCheck(dv.unmap(v.base + v.mapped, c.second), "cuMemUnmap");
+      cuCheck(dv.release(c.first), "cuMemRelease");
+      v.chunks.pop_back();
+    }
+  }
+  size_t mappedBytes() const {
+    size_t b = 0;
+    for (const VmArray& v : va) b += v.mapped;
+    return b;
   }
   int maxN(const std::vector<int>& slots) const {
     int m = 1;
@@ -295,8 +389,24 @@ struct Forest::Dev {
   }
 };
 
-Forest::Forest(const std::vector<float>& coef) : d_(new Dev()) {
+Forest::Forest(const std::vector<float>& coef, size_t maxBytes) : d_(new Dev()) {
   Dev& d = *d_;
+  GB_CK(cudaGetDevice(&d.device));
+  const DriverVmm& dv = vmm();
+  CUmemAllocationProp prop{};
+  prop.type = CU_MEM_ALLOCATION_TYPE_PINNED;
+  prop.location.type = CU_MEM_LOCATION_TYPE_DEVICE;
+  prop.location.id = d.device;
+  cuCheck(dv.granularity(&d.gran, &prop, CU_MEM_ALLOC_GRANULARITY_MINIMUM),
+          "cuMemGetAllocationGranularity");
+  // Every pool may grow to the whole budget: reserve that much address
+  // space per array (address space only; memory is mapped on growth).
+  const size_t reserve = roundUp(std::max(maxBytes, d.gran), d.gran);
+  for (int a = 0; a < kArrays; ++a) {
+    cuCheck(dv.reserve(&d.va[a].base, reserve, 0, 0, 0), "cuMemAddressReserve");
+    d.va[a].reserved = reserve;
+    d.arr[a] = reinterpret_cast<void*>(d.va[a].base);
+  }
   GB_CK(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
   d.br.main = d.stream;
   GB_CK(cudaStreamCreateWithFlags(&d.br.side, cudaStreamNonBlocking));
@@ -316,7 +426,16 @@ Forest::~Forest() {
   if (d.stream) cudaStreamSynchronize(d.stream);
   if (d.exec) cudaGraphExecDestroy(d.exec);
   if (d.graph) cudaGraphDestroy(d.graph);
-  for (void* p : d.arr) cudaFree(p);
+  const DriverVmm& dv = vmm();
+  for (VmArray& v : d.va) {
+    size_t at = 0;
+    for (const auto& c : v.chunks) {
+      dv.unmap(v.base + at, c.second);
+      dv.release(c.first);
+      at += c.second;
+    }
+    if (v.base) dv.addressFree(v.base, v.reserved);
+  }
   cudaFree(d.coef);
   cudaFree(d.counter);
   cudaFree(d.tasks);
@@ -331,7 +450,7 @@ Forest::~Forest() {
   if (d.stream) cudaStreamDestroy(d.stream);
 }
 
-int Forest::admit(std::unique_ptr<CompiledSpot> s) {
+int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   Dev& d = *d_;
   if (!s || s->tree.empty) throw Error{PPS_GB_E_ARG, "forest: spot compiled to empty ranges"};
   const Tree& t = s->tree;
@@ -359,6 +478,16 @@ int Forest::admit(std::unique_ptr<CompiledSpot> s) {
     d.freeSlots.push_back(slot);
     throw Error{PPS_GB_E_BUDGET, "forest: resident spots exceed the 32-bit row / 24-bit node "
                                  "index space"};
+  }
+  // Device bytes once the pools cover the new ranges (plus the small
+  // fixed buffers): the spot waits while that exceeds the budget.
+  size_t after = deviceBytes() - d.mappedBytes();
+  for (int a = 0; a < kArrays; ++a)
+    after += std::max(d.va[a].mapped, d.mappedFor(a, d.regions[kArray[a].region].top()));
+  if (after > budget) {
+    for (int r = 0; r < kRegions; ++r) d.regions[r].release(rec.off[r], rec.size[r], kGranule[r]);
+    d.freeSlots.push_back(slot);
+    return -1;
   }
   for (int a = 0; a < kArrays; ++a) d.grow(a);
   if ((size_t)slot >= d.counterCap) {
@@ -473,6 +602,9 @@ std::unique_ptr<CompiledSpot> Forest::retire(int slot) {
   d.live.erase(it);
   d.freeSlots.push_back(slot);
   d.dirty = true;
+  // Give back memory above the pools' new tops (nothing may still run).
+  GB_CK(cudaStreamSynchronize(d.stream));
+  for (int a = 0; a < kArrays; ++a) d.trim(a);
   return s;
 }
 
@@ -678,8 +810,7 @@ size_t Forest::deviceBytes() const {
   size_t b = (size_t)d.coefEntries * 3 * sizeof(float) + d.counterCap * sizeof(int) +
              d.tasksCap * sizeof(int) + d.wTasksCap * sizeof(int) +
              d.infoCap * sizeof(RootInfo) + d.valsCap * sizeof(double);
-  for (size_t x : d.arrBytes) b += x;
-  return b;
+  return b + d.mappedBytes();
 }
 
 size_t Forest::usedBytes() const { return d_->used; }

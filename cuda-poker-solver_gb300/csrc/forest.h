@@ -7,8 +7,9 @@
 // counter (its slot, stored in node meta bits 16-31) and its own rows;
 // nothing is shared between spots, so a spot's rows do not depend on which
 // other spots are resident. Pool ranges are handed out first-fit and freed
-// when a spot retires; a pool grows (and moves, keeping its contents) when
-// a range does not fit.
+// when a spot retires. Each pool is a fixed virtual address range: memory
+// is mapped at its end when a range does not fit and unmapped when the top
+// falls, so pools never move and growing never copies.
 #pragma once
 
 #include <cstddef>
@@ -38,14 +39,17 @@ double pairMassOf(const Tree& t);
 class Forest {
  public:
   // coef: the DCFR schedule, 3 floats (pos, neg, avg) per iteration index;
-  // a spot runs at most coef.size() / 3 iterations.
-  explicit Forest(const std::vector<float>& coef);
+  // a spot runs at most coef.size() / 3 iterations. maxBytes bounds every
+  // pool (each reserves that much address space up front).
+  Forest(const std::vector<float>& coef, size_t maxBytes);
   ~Forest();
   Forest(const Forest&) = delete;
   Forest& operator=(const Forest&) = delete;
 
-  // Places a compiled spot (rows zeroed, counter 0); returns its slot.
-  int admit(std::unique_ptr<CompiledSpot> s);
+  // Places a compiled spot (rows zeroed, counter 0) and returns its slot,
+  // taking ownership; returns -1 (spot untouched) when the forest's device
+  // bytes would exceed `budget`.
+  int admit(std::unique_ptr<CompiledSpot>& s, size_t budget);
   // Frees the spot's ranges and returns it.
   std::unique_ptr<CompiledSpot> retire(int slot);
   std::vector<int> slots() const;  // resident slots, ascending

@@ -272,8 +272,8 @@ int pps_gb_solve_noalloc(const pps_gb_spot* spot, const pps_gb_bet_config* cfg,
  * API server serialises solves behind one lock (python/pps_api.py). Here
  * many spots are resident on the GPU at once and share every launch:
  * submit() queues a spot (compiled on host threads), a driver admits
- * compiled spots in submission order while the sum of their device
- * footprints fits the HBM budget, runs check_every DCFR iterations of all
+ * compiled spots in submission order while the device memory the batch
+ * maps stays within the HBM budget, runs check_every DCFR iterations of all
  * resident spots per epoch (one CUDA graph), checks each spot's
  * exploitability with FP64 best-response walks and retires it once it is
  * at or below its target (or at max_iterations), with FP64 EV walks.

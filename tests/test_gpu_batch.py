@@ -135,19 +135,26 @@ def test_river_ev_within_a_hundredth_of_the_oracle(mixed):
         assert abs(st["ev_ip"] - r["ev_ip"]) < 0.01
 
 
-def test_budget_admits_one_at_a_time_without_changing_results(mixed):
+def test_budget_admits_one_at_a_time_without_changing_results():
+    """Two ~230 MB turn spots under a budget that holds one of them (plus
+    the pools' mapping granularity) never share the device; small river
+    spots still join; every result equals the unconstrained batch's."""
     from pps import batch as pb
-    spots, (res, _, _) = mixed
-    sub = spots[:4]
-    need = max(pb.footprint(sp.board_text(), weights(sp.oop), weights(sp.ip), sp.pot, sp.stack,
-                            sp.cfg.bet_text(), sp.cfg.raise_text() or [], sp.cfg.max_raises)
-               for sp in sub)
-    got, _, info = _solve_batch(sub, hbm_budget=need)
-    assert info["peak_active"] < len(sub)  # the two turns never shared the device
-    assert info["peak_used_bytes"] <= need
-    for r, want in zip(got, res[:4]):
+    sub = [wl.turn_c2(seed=202, uniform_config=True), wl.turn_c2(seed=203, uniform_config=True),
+           wl.river_c1(), wl.river_geo()]
+    big = max(pb.footprint(sp.board_text(), weights(sp.oop), weights(sp.ip), sp.pot, sp.stack,
+                           sp.cfg.bet_text(), sp.cfg.raise_text() or [], sp.cfg.max_raises)
+              for sp in sub)
+    budget = int(1.3 * big) + (64 << 20)
+    free, _, _ = _solve_batch(sub)
+    got, _, info = _solve_batch(sub, hbm_budget=budget)
+    assert info["peak_active"] <= 3
+    assert info["peak_used_bytes"] <= budget
+    assert info["failed"] == 0
+    for r, want in zip(got, free):
         assert r["iterations"] == want["iterations"]
-        assert abs(r["ev_oop"] - want["ev_oop"]) <= CHIP_TOL
+        for k in ("ev_oop", "ev_ip", "exploitability"):
+            assert abs(r[k] - want[k]) <= CHIP_TOL
 
 
 def test_spot_over_budget_is_refused():
