@@ -17,8 +17,8 @@
 #include <string>
 
 #include "kernels.cuh"
-#include "leaf_kernel.cuh"
 #include "plan.cuh"
+#include "terminal.cuh"
 #include "pps_gb.h"
 
 namespace pps {
@@ -61,7 +61,8 @@ struct Engine::Dev {
   int* tasks = nullptr;
   std::vector<int> hostTasks;  // host copy of the concatenated task lists
   std::vector<ListRef> fwd[2], bwd[2];
-  LeafPlan leaf;       // fused leaf-street plan (ok = false if not applicable)
+  std::vector<ListRef> sdG, fdG, inner[2];  // the group plan's backward lists
+  int4* groups = nullptr;
   std::vector<Launch> plan[2];  // per engine kind: one iteration
   bool walkReady = false;
   int maxN = 0;
@@ -88,13 +89,13 @@ V* upload(Engine::Dev& d, const std::vector<V>& v, size_t& bytes, int64_t& h2d) 
 }
 
 PlanArgs planArgs(const Engine::Dev& d) {
-  return PlanArgs{d.tree, d.rowsF, d.tasks, d.counter, 1, d.maxN, d.smemF};
+  return PlanArgs{d.tree, d.rowsF, d.tasks, d.counter, 1, d.maxN, d.smemF, d.groups,
+                  sdGroupSmem(d.maxN), fdGroupSmem(d.maxN)};
 }
 
 // Issues one planned launch (CFR mode, f32 rows) on stream s.
 void issue(Engine::Dev& d, const Launch& l, cudaStream_t s) {
-  if (l.kind == kLeafSweep) launchLeaf(d.leaf, d.tree, d.rowsF, l.tr, s);
-  else issueLaunch(planArgs(d), l, s);
+  issueLaunch(planArgs(d), l, s);
 }
 
 }  // namespace
@@ -104,10 +105,7 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
   Dev& d = *d_;
   size_t& B = deviceBytes_;
   GB_CK(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
-  d.br.main = d.stream;
-  GB_CK(cudaStreamCreateWithFlags(&d.br.side, cudaStreamNonBlocking));
-  GB_CK(cudaEventCreateWithFlags(&d.br.fork, cudaEventDisableTiming));
-  GB_CK(cudaEventCreateWithFlags(&d.br.join, cudaEventDisableTiming));
+  d.br.create(d.stream);
   d.tree.nodes = upload(d, L_.nodes, B, h2d_);
   d.tree.rows = upload(d, L_.rows, B, h2d_);
   d.tree.termVal = upload(d, L_.termVal, B, h2d_);
@@ -150,11 +148,15 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
     for (int dd = 0; dd < D; ++dd) {
       d.fwd[tr].push_back(addList(L_.fwdTasks[tr][dd]));
       d.bwd[tr].push_back(addList(L_.bwdTasks[tr][dd]));
+      d.inner[tr].push_back(addList(L_.innerTasks[tr][dd]));
     }
-  d.leaf = planLeaf(t_, L_, all);
+  for (int dd = 0; dd < D; ++dd) {
+    d.sdG.push_back(addList(L_.sdGroupTasks[dd]));
+    d.fdG.push_back(addList(L_.fdGroupTasks[dd]));
+  }
   d.tasks = upload(d, all, B, h2d_);
   d.hostTasks = all;
-  if (d.leaf.ok) finishLeaf(d.leaf, d.tasks, [&](size_t n) { return d.own(alloc<float>(n, B)); });
+  d.groups = reinterpret_cast<int4*>(upload(d, L_.groups, B, h2d_));
 
   d.maxN = L_.maxN;
   d.smemF = bwdScratchBytes<float>(d.maxN);
@@ -162,9 +164,10 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
   raiseSmemLimit((const void*)bwdLevelK<float>, d.smemF);
   raiseSmemLimit((const void*)bwdLevelK<double>, d.smemD);
   raiseSmemLimit((const void*)bwdTerminalK<float>, d.smemF);
-  if (d.leaf.ok) GB_CK(prepareLeaf(d.leaf));
+  raiseSmemLimit((const void*)sdGroupK, sdGroupSmem(d.maxN));
+  raiseSmemLimit((const void*)fdGroupK, fdGroupSmem(d.maxN));
   buildPlans();
-  engineKind_ = d.leaf.ok ? 1 : 0;
+  engineKind_ = 0;
   zeroRows();
 }
 
@@ -175,9 +178,7 @@ Engine::~Engine() {
   if (d_->stream) cudaStreamSynchronize(d_->stream);
   for (void* p : d_->owned) cudaFree(p);
   if (d_->stream) cudaStreamDestroy(d_->stream);
-  if (d_->br.side) cudaStreamDestroy(d_->br.side);
-  if (d_->br.fork) cudaEventDestroy(d_->br.fork);
-  if (d_->br.join) cudaEventDestroy(d_->br.join);
+  d_->br.destroy();
 }
 
 void* Engine::stream() const { return (void*)d_->stream; }
@@ -216,47 +217,59 @@ double Engine::taskBytes(int task, int tr, bool fwd) const {
   }
 }
 
+// Plans of one iteration. Kind 0 (default): per backward level, the
+// showdown groups, the fold groups and the interior tasks run as three
+// concurrent launches (terminals read only the traverser's reach rows and
+// write their own value rows; interior tasks read value rows of deeper
+// levels). Kind 1: the same levels with one CTA per terminal node
+// (bwdTerminalK beside bwdInteriorK).
 void Engine::buildPlans() {
   Dev& d = *d_;
-  const int D = (int)L_.bwdTasks[0].size();
   auto listBytes = [&](const std::vector<int>& v, int tr, bool fwd) {
     double b = 0;
     for (int task : v) b += taskBytes(task, tr, fwd);
     return b;
   };
+  auto groupBytes = [&](const std::vector<int>& v, int tr) {
+    double b = 0;
+    for (int task : v) {
+      const TermGroup& g = L_.groups[(unsigned)task >> 8];
+      for (int k = 0; k < 4; ++k)
+        if (g.node[k] >= 0) b += taskBytes(makeTask(task & 3, 0, g.node[k]), tr, false);
+    }
+    return b;
+  };
   for (int kind = 0; kind < 2; ++kind) {
     std::vector<Launch>& P = d.plan[kind];
     P.clear();
-    const bool leaf = kind == 1 && d.leaf.ok;
     for (int tr = 0; tr < 2; ++tr) {
-      const std::vector<std::vector<int>>& fw = leaf ? d.leaf.fwdTasks[tr] : L_.fwdTasks[tr];
-      const std::vector<std::vector<int>>& bw = leaf ? d.leaf.bwdTasks[tr] : L_.bwdTasks[tr];
-      const std::vector<ListRef>& fr = leaf ? d.leaf.fwd[tr] : d.fwd[tr];
-      const std::vector<ListRef>& brf = leaf ? d.leaf.bwd[tr] : d.bwd[tr];
-      for (int dd = 0; dd < (int)fr.size(); ++dd)
-        if (fr[dd].count) P.push_back({kFwd, tr, fr[dd], listBytes(fw[dd], tr, true)});
-      if (leaf) P.push_back({kLeafSweep, tr, ListRef{}, d.leaf.algoBytes[tr]});
-      for (int dd = (int)brf.size() - 1; dd >= 0; --dd) {
-        if (!brf[dd].count) continue;
-        if (leaf) {
-          P.push_back({kBwd, tr, brf[dd], listBytes(bw[dd], tr, false)});
-          continue;
+      const int D = (int)d.fwd[tr].size();
+      for (int dd = 0; dd < D; ++dd)
+        if (d.fwd[tr][dd].count)
+          P.push_back({kFwd, tr, d.fwd[tr][dd], listBytes(L_.fwdTasks[tr][dd], tr, true)});
+      for (int dd = D - 1; dd >= 0; --dd) {
+        std::vector<Launch> set;
+        if (kind == 0) {
+          if (d.sdG[dd].count)
+            set.push_back({kSdGroup, tr, d.sdG[dd], groupBytes(L_.sdGroupTasks[dd], tr)});
+          if (d.fdG[dd].count)
+            set.push_back({kFdGroup, tr, d.fdG[dd], groupBytes(L_.fdGroupTasks[dd], tr)});
+        } else {
+          const std::vector<int>& v = L_.bwdTasks[tr][dd];
+          const int nt = terminalCount(v);
+          if (nt)
+            set.push_back({kBwdTerm, tr, ListRef{d.bwd[tr][dd].off, nt},
+                           listBytes(std::vector<int>(v.begin(), v.begin() + nt), tr, false)});
         }
-        // The list is sorted showdown, fold, chance, decide: terminal tasks
-        // (kinds 2-3) lead. Terminals read only the traverser's reach row and
-        // write their own cfv rows; interior tasks read child cfv rows of
-        // deeper levels, so both halves of a level run at once.
-        const std::vector<int>& v = bw[dd];
-        const int nt = terminalCount(v);
-        const std::vector<int> vt(v.begin(), v.begin() + nt), vi(v.begin() + nt, v.end());
-        const ListRef lt{brf[dd].off, nt}, li{brf[dd].off + nt, brf[dd].count - nt};
-        if (nt) P.push_back({kBwdTerm, tr, lt, listBytes(vt, tr, false), li.count > 0});
-        if (li.count) P.push_back({kBwdInt, tr, li, listBytes(vi, tr, false)});
+        if (d.inner[tr][dd].count)
+          set.push_back({kBwdInt, tr, d.inner[tr][dd],
+                         listBytes(L_.innerTasks[tr][dd], tr, false)});
+        for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
+        P.insert(P.end(), set.begin(), set.end());
       }
     }
     P.push_back({kCounter, 0, ListRef{}, 0.0});
   }
-  (void)D;
 }
 
 void Engine::zeroRows() {
@@ -328,7 +341,7 @@ void Engine::capture() {
 }
 
 void Engine::setEngineKind(int kind) {
-  const int k = kind == 1 && d_->leaf.ok ? 1 : 0;
+  const int k = kind == 1 ? 1 : 0;
   if (k == engineKind_ && d_->exec) return;
   engineKind_ = k;
   capture();

@@ -56,8 +56,9 @@ class Engine {
   int64_t h2dBytes() const { return h2d_; }
   int64_t d2hBytes() const { return d2h_; }
 
-  // Selects the iteration graph: 0 = depth-level kernels; 1 = fused
-  // leaf-street kernel where available. Recaptures on change.
+  // Selects the iteration graph's terminal kernels: 0 = groups of four
+  // nodes of one level and board state (default); 1 = one CTA per node.
+  // Recaptures on change.
   void setEngineKind(int kind);
   int engineKind() const { return engineKind_; }
   int launchesPerIteration() const { return launchesPerIter_; }
@@ -71,7 +72,7 @@ class Engine {
   const Tree& t_;
   HostLayout L_;
   std::unique_ptr<Dev> d_;
-  int engineKind_ = 1;
+  int engineKind_ = 0;
   int launchesPerIter_ = 0;
   size_t deviceBytes_ = 0;
   mutable int64_t h2d_ = 0, d2h_ = 0;

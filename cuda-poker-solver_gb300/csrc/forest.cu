@@ -41,13 +41,13 @@ namespace {
 // Pools. A region is one index space (node ids, row quads, ...); arrays
 // are the device buffers indexed by it.
 enum Region { rNode, rChild, rState, rU8, rU16, rI16, rSd, rReg, rCfv, rReach0, rReach1, rW,
-              kRegions };
+              rGroup, kRegions };
 // Allocation granule per region, in entries: every range starts on a
 // 16-byte boundary (u16 tables are staged with 16-byte loads).
-constexpr size_t kGranule[kRegions] = {1, 4, 1, 16, 8, 8, 1, 1, 1, 1, 1, 2};
+constexpr size_t kGranule[kRegions] = {1, 4, 1, 16, 8, 8, 1, 1, 1, 1, 1, 2, 1};
 
 enum Array { aNodes, aRows, aTerm, aChild, aState, aU8, aU16, aI16, aSd, aReg, aStr, aCfvF,
-             aCfvD, aReachF0, aReachD0, aReachF1, aReachD1, aW, kArrays };
+             aCfvD, aReachF0, aReachD0, aReachF1, aReachD1, aW, aGroups, kArrays };
 struct ArrayDef {
   Region region;
   size_t entryBytes;
@@ -58,7 +58,8 @@ const ArrayDef kArray[kArrays] = {
     {rU16, 2},                {rI16, 2},                  {rSd, sizeof(ShowdownInfo)},
     {rReg, 16},               {rReg, 16},                 {rCfv, 16},
     {rCfv, 32},               {rReach0, 16},              {rReach0, 32},
-    {rReach1, 16},            {rReach1, 32},              {rW, 8}};
+    {rReach1, 16},            {rReach1, 32},              {rW, 8},
+    {rGroup, sizeof(TermGroup)}};
 
 size_t roundUp(size_t n, size_t g) { return (n + g - 1) / g * g; }
 
@@ -75,6 +76,7 @@ void regionSizes(const Tree& t, const HostLayout& L, size_t out[kRegions]) {
   out[rReach0] = L.reachQuads[0];
   out[rReach1] = L.reachQuads[1];
   out[rW] = (size_t)t.side[0].n + (size_t)t.side[1].n;  // w0 then w1
+  out[rGroup] = L.groups.size();
 }
 
 size_t footprintOf(const Tree& t, const HostLayout& L) {
@@ -254,8 +256,10 @@ struct SlotRec {
   uint32_t rootCfvQ = 0, rootRegQ = 0;
   int depth = 0;
   // Task lists per traverser and depth, node ids relocated; backward lists
-  // keep the layout's order (terminal tasks first).
-  std::vector<std::vector<int>> fwd[2], bwd[2];
+  // keep the layout's order (terminal tasks first). The iteration uses the
+  // terminal group lists (group ids relocated) and the interior lists.
+  std::vector<std::vector<int>> fwd[2], bwd[2], inner[2];
+  std::vector<std::vector<int>> sdG, fdG;
 };
 
 struct Forest::Dev {
@@ -408,10 +412,7 @@ Forest::Forest(const std::vector<float>& coef, size_t maxBytes) : d_(new Dev()) 
     d.arr[a] = reinterpret_cast<void*>(d.va[a].base);
   }
   GB_CK(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
-  d.br.main = d.stream;
-  GB_CK(cudaStreamCreateWithFlags(&d.br.side, cudaStreamNonBlocking));
-  GB_CK(cudaEventCreateWithFlags(&d.br.fork, cudaEventDisableTiming));
-  GB_CK(cudaEventCreateWithFlags(&d.br.join, cudaEventDisableTiming));
+  d.br.create(d.stream);
   GB_CK(cudaEventCreate(&d.evA));
   GB_CK(cudaEventCreate(&d.evB));
   d.coefEntries = (int)(coef.size() / 3);
@@ -442,9 +443,7 @@ Forest::~Forest() {
   cudaFree(d.wTasks);
   cudaFree(d.info);
   cudaFree(d.vals);
-  if (d.br.side) cudaStreamDestroy(d.br.side);
-  if (d.br.fork) cudaEventDestroy(d.br.fork);
-  if (d.br.join) cudaEventDestroy(d.br.join);
+  d.br.destroy();
   if (d.evA) cudaEventDestroy(d.evA);
   if (d.evB) cudaEventDestroy(d.evB);
   if (d.stream) cudaStreamDestroy(d.stream);
@@ -471,7 +470,7 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   bool fits = rec.off[rNode] + N < ((size_t)1 << 24);
   for (int r : {rReg, rCfv, rReach0, rReach1})
     fits = fits && rec.off[r] + rec.size[r] <= 0xffffffffull;
-  for (int r : {rChild, rState, rU8, rU16, rI16, rSd, rW})
+  for (int r : {rChild, rState, rU8, rU16, rI16, rSd, rW, rGroup})
     fits = fits && rec.off[r] + rec.size[r] < ((size_t)1 << 31);
   if (!fits) {
     for (int r = 0; r < kRegions; ++r) d.regions[r].release(rec.off[r], rec.size[r], kGranule[r]);
@@ -546,6 +545,10 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   put(aU16, off[rU16], L.poolU16.data(), L.poolU16.size() * 2);
   put(aI16, off[rI16], L.poolI16.data(), L.poolI16.size() * 2);
   put(aSd, off[rSd], L.poolSd.data(), L.poolSd.size() * sizeof(ShowdownInfo));
+  for (TermGroup& g : L.groups)
+    for (int& u : g.node)
+      if (u >= 0) u += (int)off[rNode];
+  put(aGroups, off[rGroup], L.groups.data(), L.groups.size() * sizeof(TermGroup));
   for (int a : {aReg, aStr, aCfvF, aCfvD, aReachF0, aReachD0, aReachF1, aReachD1}) {
     const Region r = kArray[a].region;
     const size_t bytes = rec.size[r] * kArray[a].entryBytes;
@@ -571,10 +574,17 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   for (int tr = 0; tr < 2; ++tr) {
     rec.fwd[tr] = std::move(L.fwdTasks[tr]);
     rec.bwd[tr] = std::move(L.bwdTasks[tr]);
-    for (auto* lists : {&rec.fwd[tr], &rec.bwd[tr]})
+    rec.inner[tr] = std::move(L.innerTasks[tr]);
+    for (auto* lists : {&rec.fwd[tr], &rec.bwd[tr], &rec.inner[tr]})
       for (auto& v : *lists)
         for (int& task : v) task = (int)((unsigned)task + nodeShift);
   }
+  const unsigned groupShift = (unsigned)off[rGroup] << 8;
+  rec.sdG = std::move(L.sdGroupTasks);
+  rec.fdG = std::move(L.fdGroupTasks);
+  for (auto* lists : {&rec.sdG, &rec.fdG})
+    for (auto& v : *lists)
+      for (int& task : v) task = (int)((unsigned)task + groupShift);
   // The host tables are on the device now; keep only what queries need.
   GB_CK(cudaStreamSynchronize(d.stream));
   L.termVal = {};
@@ -584,6 +594,7 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   L.poolI16 = {};
   L.poolSd = {};
   L.states = {};
+  L.groups = {};
   d.used += s->bytes;
   rec.spot = std::move(s);
   d.live[slot] = std::move(rec);
@@ -625,46 +636,37 @@ namespace {
 // when `split`). Returns the refs into `all`.
 struct Lists {
   std::vector<int> all;
-  std::vector<ListRef> fwd[2], term[2], inner[2], bwd[2];
+  std::vector<ListRef> fwd[2], bwd[2], inner[2], sdG, fdG;
 };
 
-Lists gather(const std::map<int, SlotRec>& live, const std::vector<int>& slots) {
+Lists gather(const std::map<int, SlotRec>& live, const std::vector<int>& slots, bool iteration) {
   Lists out;
   int D = 0;
   for (int s : slots) D = std::max(D, live.at(s).depth);
-  for (int tr = 0; tr < 2; ++tr) {
-    out.fwd[tr].resize(D);
-    out.term[tr].resize(D);
-    out.inner[tr].resize(D);
-    out.bwd[tr].resize(D);
-    for (int dd = 0; dd < D; ++dd) {
-      const int f0 = (int)out.all.size();
-      for (int s : slots) {
-        const SlotRec& r = live.at(s);
-        if (dd < r.depth)
-          out.all.insert(out.all.end(), r.fwd[tr][dd].begin(), r.fwd[tr][dd].end());
-      }
-      out.fwd[tr][dd] = ListRef{f0, (int)out.all.size() - f0};
-      const int b0 = (int)out.all.size();
-      for (int s : slots) {
-        const SlotRec& r = live.at(s);
-        if (dd >= r.depth) continue;
-        const auto& v = r.bwd[tr][dd];
-        out.all.insert(out.all.end(), v.begin(), v.begin() + terminalCount(v));
-      }
-      const int i0 = (int)out.all.size();
-      for (int s : slots) {
-        const SlotRec& r = live.at(s);
-        if (dd >= r.depth) continue;
-        const auto& v = r.bwd[tr][dd];
-        out.all.insert(out.all.end(), v.begin() + terminalCount(v), v.end());
-      }
-      const int e = (int)out.all.size();
-      out.term[tr][dd] = ListRef{b0, i0 - b0};
-      out.inner[tr][dd] = ListRef{i0, e - i0};
-      out.bwd[tr][dd] = ListRef{b0, e - b0};
+  auto cat = [&](auto pick) {
+    const int b = (int)out.all.size();
+    for (int s : slots) {
+      const std::vector<int>* v = pick(live.at(s));
+      if (v) out.all.insert(out.all.end(), v->begin(), v->end());
     }
-  }
+    return ListRef{b, (int)out.all.size() - b};
+  };
+  auto at = [](const std::vector<std::vector<int>>& lists, int dd) {
+    return dd < (int)lists.size() ? &lists[dd] : nullptr;
+  };
+  for (int tr = 0; tr < 2; ++tr)
+    for (int dd = 0; dd < D; ++dd) {
+      out.fwd[tr].push_back(cat([&](const SlotRec& r) { return at(r.fwd[tr], dd); }));
+      if (iteration)
+        out.inner[tr].push_back(cat([&](const SlotRec& r) { return at(r.inner[tr], dd); }));
+      else
+        out.bwd[tr].push_back(cat([&](const SlotRec& r) { return at(r.bwd[tr], dd); }));
+    }
+  if (iteration)
+    for (int dd = 0; dd < D; ++dd) {
+      out.sdG.push_back(cat([&](const SlotRec& r) { return at(r.sdG, dd); }));
+      out.fdG.push_back(cat([&](const SlotRec& r) { return at(r.fdG, dd); }));
+    }
   return out;
 }
 
@@ -679,7 +681,7 @@ void Forest::iterate(int n) {
   if (d.dirty || !d.exec) {
     d.dropGraph();
     const std::vector<int> all = slots();
-    Lists ls = gather(d.live, all);
+    Lists ls = gather(d.live, all, true);
     ensureBuf(d.tasks, d.tasksCap, std::max<size_t>(ls.all.size(), 1));
     if (!ls.all.empty())
       GB_CK(cudaMemcpyAsync(d.tasks, ls.all.data(), ls.all.size() * sizeof(int),
@@ -690,17 +692,22 @@ void Forest::iterate(int n) {
       for (int dd = 0; dd < D; ++dd)
         if (ls.fwd[tr][dd].count) d.plan.push_back({kFwd, tr, ls.fwd[tr][dd], 0.0});
       for (int dd = D - 1; dd >= 0; --dd) {
-        const ListRef lt = ls.term[tr][dd], li = ls.inner[tr][dd];
-        if (lt.count) d.plan.push_back({kBwdTerm, tr, lt, 0.0, li.count > 0});
-        if (li.count) d.plan.push_back({kBwdInt, tr, li, 0.0});
+        std::vector<Launch> set;
+        if (ls.sdG[dd].count) set.push_back({kSdGroup, tr, ls.sdG[dd], 0.0});
+        if (ls.fdG[dd].count) set.push_back({kFdGroup, tr, ls.fdG[dd], 0.0});
+        if (ls.inner[tr][dd].count) set.push_back({kBwdInt, tr, ls.inner[tr][dd], 0.0});
+        for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
+        d.plan.insert(d.plan.end(), set.begin(), set.end());
       }
     }
     d.plan.push_back({kCounter, 0, ListRef{}, 0.0});
     const int maxN = d.maxN(all);
-    const size_t smem = bwdScratchBytes<float>(maxN);
-    raiseSmemLimit((const void*)bwdTerminalK<float>, smem);
+    const size_t smemSd = sdGroupSmem(maxN), smemFd = fdGroupSmem(maxN);
+    raiseSmemLimit((const void*)sdGroupK, smemSd);
+    raiseSmemLimit((const void*)fdGroupK, smemFd);
     const PlanArgs args{d.tree(), d.rows<float>(aReachF0, aReachF1, aCfvF), d.tasks, d.counter,
-                        (int)d.counterCap, maxN, smem};
+                        (int)d.counterCap, maxN, bwdScratchBytes<float>(maxN),
+                        static_cast<const int4*>(d.arr[aGroups]), smemSd, smemFd};
     GB_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
     issuePlan(d.plan, d.br, [&](const Launch& l, cudaStream_t s) { issueLaunch(args, l, s); });
     const cudaError_t launchErr = cudaGetLastError();
@@ -736,7 +743,7 @@ std::vector<double> Forest::walkValues(const std::vector<int>& slots, int tr, in
   Dev& d = *d_;
   std::vector<double> out(slots.size(), 0.0);
   if (slots.empty()) return out;
-  Lists ls = gather(d.live, slots);
+  Lists ls = gather(d.live, slots, false);
   ensureBuf(d.wTasks, d.wTasksCap, std::max<size_t>(ls.all.size(), 1));
   if (!ls.all.empty())
     GB_CK(cudaMemcpyAsync(d.wTasks, ls.all.data(), ls.all.size() * sizeof(int),

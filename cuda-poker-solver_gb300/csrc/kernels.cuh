@@ -400,9 +400,8 @@ __device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, in
     }
     const ShowdownInfo f = fs[j];
     const int le = f.x & 0xffff, te = f.x >> 16;
-    const int c1 = f.y & 0xff, c2 = (f.y >> 8) & 0xff;
-    const int a1 = seg[c1] + c1, a2 = seg[c2] + c2;
-    const int len1 = seg[c1 + 1] - seg[c1], len2 = seg[c2 + 1] - seg[c2];
+    const int len1 = f.y & 0xff, len2 = (f.y >> 8) & 0xff;
+    const int a1 = f.w & 0xffff, a2 = f.w >> 16;
     const T x1le = ws.X[a1 + ((f.y >> 16) & 0xff)], x1te = ws.X[a1 + (f.y >> 24)];
     const T x2le = ws.X[a2 + (f.z & 0xff)], x2te = ws.X[a2 + ((f.z >> 8) & 0xff)];
     const int same = (int)(f.z >> 16) - 1;

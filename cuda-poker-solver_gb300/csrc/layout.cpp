@@ -140,13 +140,14 @@ HostLayout buildLayout(const Tree& t) {
         };
         const int so = t.side[tr].sameOther[b];
         const int same = so >= 0 ? slotOf(ol, so) : -1;
+        const int len1 = (int)posOfCard[c1].size(), len2 = (int)posOfCard[c2].size();
         ShowdownInfo info;
         info.x = (uint32_t)le | ((uint32_t)te << 16);
-        info.y = (uint32_t)c1 | ((uint32_t)c2 << 8) | ((uint32_t)below(c1, le) << 16) |
+        info.y = (uint32_t)len1 | ((uint32_t)len2 << 8) | ((uint32_t)below(c1, le) << 16) |
                  ((uint32_t)below(c1, te) << 24);
         info.z = (uint32_t)below(c2, le) | ((uint32_t)below(c2, te) << 8) |
                  ((uint32_t)(same + 1) << 16);
-        info.w = 0;
+        info.w = (uint32_t)(segStart[c1] + c1) | ((uint32_t)(segStart[c2] + c2) << 16);
         L.poolSd.push_back(info);
       }
     }
@@ -251,7 +252,30 @@ HostLayout buildLayout(const Tree& t) {
     for (int d = 0; d < D; ++d) {
       auto& b = L.bwdTasks[tr][d];
       for (auto* v : {&sd[d], &fd[d], &ch[d], &dc[d]}) b.insert(b.end(), v->begin(), v->end());
+      L.innerTasks[tr].push_back(ch[d]);
+      L.innerTasks[tr].back().insert(L.innerTasks[tr].back().end(), dc[d].begin(), dc[d].end());
     }
+  }
+  // Terminal groups: per depth, the showdown (then fold) nodes of one board
+  // state in fours, in node order (the same groups serve both traversers).
+  L.sdGroupTasks.assign(D, {});
+  L.fdGroupTasks.assign(D, {});
+  for (int kind : {(int)kShowdown, (int)kFold}) {
+    std::vector<std::vector<std::vector<int>>> byState(D, std::vector<std::vector<int>>(S));
+    for (int u = 0; u < N; ++u)
+      if (t.nodes[u].kind == kind) byState[t.nodes[u].depth][t.nodes[u].state].push_back(u);
+    for (int d = 0; d < D; ++d)
+      for (int s = 0; s < S; ++s) {
+        const auto& v = byState[d][s];
+        for (size_t i = 0; i < v.size(); i += 4) {
+          TermGroup g{{-1, -1, -1, -1}};
+          for (size_t k = 0; k < 4 && i + k < v.size(); ++k) g.node[k] = v[i + k];
+          const int task = makeTask(kind == kShowdown ? kTaskShowdown : kTaskFold, 0,
+                                    (int)L.groups.size());
+          (kind == kShowdown ? L.sdGroupTasks : L.fdGroupTasks)[d].push_back(task);
+          L.groups.push_back(g);
+        }
+      }
   }
   if (N >= (1 << 24)) throw Error{PPS_GB_E_MEMORY, "tree too large for 24-bit task node ids"};
   alignU16(L.poolU16);

@@ -73,13 +73,21 @@ struct alignas(16) StateDev {
                     // per traverser slot (see showdownInfo)
 };
 
-// Showdown entry of one traverser combo: x = le | te << 16 (opponents
-// strictly weaker / weaker-or-equal, in sorted positions); y = c1 | c2 <<
-// 8 | k1le << 16 | k1te << 24 and z = k2le | k2te << 8 | (same+1) << 16,
-// where kXle / kXte count card cX's segment entries below le / te and
-// `same` is the opponent slot of the identical combo (-1: none).
+// Showdown entry of one traverser combo (cards c1, c2): x = le | te << 16
+// (opponents strictly weaker / weaker-or-equal, in sorted positions);
+// y = len1 | len2 << 8 | k1le << 16 | k1te << 24; z = k2le | k2te << 8 |
+// (same+1) << 16; w = a1 | a2 << 16. lenX is the length of card cX's
+// segment, kXle / kXte count its entries below le / te, aX = seg[cX] + cX
+// is where its prefix run starts in the kernels' segment scan, and `same`
+// is the opponent slot of the identical combo (-1: none).
 struct alignas(16) ShowdownInfo {
   uint32_t x, y, z, w;
+};
+
+// Four terminal nodes (showdown or fold) of one depth and one board state,
+// evaluated together (-1: no node).
+struct alignas(16) TermGroup {
+  int node[4];
 };
 
 struct HostLayout {
@@ -101,6 +109,12 @@ struct HostLayout {
   // per chance branch; backward = showdowns, folds, chance chunks, decide
   // chunks (longest tasks first).
   std::vector<std::vector<int>> fwdTasks[2], bwdTasks[2];
+  // The f32 iteration's backward lists: terminal group tasks per depth
+  // (node field = index into `groups`; the same for both traversers) and
+  // the chance + decide tasks per traverser and depth.
+  std::vector<TermGroup> groups;
+  std::vector<std::vector<int>> sdGroupTasks, fdGroupTasks;
+  std::vector<std::vector<int>> innerTasks[2];
   int maxN = 0;        // largest list size (either side)
   int maxCardSeg = 0;  // longest card segment of any list
 };

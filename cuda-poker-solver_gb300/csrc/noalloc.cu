@@ -120,17 +120,25 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
                                   " floats; the spot needs " + std::to_string(t.rowTotal)};
   const HostLayout L = buildLayout(t);
 
-  // Task lists (as the engine concatenates them) and the row map.
+  // Task lists of the default iteration (the engine's kind 0: forward
+  // levels, then per backward level the showdown groups, the fold groups and
+  // the interior tasks) and the row map.
   std::vector<int> tasks;
   const int D = (int)L.bwdTasks[0].size();
-  std::vector<std::pair<int, int>> fwd[2], bwd[2];
-  for (int tr = 0; tr < 2; ++tr)
-    for (int d = 0; d < D; ++d) {
-      fwd[tr].push_back({(int)tasks.size(), (int)L.fwdTasks[tr][d].size()});
-      tasks.insert(tasks.end(), L.fwdTasks[tr][d].begin(), L.fwdTasks[tr][d].end());
-      bwd[tr].push_back({(int)tasks.size(), (int)L.bwdTasks[tr][d].size()});
-      tasks.insert(tasks.end(), L.bwdTasks[tr][d].begin(), L.bwdTasks[tr][d].end());
+  std::vector<std::pair<int, int>> fwd[2], sdG, fdG, inner[2];
+  auto add = [&](const std::vector<int>& v) {
+    const std::pair<int, int> r{(int)tasks.size(), (int)v.size()};
+    tasks.insert(tasks.end(), v.begin(), v.end());
+    return r;
+  };
+  for (int d = 0; d < D; ++d) {
+    sdG.push_back(add(L.sdGroupTasks[d]));
+    fdG.push_back(add(L.fdGroupTasks[d]));
+    for (int tr = 0; tr < 2; ++tr) {
+      fwd[tr].push_back(add(L.fwdTasks[tr][d]));
+      inner[tr].push_back(add(L.innerTasks[tr][d]));
     }
+  }
   std::vector<RowMap> rowMap;
   int dense = 0;
   for (int u : t.decideNodes) {
@@ -161,6 +169,7 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
                oStates = A.take(bytesOf(L.states)), oU8 = A.take(bytesOf(L.poolU8)),
                oU16 = A.take(bytesOf(L.poolU16)), oI16 = A.take(bytesOf(L.poolI16)),
                oSd = A.take(bytesOf(L.poolSd)), oTasks = A.take(bytesOf(tasks)),
+               oGroups = A.take(bytesOf(L.groups)),
                oMap = A.take(bytesOf(rowMap)), oReg = A.take(L.regQuads * 16),
                oStr = A.take(L.regQuads * 16), oCfv = A.take(L.cfvQuads * 16),
                oReach0 = A.take(L.reachQuads[0] * 16), oReach1 = A.take(L.reachQuads[1] * 16),
@@ -185,6 +194,7 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
   put(oI16, L.poolI16);
   put(oSd, L.poolSd);
   put(oTasks, tasks);
+  put(oGroups, L.groups);
   put(oMap, rowMap);
   put(oCoef, coef);
   put(oReach0, rootReach[0]);
@@ -224,8 +234,10 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
   rows.cfv = reinterpret_cast<float*>(base + oCfv);
   const int* dTasks = reinterpret_cast<const int*>(base + oTasks);
 
-  const size_t smem = bwdScratchBytes<float>(L.maxN);
-  raiseSmemLimit((const void*)bwdLevelK<float>, smem);
+  const int4* groups = reinterpret_cast<const int4*>(base + oGroups);
+  const size_t smemSd = sdGroupSmem(L.maxN), smemFd = fdGroupSmem(L.maxN);
+  raiseSmemLimit((const void*)sdGroupK, smemSd);
+  raiseSmemLimit((const void*)fdGroupK, smemFd);
   auto grid = [](int count) { return (unsigned)std::min(count, 1 << 20); };
   for (int it = 0; it < iterations; ++it) {
     for (int tr = 0; tr < 2; ++tr) {
@@ -233,10 +245,17 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
         if (fwd[tr][d].second)
           fwdLevelK<float><<<grid(fwd[tr][d].second), kThreads, 0, stream>>>(
               tree, rows, dTasks + fwd[tr][d].first, fwd[tr][d].second, tr, 0);
-      for (int d = D - 1; d >= 0; --d)
-        if (bwd[tr][d].second)
-          bwdLevelK<float><<<grid(bwd[tr][d].second), kThreads, smem, stream>>>(
-              tree, rows, dTasks + bwd[tr][d].first, bwd[tr][d].second, tr, kModeCFR, L.maxN);
+      for (int d = D - 1; d >= 0; --d) {
+        if (sdG[d].second)
+          sdGroupK<<<grid(sdG[d].second), kTermThreads, smemSd, stream>>>(
+              tree, rows, groups, dTasks + sdG[d].first, sdG[d].second, tr, L.maxN);
+        if (fdG[d].second)
+          fdGroupK<<<grid(fdG[d].second), kTermThreads, smemFd, stream>>>(
+              tree, rows, groups, dTasks + fdG[d].first, fdG[d].second, tr, L.maxN);
+        if (inner[tr][d].second)
+          bwdInteriorK<float><<<grid(inner[tr][d].second), kThreads, 0, stream>>>(
+              tree, rows, dTasks + inner[tr][d].first, inner[tr][d].second, tr, kModeCFR);
+      }
     }
     advanceCounterK<<<1, 32, 0, stream>>>(counter, 1);
     NA_CK(cudaGetLastError());

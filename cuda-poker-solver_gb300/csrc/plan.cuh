@@ -13,6 +13,7 @@
 #include "compiler.h"
 #include "kernels.cuh"
 #include "pps_gb.h"
+#include "terminal.cuh"
 
 namespace pps {
 namespace gb {
@@ -31,10 +32,10 @@ struct ListRef {
   int off = 0, count = 0;
 };
 
-enum LaunchKind { kFwd, kBwd, kBwdTerm, kBwdInt, kLeafSweep, kCounter };
+enum LaunchKind { kFwd, kBwd, kBwdTerm, kBwdInt, kSdGroup, kFdGroup, kCounter };
 inline const char* launchName(LaunchKind k) {
   static const char* names[] = {"fwd_level", "bwd_level", "bwd_terminal", "bwd_interior",
-                                "leaf_street", "counter"};
+                                "bwd_showdown", "bwd_fold", "counter"};
   return names[k];
 }
 
@@ -56,13 +57,16 @@ struct PlanArgs {
   int spots;    // counters advanced per iteration
   int maxN;     // largest combo list (shared scratch layout)
   size_t smem;  // bwdScratchBytes<float>(maxN)
+  const int4* groups;     // terminal groups (TermGroup)
+  size_t smemSd, smemFd;  // sdGroupSmem / fdGroupSmem(maxN)
 };
 
 inline unsigned gridOf(int count) { return (unsigned)std::min(count, 1 << 20); }
 
-// One CFR-mode launch of the plan on stream s (kLeafSweep is issued by the
-// engine that owns a leaf plan).
-inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t s) {
+// One CFR-mode launch of the plan on stream s. Internal linkage, like the
+// kernels it launches that have no template parameter: each translation
+// unit launches (and sets the shared-memory limit of) its own copy.
+static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t s) {
   const unsigned g = gridOf(l.list.count);
   const int* tk = a.tasks + l.list.off;
   switch (l.kind) {
@@ -81,37 +85,65 @@ inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t s) {
       bwdInteriorK<float><<<g, kThreads, 0, s>>>(a.tree, a.rows, tk, l.list.count, l.tr,
                                                  kModeCFR);
       break;
+    case kSdGroup:
+      sdGroupK<<<g, kTermThreads, a.smemSd, s>>>(a.tree, a.rows, a.groups, tk, l.list.count,
+                                                 l.tr, a.maxN);
+      break;
+    case kFdGroup:
+      fdGroupK<<<g, kTermThreads, a.smemFd, s>>>(a.tree, a.rows, a.groups, tk, l.list.count,
+                                                 l.tr, a.maxN);
+      break;
     case kCounter:
       advanceCounterK<<<(a.spots + 255) / 256, 256, 0, s>>>(a.counter, a.spots);
-      break;
-    case kLeafSweep:
       break;
   }
 }
 
-// Streams and events of a two-branch plan.
+// Streams and events of a plan with up to kSides + 1 concurrent branches.
+constexpr int kSides = 3;
 struct Branches {
-  cudaStream_t main = nullptr, side = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaStream_t main = nullptr, side[kSides] = {};
+  cudaEvent_t fork = nullptr, join[kSides] = {};
+  void create(cudaStream_t mainStream) {
+    main = mainStream;
+    GB_CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    for (int k = 0; k < kSides; ++k) {
+      GB_CK(cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking));
+      GB_CK(cudaEventCreateWithFlags(&join[k], cudaEventDisableTiming));
+    }
+  }
+  void destroy() {
+    if (fork) cudaEventDestroy(fork);
+    for (int k = 0; k < kSides; ++k) {
+      if (side[k]) cudaStreamDestroy(side[k]);
+      if (join[k]) cudaEventDestroy(join[k]);
+    }
+  }
 };
 
-// Issues a plan; a launch marked withNext runs beside the next one on the
-// side stream, forked from and joined back into the main stream. `one`
-// issues a single launch (so callers can add launch kinds of their own).
+// Issues a plan; a run of launches chained by withNext runs concurrently:
+// the first on the main stream, the others on side streams forked from it
+// and joined back (graph branches under capture). `one` issues a single
+// launch on a stream.
 template <typename IssueOne>
 void issuePlan(const std::vector<Launch>& P, const Branches& b, IssueOne&& one) {
-  for (size_t i = 0; i < P.size(); ++i) {
-    if (P[i].withNext && i + 1 < P.size()) {
-      GB_CK(cudaEventRecord(b.fork, b.main));
-      GB_CK(cudaStreamWaitEvent(b.side, b.fork, 0));
+  for (size_t i = 0; i < P.size();) {
+    size_t j = i;
+    while (j + 1 < P.size() && P[j].withNext && (int)(j - i) < kSides) ++j;
+    if (j == i) {
       one(P[i], b.main);
-      one(P[i + 1], b.side);
-      GB_CK(cudaEventRecord(b.join, b.side));
-      GB_CK(cudaStreamWaitEvent(b.main, b.join, 0));
       ++i;
-    } else {
-      one(P[i], b.main);
+      continue;
     }
+    GB_CK(cudaEventRecord(b.fork, b.main));
+    for (size_t k = i + 1; k <= j; ++k) GB_CK(cudaStreamWaitEvent(b.side[k - i - 1], b.fork, 0));
+    one(P[i], b.main);
+    for (size_t k = i + 1; k <= j; ++k) one(P[k], b.side[k - i - 1]);
+    for (size_t k = i + 1; k <= j; ++k) {
+      GB_CK(cudaEventRecord(b.join[k - i - 1], b.side[k - i - 1]));
+      GB_CK(cudaStreamWaitEvent(b.main, b.join[k - i - 1], 0));
+    }
+    i = j + 1;
   }
 }
 

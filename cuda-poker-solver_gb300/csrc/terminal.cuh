@@ -1,0 +1,363 @@
+// Terminal groups: the showdown and fold nodes of one depth level and one
+// board state, taken four at a time (the f32 DCFR iteration).
+//
+// The four nodes share the state's tables (strength order, card segments,
+// card lists, showdown entries), so a CTA stages those once and runs the
+// four nodes' arithmetic side by side as float4 lanes: reach rows are staged
+// transposed (entry j of the four rows is one float4), every scan and
+// gather moves float4s, and each table entry is decoded once for all four
+// nodes. The per-node formulas are those of showdownNode / foldNode
+// (kernels.cuh; the reference's cuda/gpu_cfr.cu:355-406 and 433-454):
+//   showdown: win / tie / lose masses from an exclusive prefix of the
+//     strength-sorted opponent reach (blocks of 128 positions, block
+//     totals accumulated compensated, as (hi, lo) pairs), minus the
+//     opponents holding either card (per-card segment prefixes X read at
+//     precomputed counts), plus the identical combo once in the tie band;
+//   fold: (total - card sums of both cards + identical combo) x payoff,
+//     card sums in a fixed order (no atomics).
+#pragma once
+
+#include "kernels.cuh"
+
+namespace pps {
+namespace gb {
+
+constexpr int kTermThreads = 256;
+
+// ---- float4 lane arithmetic ----
+__device__ __forceinline__ float4 operator+(float4 a, float4 b) {
+  return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+__device__ __forceinline__ float4 operator-(float4 a, float4 b) {
+  return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+}
+__device__ __forceinline__ float4& operator+=(float4& a, float4 b) { return a = a + b; }
+__device__ __forceinline__ float4 max0(float4 a) {
+  return make_float4(a.x > 0.f ? a.x : 0.f, a.y > 0.f ? a.y : 0.f, a.z > 0.f ? a.z : 0.f,
+                     a.w > 0.f ? a.w : 0.f);
+}
+__device__ __forceinline__ float4 zero4() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+__device__ __forceinline__ float4 shflUp4(float4 v, int off, int width = 32) {
+  return make_float4(__shfl_up_sync(0xffffffffu, v.x, off, width),
+                     __shfl_up_sync(0xffffffffu, v.y, off, width),
+                     __shfl_up_sync(0xffffffffu, v.z, off, width),
+                     __shfl_up_sync(0xffffffffu, v.w, off, width));
+}
+__device__ __forceinline__ float4 shflXor4(float4 v, int mask, int width = 32) {
+  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, mask, width),
+                     __shfl_xor_sync(0xffffffffu, v.y, mask, width),
+                     __shfl_xor_sync(0xffffffffu, v.z, mask, width),
+                     __shfl_xor_sync(0xffffffffu, v.w, mask, width));
+}
+__device__ __forceinline__ float comp4(float4 v, int g) {
+  return g == 0 ? v.x : g == 1 ? v.y : g == 2 ? v.z : v.w;
+}
+
+// ---- shared-memory layout of a group task (maxN: largest list) ----
+// The sorted prefix gives each thread kSpan consecutive positions, so one
+// pass of kTermThreads threads covers every list (kSpan * 256 >= 1327); a
+// warp's 256 positions form one compensation block.
+constexpr int kSpan = 8;
+constexpr int kSpanShift = 8;  // log2(32 * kSpan): position -> warp block
+__host__ __device__ inline int groupTabEntries(int maxN) { return (3 * maxN + 53 + 7) / 8 * 8; }
+__host__ __device__ inline int groupPrefixEntries(int maxN) { return maxN + kSpan; }
+__host__ __device__ inline int groupXEntries(int maxN) { return 2 * maxN + 52; }
+constexpr int kGroupBlocks = kTermThreads / 32 + 1;  // warp blocks + the total
+
+// Showdown groups: tab | rs4 | P4 | X4 | W4 | WH | WL.
+__host__ __device__ inline size_t sdGroupSmem(int maxN) {
+  return (size_t)groupTabEntries(maxN) * 2 +
+         16 * ((size_t)4 * ((maxN + 3) / 4) + groupPrefixEntries(maxN) + groupXEntries(maxN) +
+               3 * kGroupBlocks);
+}
+// Fold groups: tab | rs4 | cs4[53] | warp partials[8].
+__host__ __device__ inline size_t fdGroupSmem(int maxN) {
+  return (size_t)groupTabEntries(maxN) * 2 + 16 * ((size_t)4 * ((maxN + 3) / 4) + 53 + 8);
+}
+
+// Stages the group's opponent reach rows transposed: rs4[j] holds entry j
+// of the four rows (0 for an absent node).
+static __device__ __forceinline__ void stageRows4(float4* rs4, const DevTree& t, const DevRows<float>& rows,
+                                           const int (&u)[4], int tr, int no) {
+  const float* r[4];
+#pragma unroll
+  for (int g = 0; g < 4; ++g)
+    r[g] = u[g] >= 0 ? rows.reach[tr] + (size_t)t.rows[u[g]].reachQ[tr] * 4 : nullptr;
+  for (int q = threadIdx.x; q < quadsOf(no); q += blockDim.x) {
+    float4 v[4];
+#pragma unroll
+    for (int g = 0; g < 4; ++g)
+      v[g] = r[g] ? *reinterpret_cast<const float4*>(r[g] + 4 * q) : zero4();
+    rs4[4 * q + 0] = make_float4(v[0].x, v[1].x, v[2].x, v[3].x);
+    rs4[4 * q + 1] = make_float4(v[0].y, v[1].y, v[2].y, v[3].y);
+    rs4[4 * q + 2] = make_float4(v[0].z, v[1].z, v[2].z, v[3].z);
+    rs4[4 * q + 3] = make_float4(v[0].w, v[1].w, v[2].w, v[3].w);
+  }
+}
+
+// Value rows of the group's nodes (nullptr for an absent node).
+static __device__ __forceinline__ void outRows4(float* (&out)[4], const DevTree& t,
+                                                const DevRows<float>& rows, const int (&u)[4]) {
+#pragma unroll
+  for (int g = 0; g < 4; ++g)
+    out[g] = u[g] >= 0 ? rows.cfv + (size_t)t.rows[u[g]].cfvQ * 4 : nullptr;
+}
+static __device__ __forceinline__ void storeOut4(float* const (&out)[4], int i, float4 c) {
+  if (out[0]) out[0][i] = c.x;
+  if (out[1]) out[1][i] = c.y;
+  if (out[2]) out[2][i] = c.z;
+  if (out[3]) out[3][i] = c.w;
+}
+
+static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& rows, const int (&u)[4],
+                              int tr, unsigned char* smem, int maxN) {
+  const NodeDev nd = t.nodes[u[0]];
+  const StateDev& st = t.states[nd.state];
+  const int opp = 1 - tr;
+  const int no = st.n[opp], nt = st.n[tr];
+  uint16_t* tab = reinterpret_cast<uint16_t*>(smem);
+  float4* rs4 = reinterpret_cast<float4*>(smem + (size_t)groupTabEntries(maxN) * 2);
+  float4* P4 = rs4 + 4 * ((maxN + 3) / 4);
+  float4* X4 = P4 + groupPrefixEntries(maxN);
+  float4* W4 = X4 + groupXEntries(maxN);
+  float* BH = reinterpret_cast<float*>(W4 + kGroupBlocks);  // [warp block][4]
+  float* BL = BH + 4 * kGroupBlocks;
+  const uint16_t* ord = tab;
+  const uint16_t* seg = ord + no;
+  const uint16_t* segSlot = seg + 53;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+
+  stageTab(tab, t.poolU16 + st.sdOff[tr], 3 * no + 53);
+  stageRows4(rs4, t, rows, u, tr, no);
+  __syncthreads();
+
+  // Exclusive prefixes of the strength-sorted reach in one pass: thread t
+  // takes positions [8t, 8t + 8); lane totals are scanned within the warp
+  // (uncompensated within a warp's 256 positions) and the warp totals go
+  // to W4 for the compensated pass below. Warps past the list end skip it.
+  const int nbw = (no >> kSpanShift) + 1;  // warp blocks covering 0..no
+  if (warp < nbw) {
+    const int k0 = threadIdx.x * kSpan;
+    float4 v[kSpan];
+    const bool any = k0 <= no;
+    const uint4 o8 = any && k0 < no ? *reinterpret_cast<const uint4*>(ord + k0) : make_uint4(0, 0, 0, 0);
+    const uint16_t* o = reinterpret_cast<const uint16_t*>(&o8);
+#pragma unroll
+    for (int j = 0; j < kSpan; ++j) v[j] = k0 + j < no ? rs4[o[j]] : zero4();
+    float4 pre[kSpan];
+    float4 run = zero4();
+#pragma unroll
+    for (int j = 0; j < kSpan; ++j) {
+      pre[j] = run;
+      run += v[j];
+    }
+    float4 incl = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const float4 x = shflUp4(incl, off);
+      if (lane >= off) incl += x;
+    }
+    float4 ex = shflUp4(incl, 1);
+    if (lane == 0) ex = zero4();
+    if (any)
+#pragma unroll
+      for (int j = 0; j < kSpan; ++j) P4[k0 + j] = ex + pre[j];
+    if (lane == 31) W4[warp] = incl;
+  }
+  // Card segments, four cards per warp (8 lanes x 8 entries per card):
+  // X4[seg[c] + c + k] = reach of the card's first k entries, k = 0..len.
+  for (int cb = warp * 4; cb < 52; cb += nw * 4) {
+    const int c = cb + (lane >> 3), sub = lane & 7;
+    const int s0 = seg[c], len = seg[c + 1] - s0;
+    float4 pre[8];
+    float4 run = zero4();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int e = sub * 8 + j;
+      pre[j] = run;
+      if (e < len) run += rs4[segSlot[s0 + e]];
+    }
+    float4 incl = run;
+#pragma unroll
+    for (int off = 1; off < 8; off <<= 1) {
+      const float4 x = shflUp4(incl, off, 8);
+      if (sub >= off) incl += x;
+    }
+    float4 base = shflUp4(incl, 1, 8);
+    if (sub == 0) base = zero4();
+    float4* xo = X4 + s0 + c;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int e = sub * 8 + j;
+      if (e <= len) xo[e] = base + pre[j];
+    }
+  }
+  __syncthreads();
+  // Compensated exclusive prefix of the warp-block totals, one thread per
+  // node.
+  if (threadIdx.x < 4) {
+    const int g = threadIdx.x;
+    float hi = 0.f, lo = 0.f;
+    for (int b = 0; b < nbw; ++b) {
+      BH[4 * b + g] = hi;
+      BL[4 * b + g] = lo;
+      addComp(hi, lo, comp4(W4[b], g));
+    }
+  }
+  __syncthreads();
+
+  const float4* BH4 = reinterpret_cast<const float4*>(BH);
+  const float4* BL4 = reinterpret_cast<const float4*>(BL);
+  float4 win4 = zero4(), tie4 = zero4(), lose4 = zero4();
+  {
+    float w[4] = {0.f, 0.f, 0.f, 0.f}, ti[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int g = 0; g < 4; ++g)
+      if (u[g] >= 0) {
+        const float* tv = t.termVal + ((size_t)u[g] * 2 + tr) * 4;
+        w[g] = tv[0];
+        ti[g] = tv[1];
+        lo[g] = tv[2];
+      }
+    win4 = make_float4(w[0], w[1], w[2], w[3]);
+    tie4 = make_float4(ti[0], ti[1], ti[2], ti[3]);
+    lose4 = make_float4(lo[0], lo[1], lo[2], lo[3]);
+  }
+  const ShowdownInfo* info = t.poolSd + st.sdInfoOff[tr];
+  const int bn = no >> kSpanShift;
+  const float4 TH = BH4[bn], TL = BL4[bn], Pno = P4[no];
+  float* out[4];
+  outRows4(out, t, rows, u);
+  const int nt4 = quadsOf(nt) * 4;
+#pragma unroll 2
+  for (int i = threadIdx.x; i < nt4; i += blockDim.x) {
+    if (i >= nt) {
+      storeOut4(out, i, zero4());
+      continue;
+    }
+    const ShowdownInfo f = info[i];
+    const int le = f.x & 0xffff, te = f.x >> 16;
+    const int len1 = f.y & 0xff, len2 = (f.y >> 8) & 0xff;
+    const int a1 = f.w & 0xffff, a2 = f.w >> 16;
+    const float4 x1le = X4[a1 + ((f.y >> 16) & 0xff)], x1te = X4[a1 + (f.y >> 24)];
+    const float4 x2le = X4[a2 + (f.z & 0xff)], x2te = X4[a2 + ((f.z >> 8) & 0xff)];
+    const float4 x1end = X4[a1 + len1], x2end = X4[a2 + len2];
+    const int same = (int)(f.z >> 16) - 1;
+    const float4 sameR = same >= 0 ? rs4[same] : zero4();
+    const int bl = le >> kSpanShift, bt = te >> kSpanShift;
+    const float4 bhl = BH4[bl], bll = BL4[bl], bht = BH4[bt], blt = BL4[bt];
+    const float4 ple = P4[le], pte = P4[te];
+    const float4 below = bhl + (bll + ple);
+    const float4 band = (bht - bhl) + (blt - bll) + (pte - ple);
+    const float4 above = (TH - bht) + (TL - blt) + (Pno - pte);
+    const float4 lm = max0(below - x1le - x2le);
+    const float4 tm = max0(band - (x1te - x1le) - (x2te - x2le) + sameR);
+    const float4 gm = max0(above - (x1end - x1te) - (x2end - x2te));
+    const float4 c = make_float4(lm.x * win4.x + tm.x * tie4.x + gm.x * lose4.x,
+                                 lm.y * win4.y + tm.y * tie4.y + gm.y * lose4.y,
+                                 lm.z * win4.z + tm.z * tie4.z + gm.z * lose4.z,
+                                 lm.w * win4.w + tm.w * tie4.w + gm.w * lose4.w);
+    storeOut4(out, i, c);
+  }
+}
+
+static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, const int (&u)[4], int tr,
+                          unsigned char* smem, int maxN) {
+  const NodeDev nd = t.nodes[u[0]];
+  const StateDev& st = t.states[nd.state];
+  const int opp = 1 - tr;
+  const int no = st.n[opp], nt = st.n[tr];
+  uint16_t* csr = reinterpret_cast<uint16_t*>(smem);
+  float4* rs4 = reinterpret_cast<float4*>(smem + (size_t)groupTabEntries(maxN) * 2);
+  float4* cs4 = rs4 + 4 * ((maxN + 3) / 4);  // [52] card sums, [52] total
+  float4* part = cs4 + 53;                   // [8] warp partial totals
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+
+  stageTab(csr, t.poolU16 + st.csrOff[opp], 53 + 2 * no);
+  stageRows4(rs4, t, rows, u, tr, no);
+  __syncthreads();
+  // Card sums, four cards per warp (8 lanes x 8 entries, then a fixed
+  // xor tree over the 8 lanes).
+  for (int cb = warp * 4; cb < 52; cb += nw * 4) {
+    const int c = cb + (lane >> 3), sub = lane & 7;
+    const int s0 = csr[c], len = csr[c + 1] - s0;
+    float4 a = zero4();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int e = sub * 8 + j;
+      if (e < len) a += rs4[csr[53 + s0 + e]];
+    }
+#pragma unroll
+    for (int m = 4; m > 0; m >>= 1) a += shflXor4(a, m, 8);
+    if (sub == 0) cs4[c] = a;
+  }
+  // Total: strided partial sums, a fixed xor tree per warp, warps in order.
+  {
+    float4 a = zero4();
+    for (int j = threadIdx.x; j < no; j += blockDim.x) a += rs4[j];
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) a += shflXor4(a, m);
+    if (lane == 0) part[warp] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float4 s = part[0];
+    for (int w = 1; w < nw; ++w) s += part[w];
+    cs4[52] = s;
+  }
+  __syncthreads();
+  const float4 tot = cs4[52];
+  float v[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int g = 0; g < 4; ++g)
+    if (u[g] >= 0) v[g] = t.termVal[((size_t)u[g] * 2 + tr) * 4];
+  const uint16_t* cards = reinterpret_cast<const uint16_t*>(t.poolU8 + st.cardsOff[tr]);
+  const int16_t* same = t.poolI16 + st.sameOff[tr];
+  float* out[4];
+  outRows4(out, t, rows, u);
+  const int nt4 = quadsOf(nt) * 4;
+#pragma unroll 2
+  for (int i = threadIdx.x; i < nt4; i += blockDim.x) {
+    if (i >= nt) {
+      storeOut4(out, i, zero4());
+      continue;
+    }
+    const int cp = cards[i], sm = same[i];
+    float4 w = tot - cs4[cp & 0xff] - cs4[cp >> 8];
+    if (sm >= 0) w += rs4[sm];
+    w = max0(w);
+    storeOut4(out, i, make_float4(w.x * v[0], w.y * v[1], w.z * v[2], w.w * v[3]));
+  }
+}
+
+// One CTA per group task: task word kind 3 (showdown) or 2 (fold), node
+// field = index into the group table (four node ids, -1 for none). One
+// kernel per kind (the showdown tables need 4x the shared memory and more
+// registers; folds fit more CTAs per SM). Internal linkage: this header is
+// included by more than one translation unit, each keeping its own copy.
+static __global__ void __launch_bounds__(kTermThreads, 2)
+sdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
+         const int* __restrict__ tasks, int count, int tr, int maxN) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
+    const int4 g = groups[(unsigned)tasks[i] >> 8];
+    const int u[4] = {g.x, g.y, g.z, g.w};
+    showdownGroup(t, rows, u, tr, smem, maxN);
+    __syncthreads();  // the next task reuses the shared memory
+  }
+}
+
+static __global__ void __launch_bounds__(kTermThreads, 4)
+fdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
+         const int* __restrict__ tasks, int count, int tr, int maxN) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
+    const int4 g = groups[(unsigned)tasks[i] >> 8];
+    const int u[4] = {g.x, g.y, g.z, g.w};
+    foldGroup(t, rows, u, tr, smem, maxN);
+    __syncthreads();
+  }
+}
+
+}  // namespace gb
+}  // namespace pps

@@ -97,7 +97,7 @@ typedef struct {
   int64_t device_bytes;
   int64_t h2d_bytes; /* host->device bytes copied since creation */
   int64_t d2h_bytes; /* device->host bytes copied since creation */
-  int32_t engine;    /* 0 depth-level kernels, 1 fused leaf-street kernel */
+  int32_t engine;    /* 0 terminal groups (default), 1 per-node terminal kernels */
 } pps_gb_info;
 
 /* Per kernel class of one profile pass (pps_gb_profile). */
@@ -217,8 +217,10 @@ int pps_gb_write_rows(pps_gb_solver* h, int which, const float* in,
  * *value the range-weighted root value in chips. */
 int pps_gb_walk(pps_gb_solver* h, int traverser, int mode, double* root_cfv,
                 double* value);
-/* Iteration engine choice for the CFR graph: 0 = depth-level kernels,
- * 1 = fused leaf-street kernel where the tree allows it (default). */
+/* Extension: backward terminal kernels of the CFR graph. 0 (default) =
+ * showdown and fold nodes of one level and board state in groups of four
+ * (one CTA each, float4 lanes); 1 = one CTA per terminal node. Both follow
+ * the same formulas; rows agree to f32 rounding. */
 int pps_gb_set_engine(pps_gb_solver* h, int engine);
 
 /* Benchmark helper: enqueues n further DCFR iterations (graph replays that

@@ -50,13 +50,15 @@ def _spots():
 
 
 def _submit(b, sp, frac=0.005):
+    """frac: target exploitability as a fraction of the pot (< 0: none)."""
     streets = None
     if sp.street_cfgs:
         streets = [{"bets": c.bet_text(), "raises": c.raise_text() or [],
                     "max_raises": c.max_raises} for c in sp.street_cfgs]
     return b.submit(sp.board_text(), weights(sp.oop), weights(sp.ip), sp.pot, sp.stack,
                     bets=sp.cfg.bet_text(), raises=sp.cfg.raise_text() or [],
-                    max_raises=sp.cfg.max_raises, streets=streets, target_frac=frac)
+                    max_raises=sp.cfg.max_raises, streets=streets,
+                    target=frac * sp.pot if frac > 0 else -1.0)
 
 
 def _normwise(a, b):
@@ -124,15 +126,25 @@ def test_batch_equals_lone_solver(mixed):
         assert _normwise(rows[i], lone) <= ROW_TOL
 
 
-def test_river_ev_within_a_hundredth_of_the_oracle(mixed):
-    spots, (res, _, _) = mixed
-    for i in (0, 1):
-        sp, r = spots[i], res[i]
+def test_river_ev_within_a_hundredth_of_the_oracle():
+    """River spots run in a batch to a fixed 512 iterations (no target):
+    EVs within 0.01 chips of the FP64 CPU oracle after the same iterations.
+    (Early on, regret matching amplifies f32 rounding wherever regrets sit
+    at zero, so the gate is taken where the strategies have settled.)"""
+    import pps
+    spots = [wl.river_c1(), wl.river_geo()]
+    b = pps.Batch(check_every=CHECK, max_iterations=512)
+    tickets = [_submit(b, sp, frac=-1.0) for sp in spots]
+    assert b.run(timeout=120)
+    for sp, t in zip(spots, tickets):
+        r = b.result(t)
+        assert r["iterations"] == 512 and not r["converged"]
         o = oracle(sp, precision=64)
-        o.iterate(r["iterations"])
+        o.iterate(512)
         st = o.stats(sp.pot)
         assert abs(st["ev_oop"] - r["ev_oop"]) < 0.01
         assert abs(st["ev_ip"] - r["ev_ip"]) < 0.01
+    b.close()
 
 
 def test_budget_admits_one_at_a_time_without_changing_results():

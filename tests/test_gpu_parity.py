@@ -107,18 +107,36 @@ def test_deterministic_rows():
     assert np.array_equal(a.read_rows(1), b.read_rows(1))
 
 
-@pytest.mark.parametrize("name", ["river_c1", "turn_api", "turn_short", "flop_short"])
-def test_engines_bitwise_equal(name):
-    """The fused leaf-street kernel and the depth-level kernels run the same
-    per-node arithmetic: identical rows."""
+@pytest.mark.parametrize("name", ["river_c1", "turn_api", "turn_short", "flop_short", "river_geo"])
+def test_terminal_groups_match_per_node_kernels(name):
+    """Engine 0 (showdown / fold nodes in groups of four, float4 lanes,
+    128-position prefix blocks) and engine 1 (one CTA per terminal node,
+    32-position blocks) evaluate the same formulas: after 1 iteration the
+    rows agree to f32 rounding (normwise 1e-5); after 300 the solutions pass
+    the oracle gates against each other (EV within 0.01 chips,
+    exploitability ratio in [0.5, 2], or within 0.01 chips where it is ~0).
+    In between, regret matching
+    amplifies rounding wherever regrets sit at zero (see the row cases
+    above), so rows are not compared there."""
     spot = wl.NAMED[name]()
-    a, b = solver(spot), solver(spot)
-    a.set_engine(0)
-    b.set_engine(1)
-    a.solve(20)
-    b.solve(20)
-    for which in (0, 1):
-        assert np.array_equal(a.read_rows(which), b.read_rows(which))
+    for iters in (1, 300):
+        a, b = solver(spot), solver(spot)
+        a.set_engine(0)
+        b.set_engine(1)
+        a.solve(iters)
+        b.solve(iters)
+        assert a.info().engine == 0 and b.info().engine == 1
+        if iters == 1:
+            for which in (0, 1):
+                ra = np.asarray(a.read_rows(which), dtype=np.float64)
+                rb = np.asarray(b.read_rows(which), dtype=np.float64)
+                assert np.max(np.abs(ra - rb)) <= 1e-5 * max(np.max(np.abs(rb)), 1e-30)
+            continue
+        sa, sb = a.stats(), b.stats()
+        assert abs(sa["ev_oop"] - sb["ev_oop"]) < 0.01
+        assert abs(sa["ev_ip"] - sb["ev_ip"]) < 0.01
+        ea, eb = sa["exploitability"], sb["exploitability"]
+        assert abs(ea - eb) < 0.01 or 0.5 <= ea / max(eb, 1e-9) <= 2.0, (ea, eb)
 
 
 def test_full_size_turn_c3_properties():
