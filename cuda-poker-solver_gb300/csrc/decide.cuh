@@ -1,0 +1,207 @@
+// Decide records: the f32 DCFR iteration's decide-node tasks with every row
+// address resolved on the host.
+//
+// A node-based task (kernels.cuh) reaches its rows through a chain of
+// dependent loads (task -> node -> state / children / own row -> each
+// child's row -> data); at four or five round trips of device memory
+// latency per task this chain, not bandwidth, bounds the level launches.
+// A record holds the addresses themselves, so a CTA loads its task offset,
+// then the record (one cache line for up to 12 actions), then the data.
+//
+// Record layout (uint32 words, 16-byte aligned; task lists hold record
+// offsets in 16-byte units):
+//   [0] regQ   regret / strategy rows of the node (quads)
+//   [1] rowQ   backward: the node's value row; forward: its reach row in
+//              the traverser's layout (quads)
+//   [2] n | na << 16 | own << 24   combos of the row's side, actions,
+//              own = 1 when the traverser acts (backward update)
+//   [3] chunk | spot << 16         quad chunk (kChunkQuads quads), spot slot
+//   [4 + a]    action a's child row: backward its value row, forward its
+//              reach row in the traverser's layout (quads)
+// The arithmetic is decideChunk's / fwdDecideChunk's (the reference's
+// cuda/gpu_cfr.cu:240-263 and 479-523).
+#pragma once
+
+#include "kernels.cuh"
+
+namespace pps {
+namespace gb {
+
+__host__ __device__ inline int recordWords(int na) { return (4 + na + 3) / 4 * 4; }
+
+struct DecRec {
+  uint32_t regQ, rowQ;
+  int n, na, own, chunk, spot;
+  const uint32_t* kid;
+};
+
+__device__ __forceinline__ DecRec loadRec(const uint32_t* __restrict__ recs, uint32_t off16) {
+  const uint32_t* r = recs + (size_t)off16 * 4;
+  const uint4 h = *reinterpret_cast<const uint4*>(r);
+  DecRec d;
+  d.regQ = h.x;
+  d.rowQ = h.y;
+  d.n = (int)(h.z & 0xffff);
+  d.na = (int)((h.z >> 16) & 0xff);
+  d.own = (int)(h.z >> 24);
+  d.chunk = (int)(h.w & 0xffff);
+  d.spot = (int)(h.w >> 16);
+  d.kid = r + 4;
+  return d;
+}
+
+// Backward decide record (CFR mode, f32 rows).
+__device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<float>& rows,
+                                             const DecRec& r) {
+  const int nq = quadsOf(r.n);
+  const int q = r.chunk * kChunkQuads + (int)threadIdx.x;
+  if (q >= nq) return;
+  float* out = rows.cfv + (size_t)r.rowQ * 4;
+  bool live[4];
+  for (int l = 0; l < 4; ++l) live[l] = 4 * q + l < r.n;
+  const int na = r.na;
+  if (!r.own) {
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int a = 0; a < na; ++a) {
+      float c[4];
+      ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, c);
+      for (int l = 0; l < 4; ++l) v[l] += c[l];
+    }
+    for (int l = 0; l < 4; ++l)
+      if (!live[l]) v[l] = 0.f;
+    stq(out + 4 * q, v);
+    return;
+  }
+  float* reg = t.regret + (size_t)r.regQ * 4;
+  float* str = t.strat + (size_t)r.regQ * 4;
+  const float* c3 = t.coef + (size_t)t.counter[r.spot] * 3;
+  const float pos = c3[0], neg = c3[1], avg = c3[2];
+  const float uniform = 1.f / (float)na;
+  float val[4] = {0.f, 0.f, 0.f, 0.f}, acc[4] = {0.f, 0.f, 0.f, 0.f};
+  if (na <= kRegNa) {
+    // Regrets stay in registers (then their sigmas); the children's values
+    // are loaded for the value and again (cache hits) for the update.
+    float x[kRegNa][4];
+#pragma unroll
+    for (int a = 0; a < kRegNa; ++a)
+      if (a < na) {
+        ldq(reg + ((size_t)a * nq + q) * 4, x[a]);
+        for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[a][l], 0);
+      }
+#pragma unroll
+    for (int a = 0; a < kRegNa; ++a)
+      if (a < na) {
+        float cv[4];
+        ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, cv);
+        for (int l = 0; l < 4; ++l) {
+          x[a][l] = live[l] ? sigmaOf(x[a][l], acc[l], uniform, 0) : 0.f;
+          val[l] += x[a][l] * cv[l];
+        }
+      }
+    stq(out + 4 * q, val);
+#pragma unroll
+    for (int a = 0; a < kRegNa; ++a)
+      if (a < na) {
+        float rg[4], sg[4], cv[4];
+        const size_t o = ((size_t)a * nq + q) * 4;
+        ldq(reg + o, rg);
+        ldq(str + o, sg);
+        ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, cv);
+        for (int l = 0; l < 4; ++l) {
+          sg[l] = sg[l] * avg + x[a][l];
+          rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (cv[l] - val[l]);
+        }
+        stq(str + o, sg);
+        stq(reg + o, rg);
+      }
+    return;
+  }
+  for (int a = 0; a < na; ++a) {
+    float x[4];
+    ldq(reg + ((size_t)a * nq + q) * 4, x);
+    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
+  }
+  for (int a = 0; a < na; ++a) {
+    float x[4], c[4];
+    ldq(reg + ((size_t)a * nq + q) * 4, x);
+    ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, c);
+    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, 0) : 0.f) * c[l];
+  }
+  stq(out + 4 * q, val);
+  for (int a = 0; a < na; ++a) {
+    float rg[4], sg[4], c[4];
+    const size_t o = ((size_t)a * nq + q) * 4;
+    ldq(reg + o, rg);
+    ldq(str + o, sg);
+    ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, c);
+    for (int l = 0; l < 4; ++l) {
+      const float s = live[l] ? sigmaOf(rg[l], acc[l], uniform, 0) : 0.f;
+      sg[l] = sg[l] * avg + s;
+      rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
+    }
+    stq(str + o, sg);
+    stq(reg + o, rg);
+  }
+}
+
+// Forward decide record (opponent node, CFR mode): child reach = reach x
+// sigma_a from the regrets (regret matching+).
+__device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<float>& rows,
+                                                int tr, const DecRec& r) {
+  const int nq = quadsOf(r.n);
+  const int q = r.chunk * kChunkQuads + (int)threadIdx.x;
+  if (q >= nq) return;
+  const int na = r.na;
+  const float* src = t.regret + (size_t)r.regQ * 4;
+  const float uniform = 1.f / (float)na;
+  float rr[4], acc[4] = {0.f, 0.f, 0.f, 0.f};
+  ldq(rows.reach[tr] + (size_t)r.rowQ * 4 + 4 * q, rr);
+  if (na <= kRegNa) {
+    float x[kRegNa][4];
+#pragma unroll
+    for (int a = 0; a < kRegNa; ++a)
+      if (a < na) {
+        ldq(src + ((size_t)a * nq + q) * 4, x[a]);
+        for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[a][l], 0);
+      }
+#pragma unroll
+    for (int a = 0; a < kRegNa; ++a)
+      if (a < na) {
+        float o[4];
+        for (int l = 0; l < 4; ++l)
+          o[l] = 4 * q + l < r.n ? rr[l] * sigmaOf(x[a][l], acc[l], uniform, 0) : 0.f;
+        stq(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q, o);
+      }
+    return;
+  }
+  for (int a = 0; a < na; ++a) {
+    float x[4];
+    ldq(src + ((size_t)a * nq + q) * 4, x);
+    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
+  }
+  for (int a = 0; a < na; ++a) {
+    float x[4], o[4];
+    ldq(src + ((size_t)a * nq + q) * 4, x);
+    for (int l = 0; l < 4; ++l)
+      o[l] = 4 * q + l < r.n ? rr[l] * sigmaOf(x[l], acc[l], uniform, 0) : 0.f;
+    stq(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q, o);
+  }
+}
+
+// One CTA (kThreads threads) per record, one kernel per pass. Internal
+// linkage: included by more than one translation unit.
+static __global__ void __launch_bounds__(kThreads, 6)
+decideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
+           const uint32_t* __restrict__ tasks, int count) {
+  for (int i = blockIdx.x; i < count; i += gridDim.x) decideRecord(t, rows, loadRec(recs, tasks[i]));
+}
+
+static __global__ void __launch_bounds__(kThreads, 8)
+fwdDecideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
+              const uint32_t* __restrict__ tasks, int count, int tr) {
+  for (int i = blockIdx.x; i < count; i += gridDim.x)
+    fwdDecideRecord(t, rows, tr, loadRec(recs, tasks[i]));
+}
+
+}  // namespace gb
+}  // namespace pps

@@ -62,7 +62,11 @@ struct Engine::Dev {
   std::vector<int> hostTasks;  // host copy of the concatenated task lists
   std::vector<ListRef> fwd[2], bwd[2];
   std::vector<ListRef> sdG, fdG, inner[2];  // the group plan's backward lists
+  std::vector<ListRef> bCh[2], fCh[2];       // its chance word lists
+  std::vector<ListRef> bRec[2], fRec[2];     // its decide record lists (into recTasks)
   int4* groups = nullptr;
+  uint32_t* recs = nullptr;
+  uint32_t* recTasks = nullptr;
   std::vector<Launch> plan[2];  // per engine kind: one iteration
   bool walkReady = false;
   int maxN = 0;
@@ -89,8 +93,8 @@ V* upload(Engine::Dev& d, const std::vector<V>& v, size_t& bytes, int64_t& h2d) 
 }
 
 PlanArgs planArgs(const Engine::Dev& d) {
-  return PlanArgs{d.tree, d.rowsF, d.tasks, d.counter, 1, d.maxN, d.smemF, d.groups,
-                  sdGroupSmem(d.maxN), fdGroupSmem(d.maxN)};
+  return PlanArgs{d.tree,   d.rowsF, d.tasks, d.counter, 1, d.maxN, d.smemF, d.groups,
+                  sdGroupSmem(d.maxN), fdGroupSmem(d.maxN), d.recs, d.recTasks};
 }
 
 // Issues one planned launch (CFR mode, f32 rows) on stream s.
@@ -154,6 +158,19 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
     d.sdG.push_back(addList(L_.sdGroupTasks[dd]));
     d.fdG.push_back(addList(L_.fdGroupTasks[dd]));
   }
+  std::vector<uint32_t> recTasks;
+  for (int tr = 0; tr < 2; ++tr)
+    for (int dd = 0; dd < D; ++dd) {
+      d.bCh[tr].push_back(addList(L_.bwdChance[tr][dd]));
+      d.fCh[tr].push_back(addList(L_.fwdChance[tr][dd]));
+      for (auto* pr : {&d.bRec[tr], &d.fRec[tr]}) {
+        const auto& v = pr == &d.bRec[tr] ? L_.bwdRecs[tr][dd] : L_.fwdRecs[tr][dd];
+        pr->push_back(ListRef{(int)recTasks.size(), (int)v.size()});
+        recTasks.insert(recTasks.end(), v.begin(), v.end());
+      }
+    }
+  d.recs = upload(d, L_.recPool, B, h2d_);
+  d.recTasks = upload(d, recTasks, B, h2d_);
   d.tasks = upload(d, all, B, h2d_);
   d.hostTasks = all;
   d.groups = reinterpret_cast<int4*>(upload(d, L_.groups, B, h2d_));
@@ -230,6 +247,12 @@ void Engine::buildPlans() {
     for (int task : v) b += taskBytes(task, tr, fwd);
     return b;
   };
+  auto kindOnly = [](const std::vector<int>& v, int kind) {
+    std::vector<int> out;
+    for (int w : v)
+      if ((w & 3) == kind) out.push_back(w);
+    return out;
+  };
   auto groupBytes = [&](const std::vector<int>& v, int tr) {
     double b = 0;
     for (int task : v) {
@@ -244,9 +267,21 @@ void Engine::buildPlans() {
     P.clear();
     for (int tr = 0; tr < 2; ++tr) {
       const int D = (int)d.fwd[tr].size();
-      for (int dd = 0; dd < D; ++dd)
-        if (d.fwd[tr][dd].count)
-          P.push_back({kFwd, tr, d.fwd[tr][dd], listBytes(L_.fwdTasks[tr][dd], tr, true)});
+      for (int dd = 0; dd < D; ++dd) {
+        if (kind == 1) {
+          if (d.fwd[tr][dd].count)
+            P.push_back({kFwd, tr, d.fwd[tr][dd], listBytes(L_.fwdTasks[tr][dd], tr, true)});
+          continue;
+        }
+        std::vector<Launch> set;
+        if (d.fRec[tr][dd].count)
+          set.push_back({kFwdRec, tr, d.fRec[tr][dd],
+                         listBytes(kindOnly(L_.fwdTasks[tr][dd], kTaskDecide), tr, true)});
+        if (d.fCh[tr][dd].count)
+          set.push_back({kFwd, tr, d.fCh[tr][dd], listBytes(L_.fwdChance[tr][dd], tr, true)});
+        for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
+        P.insert(P.end(), set.begin(), set.end());
+      }
       for (int dd = D - 1; dd >= 0; --dd) {
         std::vector<Launch> set;
         if (kind == 0) {
@@ -254,6 +289,14 @@ void Engine::buildPlans() {
             set.push_back({kSdGroup, tr, d.sdG[dd], groupBytes(L_.sdGroupTasks[dd], tr)});
           if (d.fdG[dd].count)
             set.push_back({kFdGroup, tr, d.fdG[dd], groupBytes(L_.fdGroupTasks[dd], tr)});
+          if (d.bCh[tr][dd].count)
+            set.push_back({kBwdInt, tr, d.bCh[tr][dd], listBytes(L_.bwdChance[tr][dd], tr, false)});
+          if (d.bRec[tr][dd].count)
+            set.push_back({kDecRec, tr, d.bRec[tr][dd],
+                           listBytes(kindOnly(L_.bwdTasks[tr][dd], kTaskDecide), tr, false)});
+          for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
+          P.insert(P.end(), set.begin(), set.end());
+          continue;
         } else {
           const std::vector<int>& v = L_.bwdTasks[tr][dd];
           const int nt = terminalCount(v);

@@ -41,13 +41,14 @@ namespace {
 // Pools. A region is one index space (node ids, row quads, ...); arrays
 // are the device buffers indexed by it.
 enum Region { rNode, rChild, rState, rU8, rU16, rI16, rSd, rReg, rCfv, rReach0, rReach1, rW,
-              rGroup, kRegions };
+              rGroup, rRec, kRegions };
 // Allocation granule per region, in entries: every range starts on a
-// 16-byte boundary (u16 tables are staged with 16-byte loads).
-constexpr size_t kGranule[kRegions] = {1, 4, 1, 16, 8, 8, 1, 1, 1, 1, 1, 2, 1};
+// 16-byte boundary (u16 tables are staged with 16-byte loads; decide
+// records are addressed in 16-byte units).
+constexpr size_t kGranule[kRegions] = {1, 4, 1, 16, 8, 8, 1, 1, 1, 1, 1, 2, 1, 4};
 
 enum Array { aNodes, aRows, aTerm, aChild, aState, aU8, aU16, aI16, aSd, aReg, aStr, aCfvF,
-             aCfvD, aReachF0, aReachD0, aReachF1, aReachD1, aW, aGroups, kArrays };
+             aCfvD, aReachF0, aReachD0, aReachF1, aReachD1, aW, aGroups, aRecs, kArrays };
 struct ArrayDef {
   Region region;
   size_t entryBytes;
@@ -59,7 +60,7 @@ const ArrayDef kArray[kArrays] = {
     {rReg, 16},               {rReg, 16},                 {rCfv, 16},
     {rCfv, 32},               {rReach0, 16},              {rReach0, 32},
     {rReach1, 16},            {rReach1, 32},              {rW, 8},
-    {rGroup, sizeof(TermGroup)}};
+    {rGroup, sizeof(TermGroup)}, {rRec, sizeof(uint32_t)}};
 
 size_t roundUp(size_t n, size_t g) { return (n + g - 1) / g * g; }
 
@@ -77,6 +78,7 @@ void regionSizes(const Tree& t, const HostLayout& L, size_t out[kRegions]) {
   out[rReach1] = L.reachQuads[1];
   out[rW] = (size_t)t.side[0].n + (size_t)t.side[1].n;  // w0 then w1
   out[rGroup] = L.groups.size();
+  out[rRec] = L.recPool.size();
 }
 
 size_t footprintOf(const Tree& t, const HostLayout& L) {
@@ -259,7 +261,8 @@ struct SlotRec {
   // keep the layout's order (terminal tasks first). The iteration uses the
   // terminal group lists (group ids relocated) and the interior lists.
   std::vector<std::vector<int>> fwd[2], bwd[2], inner[2];
-  std::vector<std::vector<int>> sdG, fdG;
+  std::vector<std::vector<int>> sdG, fdG, bCh[2], fCh[2];
+  std::vector<std::vector<uint32_t>> bRec[2], fRec[2];  // record offsets, relocated
 };
 
 struct Forest::Dev {
@@ -283,6 +286,8 @@ struct Forest::Dev {
   // Iteration graph.
   int* tasks = nullptr;
   size_t tasksCap = 0;
+  uint32_t* recTasks = nullptr;
+  size_t recTasksCap = 0;
   std::vector<Launch> plan;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -440,6 +445,7 @@ Forest::~Forest() {
   cudaFree(d.coef);
   cudaFree(d.counter);
   cudaFree(d.tasks);
+  cudaFree(d.recTasks);
   cudaFree(d.wTasks);
   cudaFree(d.info);
   cudaFree(d.vals);
@@ -470,7 +476,7 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   bool fits = rec.off[rNode] + N < ((size_t)1 << 24);
   for (int r : {rReg, rCfv, rReach0, rReach1})
     fits = fits && rec.off[r] + rec.size[r] <= 0xffffffffull;
-  for (int r : {rChild, rState, rU8, rU16, rI16, rSd, rW, rGroup})
+  for (int r : {rChild, rState, rU8, rU16, rI16, rSd, rW, rGroup, rRec})
     fits = fits && rec.off[r] + rec.size[r] < ((size_t)1 << 31);
   if (!fits) {
     for (int r = 0; r < kRegions; ++r) d.regions[r].release(rec.off[r], rec.size[r], kGranule[r]);
@@ -549,6 +555,21 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
     for (int& u : g.node)
       if (u >= 0) u += (int)off[rNode];
   put(aGroups, off[rGroup], L.groups.data(), L.groups.size() * sizeof(TermGroup));
+  // Decide records: row offsets into the pools, the spot's counter slot.
+  for (int tr = 0; tr < 2; ++tr)
+    for (int fwd = 0; fwd < 2; ++fwd) {
+      const uint32_t rowOff = (uint32_t)(fwd ? off[tr ? rReach1 : rReach0] : off[rCfv]);
+      for (const auto& v : fwd ? L.fwdRecs[tr] : L.bwdRecs[tr])
+        for (uint32_t o : v) {
+          uint32_t* r = &L.recPool[(size_t)o * 4];
+          const int na = (int)((r[2] >> 16) & 0xff);
+          r[0] += (uint32_t)off[rReg];
+          r[1] += rowOff;
+          r[3] = (r[3] & 0xffffu) | ((uint32_t)slot << 16);
+          for (int a = 0; a < na; ++a) r[4 + a] += rowOff;
+        }
+    }
+  put(aRecs, off[rRec], L.recPool.data(), L.recPool.size() * sizeof(uint32_t));
   for (int a : {aReg, aStr, aCfvF, aCfvD, aReachF0, aReachD0, aReachF1, aReachD1}) {
     const Region r = kArray[a].region;
     const size_t bytes = rec.size[r] * kArray[a].entryBytes;
@@ -579,6 +600,19 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
       for (auto& v : *lists)
         for (int& task : v) task = (int)((unsigned)task + nodeShift);
   }
+  const uint32_t recShift = (uint32_t)(off[rRec] / 4);
+  for (int tr = 0; tr < 2; ++tr) {
+    rec.bRec[tr] = std::move(L.bwdRecs[tr]);
+    rec.fRec[tr] = std::move(L.fwdRecs[tr]);
+    rec.bCh[tr] = std::move(L.bwdChance[tr]);
+    rec.fCh[tr] = std::move(L.fwdChance[tr]);
+    for (auto* lists : {&rec.bRec[tr], &rec.fRec[tr]})
+      for (auto& v : *lists)
+        for (uint32_t& o : v) o += recShift;
+    for (auto* lists : {&rec.bCh[tr], &rec.fCh[tr]})
+      for (auto& v : *lists)
+        for (int& task : v) task = (int)((unsigned)task + nodeShift);
+  }
   const unsigned groupShift = (unsigned)off[rGroup] << 8;
   rec.sdG = std::move(L.sdGroupTasks);
   rec.fdG = std::move(L.fdGroupTasks);
@@ -595,6 +629,7 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   L.poolSd = {};
   L.states = {};
   L.groups = {};
+  L.recPool = {};
   d.used += s->bytes;
   rec.spot = std::move(s);
   d.live[slot] = std::move(rec);
@@ -636,7 +671,8 @@ namespace {
 // when `split`). Returns the refs into `all`.
 struct Lists {
   std::vector<int> all;
-  std::vector<ListRef> fwd[2], bwd[2], inner[2], sdG, fdG;
+  std::vector<uint32_t> recs;  // record offsets
+  std::vector<ListRef> fwd[2], bwd[2], fCh[2], bCh[2], fRec[2], bRec[2], sdG, fdG;
 };
 
 Lists gather(const std::map<int, SlotRec>& live, const std::vector<int>& slots, bool iteration) {
@@ -654,13 +690,28 @@ Lists gather(const std::map<int, SlotRec>& live, const std::vector<int>& slots, 
   auto at = [](const std::vector<std::vector<int>>& lists, int dd) {
     return dd < (int)lists.size() ? &lists[dd] : nullptr;
   };
+  auto catRec = [&](auto pick) {
+    const int b = (int)out.recs.size();
+    for (int s : slots) {
+      const std::vector<uint32_t>* v = pick(live.at(s));
+      if (v) out.recs.insert(out.recs.end(), v->begin(), v->end());
+    }
+    return ListRef{b, (int)out.recs.size() - b};
+  };
+  auto atR = [](const std::vector<std::vector<uint32_t>>& lists, int dd) {
+    return dd < (int)lists.size() ? &lists[dd] : nullptr;
+  };
   for (int tr = 0; tr < 2; ++tr)
     for (int dd = 0; dd < D; ++dd) {
-      out.fwd[tr].push_back(cat([&](const SlotRec& r) { return at(r.fwd[tr], dd); }));
-      if (iteration)
-        out.inner[tr].push_back(cat([&](const SlotRec& r) { return at(r.inner[tr], dd); }));
-      else
+      if (iteration) {
+        out.fCh[tr].push_back(cat([&](const SlotRec& r) { return at(r.fCh[tr], dd); }));
+        out.bCh[tr].push_back(cat([&](const SlotRec& r) { return at(r.bCh[tr], dd); }));
+        out.fRec[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.fRec[tr], dd); }));
+        out.bRec[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.bRec[tr], dd); }));
+      } else {
+        out.fwd[tr].push_back(cat([&](const SlotRec& r) { return at(r.fwd[tr], dd); }));
         out.bwd[tr].push_back(cat([&](const SlotRec& r) { return at(r.bwd[tr], dd); }));
+      }
     }
   if (iteration)
     for (int dd = 0; dd < D; ++dd) {
@@ -686,18 +737,30 @@ void Forest::iterate(int n) {
     if (!ls.all.empty())
       GB_CK(cudaMemcpyAsync(d.tasks, ls.all.data(), ls.all.size() * sizeof(int),
                             cudaMemcpyHostToDevice, d.stream));
+    ensureBuf(d.recTasks, d.recTasksCap, std::max<size_t>(ls.recs.size(), 1));
+    if (!ls.recs.empty())
+      GB_CK(cudaMemcpyAsync(d.recTasks, ls.recs.data(), ls.recs.size() * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, d.stream));
     d.plan.clear();
+    auto addSet = [&](std::vector<Launch>& set) {
+      for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
+      d.plan.insert(d.plan.end(), set.begin(), set.end());
+    };
     for (int tr = 0; tr < 2; ++tr) {
-      const int D = (int)ls.fwd[tr].size();
-      for (int dd = 0; dd < D; ++dd)
-        if (ls.fwd[tr][dd].count) d.plan.push_back({kFwd, tr, ls.fwd[tr][dd], 0.0});
+      const int D = (int)ls.fRec[tr].size();
+      for (int dd = 0; dd < D; ++dd) {
+        std::vector<Launch> set;
+        if (ls.fRec[tr][dd].count) set.push_back({kFwdRec, tr, ls.fRec[tr][dd], 0.0});
+        if (ls.fCh[tr][dd].count) set.push_back({kFwd, tr, ls.fCh[tr][dd], 0.0});
+        addSet(set);
+      }
       for (int dd = D - 1; dd >= 0; --dd) {
         std::vector<Launch> set;
         if (ls.sdG[dd].count) set.push_back({kSdGroup, tr, ls.sdG[dd], 0.0});
         if (ls.fdG[dd].count) set.push_back({kFdGroup, tr, ls.fdG[dd], 0.0});
-        if (ls.inner[tr][dd].count) set.push_back({kBwdInt, tr, ls.inner[tr][dd], 0.0});
-        for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
-        d.plan.insert(d.plan.end(), set.begin(), set.end());
+        if (ls.bCh[tr][dd].count) set.push_back({kBwdInt, tr, ls.bCh[tr][dd], 0.0});
+        if (ls.bRec[tr][dd].count) set.push_back({kDecRec, tr, ls.bRec[tr][dd], 0.0});
+        addSet(set);
       }
     }
     d.plan.push_back({kCounter, 0, ListRef{}, 0.0});
@@ -707,7 +770,8 @@ void Forest::iterate(int n) {
     raiseSmemLimit((const void*)fdGroupK, smemFd);
     const PlanArgs args{d.tree(), d.rows<float>(aReachF0, aReachF1, aCfvF), d.tasks, d.counter,
                         (int)d.counterCap, maxN, bwdScratchBytes<float>(maxN),
-                        static_cast<const int4*>(d.arr[aGroups]), smemSd, smemFd};
+                        static_cast<const int4*>(d.arr[aGroups]), smemSd, smemFd,
+                        static_cast<const uint32_t*>(d.arr[aRecs]), d.recTasks};
     GB_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
     issuePlan(d.plan, d.br, [&](const Launch& l, cudaStream_t s) { issueLaunch(args, l, s); });
     const cudaError_t launchErr = cudaGetLastError();
@@ -815,7 +879,8 @@ void Forest::sync() { GB_CK(cudaStreamSynchronize(d_->stream)); }
 size_t Forest::deviceBytes() const {
   const Dev& d = *d_;
   size_t b = (size_t)d.coefEntries * 3 * sizeof(float) + d.counterCap * sizeof(int) +
-             d.tasksCap * sizeof(int) + d.wTasksCap * sizeof(int) +
+             d.tasksCap * sizeof(int) + d.recTasksCap * sizeof(uint32_t) +
+             d.wTasksCap * sizeof(int) +
              d.infoCap * sizeof(RootInfo) + d.valsCap * sizeof(double);
   return b + d.mappedBytes();
 }

@@ -277,6 +277,51 @@ HostLayout buildLayout(const Tree& t) {
         }
       }
   }
+  // Decide records and chance word lists of the default iteration.
+  for (int tr = 0; tr < 2; ++tr) {
+    L.bwdRecs[tr].assign(D, {});
+    L.fwdRecs[tr].assign(D, {});
+    L.bwdChance[tr].assign(D, {});
+    L.fwdChance[tr].assign(D, {});
+    for (int d = 0; d < D; ++d) {
+      for (int w : L.bwdTasks[tr][d])
+        if ((w & 3) == kTaskChance) L.bwdChance[tr][d].push_back(w);
+      for (int w : L.fwdTasks[tr][d])
+        if ((w & 3) == kTaskChance) L.fwdChance[tr][d].push_back(w);
+    }
+  }
+  auto addRecord = [&](uint32_t regQ, uint32_t rowQ, int n, int na, int own, int chunk,
+                       const std::vector<uint32_t>& kids) {
+    const uint32_t off = (uint32_t)(L.recPool.size() / 4);
+    L.recPool.push_back(regQ);
+    L.recPool.push_back(rowQ);
+    L.recPool.push_back((uint32_t)n | ((uint32_t)na << 16) | ((uint32_t)own << 24));
+    L.recPool.push_back((uint32_t)chunk);
+    L.recPool.insert(L.recPool.end(), kids.begin(), kids.end());
+    while (L.recPool.size() % 4) L.recPool.push_back(0);
+    return off;
+  };
+  for (int u = 0; u < N; ++u) {
+    const Node& nd = t.nodes[u];
+    if (nd.kind != kDecide) continue;
+    for (int tr = 0; tr < 2; ++tr) {
+      std::vector<uint32_t> kids(nd.na);
+      for (int a = 0; a < nd.na; ++a) kids[a] = L.rows[t.children[nd.childBase + a]].cfvQ;
+      const int nTr = t.n(u, tr);
+      const int chunksTr = (int)((quads(nTr) + kChunkQuads - 1) / kChunkQuads);
+      for (int c = 0; c < chunksTr; ++c)
+        L.bwdRecs[tr][nd.depth].push_back(
+            addRecord(L.nodes[u].regQ, L.rows[u].cfvQ, nTr, nd.na, nd.player == tr, c, kids));
+      if (nd.player == tr) continue;
+      for (int a = 0; a < nd.na; ++a)
+        kids[a] = L.rows[t.children[nd.childBase + a]].reachQ[tr];
+      const int nOpp = t.n(u, 1 - tr);
+      const int chunksOpp = (int)((quads(nOpp) + kChunkQuads - 1) / kChunkQuads);
+      for (int c = 0; c < chunksOpp; ++c)
+        L.fwdRecs[tr][nd.depth].push_back(
+            addRecord(L.nodes[u].regQ, L.rows[u].reachQ[tr], nOpp, nd.na, 0, c, kids));
+    }
+  }
   if (N >= (1 << 24)) throw Error{PPS_GB_E_MEMORY, "tree too large for 24-bit task node ids"};
   alignU16(L.poolU16);
   return L;

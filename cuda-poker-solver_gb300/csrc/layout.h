@@ -115,6 +115,12 @@ struct HostLayout {
   std::vector<TermGroup> groups;
   std::vector<std::vector<int>> sdGroupTasks, fdGroupTasks;
   std::vector<std::vector<int>> innerTasks[2];
+  // Decide records (decide.cuh) of the default iteration: the pool, and per
+  // traverser and depth the backward and forward record offsets (16-byte
+  // units); the chance tasks of those levels as task words.
+  std::vector<uint32_t> recPool;
+  std::vector<std::vector<uint32_t>> bwdRecs[2], fwdRecs[2];
+  std::vector<std::vector<int>> bwdChance[2], fwdChance[2];
   int maxN = 0;        // largest list size (either side)
   int maxCardSeg = 0;  // longest card segment of any list
 };

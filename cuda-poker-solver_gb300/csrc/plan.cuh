@@ -12,6 +12,7 @@
 
 #include "compiler.h"
 #include "kernels.cuh"
+#include "decide.cuh"
 #include "pps_gb.h"
 #include "terminal.cuh"
 
@@ -32,10 +33,12 @@ struct ListRef {
   int off = 0, count = 0;
 };
 
-enum LaunchKind { kFwd, kBwd, kBwdTerm, kBwdInt, kSdGroup, kFdGroup, kCounter };
+enum LaunchKind { kFwd, kBwd, kBwdTerm, kBwdInt, kSdGroup, kFdGroup, kDecRec, kFwdRec,
+                  kCounter };
 inline const char* launchName(LaunchKind k) {
-  static const char* names[] = {"fwd_level", "bwd_level", "bwd_terminal", "bwd_interior",
-                                "bwd_showdown", "bwd_fold", "counter"};
+  static const char* names[] = {"fwd_level",    "bwd_level", "bwd_terminal", "bwd_interior",
+                                "bwd_showdown", "bwd_fold",  "bwd_decide",   "fwd_decide",
+                                "counter"};
   return names[k];
 }
 
@@ -59,6 +62,8 @@ struct PlanArgs {
   size_t smem;  // bwdScratchBytes<float>(maxN)
   const int4* groups;     // terminal groups (TermGroup)
   size_t smemSd, smemFd;  // sdGroupSmem / fdGroupSmem(maxN)
+  const uint32_t* recs;      // decide record pool
+  const uint32_t* recTasks;  // record offsets (kDecRec / kFwdRec lists index these)
 };
 
 inline unsigned gridOf(int count) { return (unsigned)std::min(count, 1 << 20); }
@@ -92,6 +97,14 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
     case kFdGroup:
       fdGroupK<<<g, kTermThreads, a.smemFd, s>>>(a.tree, a.rows, a.groups, tk, l.list.count,
                                                  l.tr, a.maxN);
+      break;
+    case kDecRec:
+      decideRecK<<<g, kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
+                                        l.list.count);
+      break;
+    case kFwdRec:
+      fwdDecideRecK<<<g, kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
+                                           l.list.count, l.tr);
       break;
     case kCounter:
       advanceCounterK<<<(a.spots + 255) / 256, 256, 0, s>>>(a.counter, a.spots);
