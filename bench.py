@@ -1,6 +1,6 @@
 """Benchmark: DCFR iterations per second on the 48,255-node turn tree.
 
-Workload (turn_c3, BASELINE configs[2]): seeded 4-card board, 60% of combos
+Workload (turn_c3, the ~52k-node turn spot): seeded 4-card board, 60% of combos
 at weight U(0.5,1) and the rest U(0,0.2) (all 1128 combos per side), pot
 100, stack 400, bets {25, 50, 100, 150}% + all-in on both streets, raises
 2x, max 4 bets per street. A step is one DCFR iteration (both alternating
@@ -40,7 +40,7 @@ WORKLOAD = "turn_c3"
 
 
 def workload_config(spot, n_nodes):
-    return {"workload": "turn_c3: %d-node turn tree (BASELINE configs[2])" % n_nodes,
+    return {"workload": "turn_c3: %d-node turn tree, 1000-iteration solve" % n_nodes,
             "board": spot.board_text(), "ranges": "all 1128 combos, 60% U(0.5,1) / 40% U(0,0.2)",
             "pot": spot.pot, "stack": spot.stack, "bets": "0.25,0.5,1,1.5,a", "raises": "2",
             "max_bets_per_street": 4, "iterations_e2e": 1000,
@@ -145,6 +145,90 @@ def cpu_baseline(spot, seconds=12.0):
                       % n}
 
 
+def _submit(batch, sp):
+    from pps import pps_native as pn
+    w = lambda r: pn.parse_range(r) if isinstance(r, str) else r
+    return batch.submit(sp.board_text(), w(sp.oop), w(sp.ip), sp.pot, sp.stack,
+                        bets=sp.cfg.bet_text(), raises=sp.cfg.raise_text() or [],
+                        max_raises=sp.cfg.max_raises, target=0.005 * sp.pot)
+
+
+def batched_bench(spots, loop_sample, check_every=64):
+    """Batched: every spot solved to 0.5%-pot exploitability in one batch
+    (all submitted at once, host compile threads, one device forest), next
+    to the plain loop (pps.Solver per spot, solve with the same target,
+    stats, destroy) timed on a bounded sample of the same spots."""
+    import pps
+    import numpy as np
+    from pps import pps_native as pn
+    b = pps.Batch(check_every=check_every, max_iterations=4096)
+    t0 = time.perf_counter()
+    tickets = [_submit(b, sp) for sp in spots]
+    ok = b.run(timeout=600)
+    el = time.perf_counter() - t0
+    res = [b.result(t) for t in tickets]
+    info = b.info()
+    b.close()
+    its = np.array([r["iterations"] for r in res])
+    w = lambda r: pn.parse_range(r) if isinstance(r, str) else r
+    t1 = time.perf_counter()
+    for sp in loop_sample:
+        s = pps.Solver(board=sp.board_text(), oop=w(sp.oop), ip=w(sp.ip), pot=sp.pot,
+                       stack=sp.stack, bets=sp.cfg.bet_text(), raises=sp.cfg.raise_text() or [],
+                       max_raises=sp.cfg.max_raises)
+        s.solve(4096, "dcfr", 0.005 * sp.pot)
+        s.stats()
+        del s
+    loop_s = time.perf_counter() - t1
+    batched = len(spots) / el
+    loop = len(loop_sample) / loop_s
+    return {"spots": len(spots), "finished": ok, "seconds": el, "solves_per_s": batched,
+            "converged": int(sum(r["converged"] for r in res)),
+            "failed": int(sum(r["status"] != 0 for r in res)),
+            "iterations_mean": float(its.mean()), "iterations_max": int(its.max()),
+            "target": "exploitability <= 0.5%% of pot, checked every %d iterations" % check_every,
+            "max_expl_frac_pot": float(max(r["exploitability"] / sp.pot
+                                           for r, sp in zip(res, spots))),
+            "one_at_a_time": {"solves_per_s": loop, "sample": "first %d of the %d spots"
+                              % (len(loop_sample), len(spots)),
+                              "path": "pps.Solver + solve(target, checks every 128) + stats"},
+            "speedup_vs_one_at_a_time": batched / loop,
+            "device_bytes_peak": info["peak_used_bytes"],
+            "time_split_ms": {k: info[k] for k in ("admit_ms", "iterate_ms", "check_ms",
+                                                  "retire_ms", "idle_ms")}}
+
+
+def served_bench(spots, lam, count, seed=7):
+    """Served: Poisson arrivals at rate lam (a submitting thread sleeps
+    to each arrival time) into a serving batch (its own driver thread);
+    latency = finish - submit on the library clock."""
+    import pps
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, count))
+    b = pps.Batch(check_every=32, max_iterations=4096)
+    b.start()
+    tickets = []
+    t0 = time.perf_counter()
+    for i in range(count):
+        dt = arrivals[i] - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        tickets.append(_submit(b, spots[i % len(spots)]))
+    res = [b.wait(t, timeout=600) for t in tickets]
+    info = b.info()
+    b.stop()
+    b.close()
+    done = [r for r in res if r is not None and r["status"] == 0]
+    lat = np.array([r["latency_ms"] for r in done]) if done else np.array([float("nan")])
+    first = min(r["submit_ms"] for r in done) if done else 0.0
+    last = max(r["finish_ms"] for r in done) if done else 1.0
+    return {"lambda_per_s": lam, "requests": count, "completed": len(done),
+            "solves_per_s": len(done) / max((last - first) / 1000.0, 1e-9),
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "peak_active": info["peak_active"], "offered_seconds": float(arrivals[-1])}
+
+
 def run_reference(args, rank):
     """--impl reference: the CPU restatement of the reference iteration (the
     reference's own CPU path does not exist: its CPU river solver was
@@ -159,7 +243,7 @@ def run_reference(args, rank):
     for _ in range(max(1, min(args.warmup, 2))):
         o.iterate(1)
     steps = max(1, args.steps)
-    budget = 150.0
+    budget = 60.0
     t0 = time.perf_counter()
     done = 0
     while done < steps:
@@ -186,12 +270,18 @@ def run_reference(args, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-iters", type=int, default=1000,
-                    help="iterations of the end-to-end solve (BASELINE: 1000)")
+                    help="iterations of the end-to-end solve (the workload's 1000)")
+    ap.add_argument("--batch-spots", type=int, default=256,
+                    help="spots of the batched solve (0 skips batched and served)")
+    ap.add_argument("--loop-sample", type=int, default=64,
+                    help="spots of the one-at-a-time loop the batched solve is set against")
+    ap.add_argument("--served-requests", type=int, default=400,
+                    help="requests per arrival rate of the served run (0 skips it)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -277,7 +367,31 @@ def main():
             "data": "synthetic", "config": workload_config(spot, info.num_nodes),
             "e2e": e2e, "roofline": roofline, "clocks": clk.summary(),
             "gpu_launches": int(info.launches_per_iteration) * args.steps,
-            "engine": "fused leaf-street" if info.engine == 1 else "depth-level"}
+            "engine": "terminal groups + decide records" if info.engine == 0 else
+                      "per-node terminals"}
+    # The reference's own published spot (tools/quality/bench_turn.sh:40-41,
+    # 51,903 nodes; ~747-807 it/s on an RTX 4070, docs/STATUS.md:69).
+    w52 = wl.turn_w52()
+    sw = pps.Solver(board=w52.board_text(), oop=w52.oop, ip=w52.ip, pot=w52.pot, stack=w52.stack,
+                    bets=w52.cfg.bet_text(), raises=w52.cfg.raise_text(),
+                    max_raises=w52.cfg.max_raises)
+    sw.time_iterations(args.warmup)
+    w52_ms = sw.time_iterations(max(args.steps, 100))
+    line["w52"] = {"value": max(args.steps, 100) / (w52_ms / 1000.0), "unit": "iters/s",
+                   "nodes": sw.num_nodes, "published_rtx4070": "747-807 iters/s"}
+    del sw
+    if world == 1 and args.batch_spots > 0:
+        spots = wl.batched(args.batch_spots)
+        line["batched"] = batched_bench(spots, spots[:max(1, min(args.loop_sample,
+                                                                  len(spots)))])
+        if args.served_requests > 0:
+            stream = wl.batched(1024, seed=505)
+            line["served"] = {"distribution": "batched-distribution spots (seed 505, 1024 "
+                                              "cycled); "
+                                              "target 0.5%% pot; bounded sample of %d "
+                                              "requests per rate" % args.served_requests,
+                              "rates": [served_bench(stream, lam, args.served_requests)
+                                        for lam in (50, 200, 800)]}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(spot)
     print(json.dumps(line), flush=True)

@@ -78,44 +78,9 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
   const float pos = c3[0], neg = c3[1], avg = c3[2];
   const float uniform = 1.f / (float)na;
   float val[4] = {0.f, 0.f, 0.f, 0.f}, acc[4] = {0.f, 0.f, 0.f, 0.f};
-  if (na <= kRegNa) {
-    // Regrets stay in registers (then their sigmas); the children's values
-    // are loaded for the value and again (cache hits) for the update.
-    float x[kRegNa][4];
-#pragma unroll
-    for (int a = 0; a < kRegNa; ++a)
-      if (a < na) {
-        ldq(reg + ((size_t)a * nq + q) * 4, x[a]);
-        for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[a][l], 0);
-      }
-#pragma unroll
-    for (int a = 0; a < kRegNa; ++a)
-      if (a < na) {
-        float cv[4];
-        ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, cv);
-        for (int l = 0; l < 4; ++l) {
-          x[a][l] = live[l] ? sigmaOf(x[a][l], acc[l], uniform, 0) : 0.f;
-          val[l] += x[a][l] * cv[l];
-        }
-      }
-    stq(out + 4 * q, val);
-#pragma unroll
-    for (int a = 0; a < kRegNa; ++a)
-      if (a < na) {
-        float rg[4], sg[4], cv[4];
-        const size_t o = ((size_t)a * nq + q) * 4;
-        ldq(reg + o, rg);
-        ldq(str + o, sg);
-        ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, cv);
-        for (int l = 0; l < 4; ++l) {
-          sg[l] = sg[l] * avg + x[a][l];
-          rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (cv[l] - val[l]);
-        }
-        stq(str + o, sg);
-        stq(reg + o, rg);
-      }
-    return;
-  }
+  // Streaming form: a row is reloaded (a cache hit) instead of held in
+  // registers, which keeps the kernel at 40 registers and 48 warps per SM;
+  // the launches are bound by memory latency, not by instruction count.
   for (int a = 0; a < na; ++a) {
     float x[4];
     ldq(reg + ((size_t)a * nq + q) * 4, x);
@@ -156,24 +121,6 @@ __device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<
   const float uniform = 1.f / (float)na;
   float rr[4], acc[4] = {0.f, 0.f, 0.f, 0.f};
   ldq(rows.reach[tr] + (size_t)r.rowQ * 4 + 4 * q, rr);
-  if (na <= kRegNa) {
-    float x[kRegNa][4];
-#pragma unroll
-    for (int a = 0; a < kRegNa; ++a)
-      if (a < na) {
-        ldq(src + ((size_t)a * nq + q) * 4, x[a]);
-        for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[a][l], 0);
-      }
-#pragma unroll
-    for (int a = 0; a < kRegNa; ++a)
-      if (a < na) {
-        float o[4];
-        for (int l = 0; l < 4; ++l)
-          o[l] = 4 * q + l < r.n ? rr[l] * sigmaOf(x[a][l], acc[l], uniform, 0) : 0.f;
-        stq(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q, o);
-      }
-    return;
-  }
   for (int a = 0; a < na; ++a) {
     float x[4];
     ldq(src + ((size_t)a * nq + q) * 4, x);
@@ -190,13 +137,13 @@ __device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<
 
 // One CTA (kThreads threads) per record, one kernel per pass. Internal
 // linkage: included by more than one translation unit.
-static __global__ void __launch_bounds__(kThreads, 6)
+static __global__ void __launch_bounds__(kThreads, 12)
 decideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
            const uint32_t* __restrict__ tasks, int count) {
   for (int i = blockIdx.x; i < count; i += gridDim.x) decideRecord(t, rows, loadRec(recs, tasks[i]));
 }
 
-static __global__ void __launch_bounds__(kThreads, 8)
+static __global__ void __launch_bounds__(kThreads, 12)
 fwdDecideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
               const uint32_t* __restrict__ tasks, int count, int tr) {
   for (int i = blockIdx.x; i < count; i += gridDim.x)

@@ -67,7 +67,9 @@ struct Engine::Dev {
   int4* groups = nullptr;
   uint32_t* recs = nullptr;
   uint32_t* recTasks = nullptr;
-  std::vector<Launch> plan[2];  // per engine kind: one iteration
+  std::vector<Launch> plan[2];  // per engine kind: one iteration (kind 0 flattened)
+  StagedPlan staged;           // kind 0 as captured
+  StagedEvents sev;
   bool walkReady = false;
   int maxN = 0;
   size_t smemF = 0, smemD = 0;
@@ -196,6 +198,7 @@ Engine::~Engine() {
   for (void* p : d_->owned) cudaFree(p);
   if (d_->stream) cudaStreamDestroy(d_->stream);
   d_->br.destroy();
+  d_->sev.destroy();
 }
 
 void* Engine::stream() const { return (void*)d_->stream; }
@@ -234,12 +237,11 @@ double Engine::taskBytes(int task, int tr, bool fwd) const {
   }
 }
 
-// Plans of one iteration. Kind 0 (default): per backward level, the
-// showdown groups, the fold groups and the interior tasks run as three
-// concurrent launches (terminals read only the traverser's reach rows and
-// write their own value rows; interior tasks read value rows of deeper
-// levels). Kind 1: the same levels with one CTA per terminal node
-// (bwdTerminalK beside bwdInteriorK).
+// Plans of one iteration. Kind 0 (default): the staged plan of plan.cuh
+// (decide records and chance tasks per level; showdown / fold groups of a
+// depth started once its reach rows are written). Kind 1: per level, one
+// CTA per terminal node (bwdTerminalK) beside the node-based interior
+// tasks (bwdInteriorK), the arithmetic of the walks.
 void Engine::buildPlans() {
   Dev& d = *d_;
   auto listBytes = [&](const std::vector<int>& v, int tr, bool fwd) {
@@ -262,57 +264,55 @@ void Engine::buildPlans() {
     }
     return b;
   };
-  for (int kind = 0; kind < 2; ++kind) {
-    std::vector<Launch>& P = d.plan[kind];
-    P.clear();
-    for (int tr = 0; tr < 2; ++tr) {
-      const int D = (int)d.fwd[tr].size();
-      for (int dd = 0; dd < D; ++dd) {
-        if (kind == 1) {
-          if (d.fwd[tr][dd].count)
-            P.push_back({kFwd, tr, d.fwd[tr][dd], listBytes(L_.fwdTasks[tr][dd], tr, true)});
-          continue;
-        }
-        std::vector<Launch> set;
-        if (d.fRec[tr][dd].count)
-          set.push_back({kFwdRec, tr, d.fRec[tr][dd],
-                         listBytes(kindOnly(L_.fwdTasks[tr][dd], kTaskDecide), tr, true)});
-        if (d.fCh[tr][dd].count)
-          set.push_back({kFwd, tr, d.fCh[tr][dd], listBytes(L_.fwdChance[tr][dd], tr, true)});
-        for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
-        P.insert(P.end(), set.begin(), set.end());
-      }
-      for (int dd = D - 1; dd >= 0; --dd) {
-        std::vector<Launch> set;
-        if (kind == 0) {
-          if (d.sdG[dd].count)
-            set.push_back({kSdGroup, tr, d.sdG[dd], groupBytes(L_.sdGroupTasks[dd], tr)});
-          if (d.fdG[dd].count)
-            set.push_back({kFdGroup, tr, d.fdG[dd], groupBytes(L_.fdGroupTasks[dd], tr)});
-          if (d.bCh[tr][dd].count)
-            set.push_back({kBwdInt, tr, d.bCh[tr][dd], listBytes(L_.bwdChance[tr][dd], tr, false)});
-          if (d.bRec[tr][dd].count)
-            set.push_back({kDecRec, tr, d.bRec[tr][dd],
-                           listBytes(kindOnly(L_.bwdTasks[tr][dd], kTaskDecide), tr, false)});
-          for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
-          P.insert(P.end(), set.begin(), set.end());
-          continue;
-        } else {
-          const std::vector<int>& v = L_.bwdTasks[tr][dd];
-          const int nt = terminalCount(v);
-          if (nt)
-            set.push_back({kBwdTerm, tr, ListRef{d.bwd[tr][dd].off, nt},
-                           listBytes(std::vector<int>(v.begin(), v.begin() + nt), tr, false)});
-        }
-        if (d.inner[tr][dd].count)
-          set.push_back({kBwdInt, tr, d.inner[tr][dd],
-                         listBytes(L_.innerTasks[tr][dd], tr, false)});
-        for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
-        P.insert(P.end(), set.begin(), set.end());
-      }
+  // Kind 0: the staged plan (decide records, chance words, terminal groups
+  // started right after the forward level that wrote their reach rows).
+  const int D = (int)d.fwd[0].size();
+  for (int tr = 0; tr < 2; ++tr) {
+    HalfStep& h = d.staged.half[tr];
+    h.fwd.assign(D, {});
+    h.bwd.assign(D, {});
+    h.sd.assign(D, Launch{kSdGroup, tr, ListRef{}, 0.0});
+    h.fd.assign(D, Launch{kFdGroup, tr, ListRef{}, 0.0});
+    for (int dd = 0; dd < D; ++dd) {
+      if (d.fRec[tr][dd].count)
+        h.fwd[dd].push_back({kFwdRec, tr, d.fRec[tr][dd],
+                             listBytes(kindOnly(L_.fwdTasks[tr][dd], kTaskDecide), tr, true)});
+      if (d.fCh[tr][dd].count)
+        h.fwd[dd].push_back({kFwd, tr, d.fCh[tr][dd], listBytes(L_.fwdChance[tr][dd], tr, true)});
+      if (d.sdG[dd].count)
+        h.sd[dd] = {kSdGroup, tr, d.sdG[dd], groupBytes(L_.sdGroupTasks[dd], tr)};
+      if (d.fdG[dd].count)
+        h.fd[dd] = {kFdGroup, tr, d.fdG[dd], groupBytes(L_.fdGroupTasks[dd], tr)};
+      if (d.bCh[tr][dd].count)
+        h.bwd[dd].push_back({kBwdInt, tr, d.bCh[tr][dd], listBytes(L_.bwdChance[tr][dd], tr, false)});
+      if (d.bRec[tr][dd].count)
+        h.bwd[dd].push_back({kDecRec, tr, d.bRec[tr][dd],
+                             listBytes(kindOnly(L_.bwdTasks[tr][dd], kTaskDecide), tr, false)});
     }
-    P.push_back({kCounter, 0, ListRef{}, 0.0});
   }
+  d.plan[0] = d.staged.flat();
+  d.sev.ensure(D);  // events exist before any capture
+  // Kind 1: per level, one CTA per terminal node beside the interior tasks.
+  std::vector<Launch>& P = d.plan[1];
+  P.clear();
+  for (int tr = 0; tr < 2; ++tr) {
+    for (int dd = 0; dd < D; ++dd)
+      if (d.fwd[tr][dd].count)
+        P.push_back({kFwd, tr, d.fwd[tr][dd], listBytes(L_.fwdTasks[tr][dd], tr, true)});
+    for (int dd = D - 1; dd >= 0; --dd) {
+      std::vector<Launch> set;
+      const std::vector<int>& v = L_.bwdTasks[tr][dd];
+      const int nt = terminalCount(v);
+      if (nt)
+        set.push_back({kBwdTerm, tr, ListRef{d.bwd[tr][dd].off, nt},
+                       listBytes(std::vector<int>(v.begin(), v.begin() + nt), tr, false)});
+      if (d.inner[tr][dd].count)
+        set.push_back({kBwdInt, tr, d.inner[tr][dd], listBytes(L_.innerTasks[tr][dd], tr, false)});
+      for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
+      P.insert(P.end(), set.begin(), set.end());
+    }
+  }
+  P.push_back({kCounter, 0, ListRef{}, 0.0});
 }
 
 void Engine::zeroRows() {
@@ -369,7 +369,9 @@ void Engine::capture() {
   const std::vector<Launch>& P = d.plan[engineKind_];
   GB_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t launchErr = cudaSuccess;
-  issuePlan(P, d.br, [&](const Launch& l, cudaStream_t s) { issue(d, l, s); });
+  auto one = [&](const Launch& l, cudaStream_t s) { issue(d, l, s); };
+  if (engineKind_ == 0) issueStaged(d.staged, d.br, d.sev, one);
+  else issuePlan(P, d.br, one);
   launchErr = cudaGetLastError();
   cudaGraph_t g = nullptr;
   const cudaError_t endErr = cudaStreamEndCapture(d.stream, &g);

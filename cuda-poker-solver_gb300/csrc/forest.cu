@@ -288,7 +288,9 @@ struct Forest::Dev {
   size_t tasksCap = 0;
   uint32_t* recTasks = nullptr;
   size_t recTasksCap = 0;
-  std::vector<Launch> plan;
+  std::vector<Launch> plan;  // the staged plan, flattened
+  StagedPlan staged;
+  StagedEvents sev;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool dirty = true;
@@ -450,6 +452,7 @@ Forest::~Forest() {
   cudaFree(d.info);
   cudaFree(d.vals);
   d.br.destroy();
+  d.sev.destroy();
   if (d.evA) cudaEventDestroy(d.evA);
   if (d.evB) cudaEventDestroy(d.evB);
   if (d.stream) cudaStreamDestroy(d.stream);
@@ -741,29 +744,25 @@ void Forest::iterate(int n) {
     if (!ls.recs.empty())
       GB_CK(cudaMemcpyAsync(d.recTasks, ls.recs.data(), ls.recs.size() * sizeof(uint32_t),
                             cudaMemcpyHostToDevice, d.stream));
-    d.plan.clear();
-    auto addSet = [&](std::vector<Launch>& set) {
-      for (size_t k = 0; k + 1 < set.size(); ++k) set[k].withNext = true;
-      d.plan.insert(d.plan.end(), set.begin(), set.end());
-    };
     for (int tr = 0; tr < 2; ++tr) {
       const int D = (int)ls.fRec[tr].size();
+      HalfStep& h = d.staged.half[tr];
+      h.fwd.assign(D, {});
+      h.bwd.assign(D, {});
+      h.sd.assign(D, Launch{kSdGroup, tr, ListRef{}, 0.0});
+      h.fd.assign(D, Launch{kFdGroup, tr, ListRef{}, 0.0});
       for (int dd = 0; dd < D; ++dd) {
-        std::vector<Launch> set;
-        if (ls.fRec[tr][dd].count) set.push_back({kFwdRec, tr, ls.fRec[tr][dd], 0.0});
-        if (ls.fCh[tr][dd].count) set.push_back({kFwd, tr, ls.fCh[tr][dd], 0.0});
-        addSet(set);
-      }
-      for (int dd = D - 1; dd >= 0; --dd) {
-        std::vector<Launch> set;
-        if (ls.sdG[dd].count) set.push_back({kSdGroup, tr, ls.sdG[dd], 0.0});
-        if (ls.fdG[dd].count) set.push_back({kFdGroup, tr, ls.fdG[dd], 0.0});
-        if (ls.bCh[tr][dd].count) set.push_back({kBwdInt, tr, ls.bCh[tr][dd], 0.0});
-        if (ls.bRec[tr][dd].count) set.push_back({kDecRec, tr, ls.bRec[tr][dd], 0.0});
-        addSet(set);
+        if (ls.fRec[tr][dd].count) h.fwd[dd].push_back({kFwdRec, tr, ls.fRec[tr][dd], 0.0});
+        if (ls.fCh[tr][dd].count) h.fwd[dd].push_back({kFwd, tr, ls.fCh[tr][dd], 0.0});
+        if (ls.sdG[dd].count) h.sd[dd] = {kSdGroup, tr, ls.sdG[dd], 0.0};
+        if (ls.fdG[dd].count) h.fd[dd] = {kFdGroup, tr, ls.fdG[dd], 0.0};
+        if (ls.bCh[tr][dd].count) h.bwd[dd].push_back({kBwdInt, tr, ls.bCh[tr][dd], 0.0});
+        if (ls.bRec[tr][dd].count) h.bwd[dd].push_back({kDecRec, tr, ls.bRec[tr][dd], 0.0});
       }
     }
-    d.plan.push_back({kCounter, 0, ListRef{}, 0.0});
+    d.staged.counter = Launch{kCounter, 0, ListRef{}, 0.0};
+    d.plan = d.staged.flat();
+    d.sev.ensure((int)std::max(d.staged.half[0].fwd.size(), d.staged.half[1].fwd.size()));
     const int maxN = d.maxN(all);
     const size_t smemSd = sdGroupSmem(maxN), smemFd = fdGroupSmem(maxN);
     raiseSmemLimit((const void*)sdGroupK, smemSd);
@@ -773,7 +772,8 @@ void Forest::iterate(int n) {
                         static_cast<const int4*>(d.arr[aGroups]), smemSd, smemFd,
                         static_cast<const uint32_t*>(d.arr[aRecs]), d.recTasks};
     GB_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
-    issuePlan(d.plan, d.br, [&](const Launch& l, cudaStream_t s) { issueLaunch(args, l, s); });
+    issueStaged(d.staged, d.br, d.sev,
+                [&](const Launch& l, cudaStream_t s) { issueLaunch(args, l, s); });
     const cudaError_t launchErr = cudaGetLastError();
     cudaGraph_t g = nullptr;
     const cudaError_t endErr = cudaStreamEndCapture(d.stream, &g);

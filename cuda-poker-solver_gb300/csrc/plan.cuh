@@ -160,6 +160,120 @@ void issuePlan(const std::vector<Launch>& P, const Branches& b, IssueOne&& one) 
   }
 }
 
+// The default iteration as a staged plan: per traverser half-step and
+// depth, the forward launches (run together), the showdown and fold group
+// launches, and the backward interior launches (run together). Terminal
+// values depend only on reach rows, so a depth's terminal groups start as
+// soon as the forward level that wrote their reach rows is done, on their
+// own streams, beside the rest of the forward pass; a backward level waits
+// only for the terminals one depth below it.
+struct HalfStep {
+  std::vector<std::vector<Launch>> fwd, bwd;  // per depth
+  std::vector<Launch> sd, fd;                 // per depth (count 0: none)
+};
+struct StagedPlan {
+  HalfStep half[2];
+  Launch counter{kCounter, 0, ListRef{}, 0.0};
+  // Every launch in an order that respects the dependencies (profile pass).
+  std::vector<Launch> flat() const {
+    std::vector<Launch> out;
+    for (const HalfStep& h : half) {
+      for (const auto& set : h.fwd) out.insert(out.end(), set.begin(), set.end());
+      for (size_t d = 0; d < h.sd.size(); ++d) {
+        if (h.sd[d].list.count) out.push_back(h.sd[d]);
+        if (h.fd[d].list.count) out.push_back(h.fd[d]);
+      }
+      for (size_t d = h.bwd.size(); d-- > 0;)
+        out.insert(out.end(), h.bwd[d].begin(), h.bwd[d].end());
+    }
+    out.push_back(counter);
+    for (Launch& l : out) l.withNext = false;
+    return out;
+  }
+};
+
+struct StagedEvents {
+  cudaEvent_t start = nullptr, lfork = nullptr, ljoin = nullptr;
+  std::vector<cudaEvent_t> fwd, sd, fd;
+  void ensure(int D) {
+    auto mk = [](cudaEvent_t& e) {
+      if (!e) GB_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    };
+    mk(start);
+    mk(lfork);
+    mk(ljoin);
+    for (auto* v : {&fwd, &sd, &fd}) {
+      while ((int)v->size() < D) v->push_back(nullptr);
+      for (auto& e : *v) mk(e);
+    }
+  }
+  void destroy() {
+    for (cudaEvent_t e : {start, lfork, ljoin})
+      if (e) cudaEventDestroy(e);
+    for (auto* v : {&fwd, &sd, &fd})
+      for (cudaEvent_t e : *v)
+        if (e) cudaEventDestroy(e);
+    start = lfork = ljoin = nullptr;
+    fwd.clear();
+    sd.clear();
+    fd.clear();
+  }
+};
+
+// Issues a staged plan: main stream b.main, level partner b.side[2],
+// showdown groups on b.side[0], fold groups on b.side[1].
+template <typename IssueOne>
+void issueStaged(const StagedPlan& P, const Branches& b, StagedEvents& ev, IssueOne&& one) {
+  auto issueSet = [&](const std::vector<Launch>& set) {
+    if (set.empty()) return;
+    if (set.size() == 1) {
+      one(set[0], b.main);
+      return;
+    }
+    GB_CK(cudaEventRecord(ev.lfork, b.main));
+    GB_CK(cudaStreamWaitEvent(b.side[2], ev.lfork, 0));
+    one(set[0], b.main);
+    for (size_t k = 1; k < set.size(); ++k) one(set[k], b.side[2]);
+    GB_CK(cudaEventRecord(ev.ljoin, b.side[2]));
+    GB_CK(cudaStreamWaitEvent(b.main, ev.ljoin, 0));
+  };
+  for (const HalfStep& h : P.half) {
+    const int D = (int)h.fwd.size();
+    ev.ensure(D);
+    GB_CK(cudaEventRecord(ev.start, b.main));
+    std::vector<char> sdOpen(D, 0), fdOpen(D, 0);
+    auto startTerminals = [&](int d) {  // depth d's reach rows are written
+      for (int k = 0; k < 2; ++k) {
+        const Launch& l = k == 0 ? h.sd[d] : h.fd[d];
+        if (!l.list.count) continue;
+        cudaStream_t s = b.side[k];
+        GB_CK(cudaStreamWaitEvent(s, d == 0 ? ev.start : ev.fwd[d - 1], 0));
+        one(l, s);
+        GB_CK(cudaEventRecord(k == 0 ? ev.sd[d] : ev.fd[d], s));
+        (k == 0 ? sdOpen : fdOpen)[d] = 1;
+      }
+    };
+    auto joinTerminals = [&](int d) {
+      if (d >= D) return;
+      if (sdOpen[d]) GB_CK(cudaStreamWaitEvent(b.main, ev.sd[d], 0));
+      if (fdOpen[d]) GB_CK(cudaStreamWaitEvent(b.main, ev.fd[d], 0));
+      sdOpen[d] = fdOpen[d] = 0;
+    };
+    startTerminals(0);
+    for (int d = 0; d < D; ++d) {
+      issueSet(h.fwd[d]);
+      GB_CK(cudaEventRecord(ev.fwd[d], b.main));
+      if (d + 1 < D) startTerminals(d + 1);
+    }
+    for (int d = D - 1; d >= 0; --d) {
+      joinTerminals(d + 1);
+      issueSet(h.bwd[d]);
+    }
+    joinTerminals(0);
+  }
+  one(P.counter, b.main);
+}
+
 // Splits a backward level list (sorted showdown, fold, chance, decide) into
 // its terminal head and interior tail.
 inline int terminalCount(const std::vector<int>& v) {

@@ -72,7 +72,7 @@ def test_rows_match_oracle(name, iters):
 
 @pytest.mark.parametrize("name", ["river_c1", "turn_api", "turn_c2_uniform"])
 def test_solution_matches_oracle(name):
-    """Gates (the benchmark spec): root EV within 0.01 chips, root strategy
+    """Solution gates: root EV within 0.01 chips, root strategy
     within 0.10 L-inf, exploitability ratio in [0.5, 2], against the FP64
     oracle run of the same iterations."""
     spot = wl.NAMED[name]()
