@@ -114,14 +114,18 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def committed_traffic(kernel):
-    """Per-launch DRAM bytes of the kernel from the committed ncu summary."""
+def committed_traffic(kernel, algo_bytes_per_launch):
+    """Per-launch DRAM bytes of the kernel class: the DRAM/algorithmic byte
+    ratio of one ncu-captured launch (profiles/traffic.json) scaled to this
+    run's average launch, or None without a capture of the class."""
     path = os.path.join(REPO, "profiles", "traffic.json")
     try:
-        d = json.load(open(path))
-        return d.get(kernel)
+        d = json.load(open(path)).get(kernel)
     except (OSError, ValueError):
-        return None
+        return None, None
+    if not isinstance(d, dict) or "dram_over_algorithmic" not in d:
+        return None, None
+    return d["dram_over_algorithmic"] * algo_bytes_per_launch, d.get("source")
 
 
 def cpu_baseline(spot, seconds=12.0):
@@ -348,9 +352,10 @@ def main():
     name, (launches, pms, pbytes) = max(prof.items(), key=lambda kv: kv[1][1])
     peak, peak_kind = measured_peaks()
     achieved = (pbytes / launches) / (pms / launches / 1000.0) / 1e9
-    traffic = committed_traffic(name)
+    traffic, traffic_src = committed_traffic(name, pbytes / launches)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "kernel": name,
+                "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                "kernel": name,
                 "algo_bytes_per_launch": pbytes / launches,
                 "avg_launch_us": 1000.0 * pms / launches, "peak_source": peak_kind,
                 "iteration_gbs": (sum(v[2] for v in prof.values()) / min(args.steps, 20)) *
