@@ -149,6 +149,23 @@ def cpu_baseline(spot, seconds=12.0):
                       % n}
 
 
+def max_over_ranks(x, dist, device="cpu"):
+    """The job's time is the slowest rank's (identity without a process
+    group)."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def shard(items, rank, world):
+    """Batched spots per rank: independent units, no exchange between
+    ranks (replicas of the batch engine, one per GPU)."""
+    return list(items)[rank::world]
+
+
 def _submit(batch, sp):
     from pps import pps_native as pn
     w = lambda r: pn.parse_range(r) if isinstance(r, str) else r
@@ -341,9 +358,7 @@ def main():
         ms = s.time_iterations(args.steps)
     torch.cuda.synchronize()
     if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dist, "cuda")
         dist.barrier()
     value = world * args.steps / (ms / 1000.0)
 
@@ -362,6 +377,19 @@ def main():
                                  (value / world) / 1e9,
                 "profile": {k: {"launches": v[0], "ms": v[1], "algo_bytes": v[2]}
                             for k, v in prof.items()}}
+    batched = None
+    if args.batch_spots > 0:
+        spots = wl.batched(args.batch_spots)
+        mine = shard(spots, rank, world)
+        if dist:
+            dist.barrier()
+        batched = batched_bench(mine, mine[:max(1, min(args.loop_sample, len(mine)))])
+        if dist:
+            slowest = max_over_ranks(batched["seconds"], dist, "cuda")
+            batched.update({"spots": len(spots), "ranks": world, "seconds": slowest,
+                            "solves_per_s": len(spots) / slowest,
+                            "speedup_vs_one_at_a_time": len(spots) / slowest /
+                            (world * batched["one_at_a_time"]["solves_per_s"])})
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -385,11 +413,9 @@ def main():
     line["w52"] = {"value": max(args.steps, 100) / (w52_ms / 1000.0), "unit": "iters/s",
                    "nodes": sw.num_nodes, "published_rtx4070": "747-807 iters/s"}
     del sw
-    if world == 1 and args.batch_spots > 0:
-        spots = wl.batched(args.batch_spots)
-        line["batched"] = batched_bench(spots, spots[:max(1, min(args.loop_sample,
-                                                                  len(spots)))])
-        if args.served_requests > 0:
+    if batched is not None:
+        line["batched"] = batched
+        if world == 1 and args.served_requests > 0:
             stream = wl.batched(1024, seed=505)
             line["served"] = {"distribution": "batched-distribution spots (seed 505, 1024 "
                                               "cycled); "

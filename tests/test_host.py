@@ -97,3 +97,37 @@ def test_bad_inputs_rejected_on_host():
         pn.Solver(board="Qs9h2d7c", oop="TT+", ip="99+", pot=100, stack=100, bets="")
     with pytest.raises(RuntimeError):
         pn.Solver(board="QsQs2d7c", oop="TT+", ip="99+", pot=100, stack=100)
+
+
+def test_batch_footprint_host_only():
+    """pps_gb_batch_footprint compiles on the host: footprints grow with
+    the tree and the 48,255-node C3 spot needs ~1.7 GB (f32 rows, FP64 walk
+    rows, tables, groups, records)."""
+    from pps import batch as pb
+    from pps import workloads as wl
+    from helpers import weights
+
+    def fp(sp):
+        return pb.footprint(sp.board_text(), weights(sp.oop), weights(sp.ip), sp.pot,
+                            sp.stack, sp.cfg.bet_text(), sp.cfg.raise_text() or [],
+                            sp.cfg.max_raises)
+    small, mid, big = fp(wl.river_c1()), fp(wl.turn_api()), fp(wl.turn_c3())
+    assert 0 < small < mid < big
+    assert 1.2e9 < big < 2.5e9
+
+
+def test_batched_distribution():
+    """The batched / served spot distribution: ~70% river / 30% turn,
+    all-combo U(0,1) ranges, pot in [50, 200), stack/pot in [1, 8], 2-4
+    distinct bet sizes from {25, 33, 50, 75, 100, 150}% plus all-in."""
+    from pps import workloads as wl
+    spots = wl.batched(256)
+    rivers = sum(len(s.board) == 5 for s in spots)
+    assert 150 <= rivers <= 210
+    for s in spots:
+        assert 50 <= s.pot < 200
+        assert 0.99 <= s.stack / s.pot <= 8.01
+        assert 2 <= len(s.cfg.bets) <= 4 and len(set(s.cfg.bets)) == len(s.cfg.bets)
+        assert set(s.cfg.bets) <= {0.25, 0.33, 0.5, 0.75, 1.0, 1.5} and s.cfg.allin
+        assert len(s.oop) == 1326 and 0.0 <= min(s.oop) and max(s.oop) < 1.0
+    assert [s.board for s in wl.batched(8)] == [s.board for s in spots[:8]]  # seeded
