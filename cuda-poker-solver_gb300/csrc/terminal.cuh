@@ -64,11 +64,11 @@ __host__ __device__ inline int groupPrefixEntries(int maxN) { return maxN + kSpa
 __host__ __device__ inline int groupXEntries(int maxN) { return 2 * maxN + 52; }
 constexpr int kGroupBlocks = kTermThreads / 32 + 1;  // warp blocks + the total
 
-// Showdown groups: tab | rs4 | P4 | X4 | W4 | WH | WL.
+// Showdown groups: tab | P4 | X4 | W4 | WH | WL. The P4 region first holds
+// the staged (transposed, unsorted) reach rows, then the sorted prefixes.
 __host__ __device__ inline size_t sdGroupSmem(int maxN) {
   return (size_t)groupTabEntries(maxN) * 2 +
-         16 * ((size_t)4 * ((maxN + 3) / 4) + groupPrefixEntries(maxN) + groupXEntries(maxN) +
-               3 * kGroupBlocks);
+         16 * ((size_t)groupPrefixEntries(maxN) + groupXEntries(maxN) + 3 * kGroupBlocks);
 }
 // Fold groups: tab | rs4 | cs4[53] | warp partials[8].
 __host__ __device__ inline size_t fdGroupSmem(int maxN) {
@@ -116,8 +116,8 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   const int opp = 1 - tr;
   const int no = st.n[opp], nt = st.n[tr];
   uint16_t* tab = reinterpret_cast<uint16_t*>(smem);
-  float4* rs4 = reinterpret_cast<float4*>(smem + (size_t)groupTabEntries(maxN) * 2);
-  float4* P4 = rs4 + 4 * ((maxN + 3) / 4);
+  float4* P4 = reinterpret_cast<float4*>(smem + (size_t)groupTabEntries(maxN) * 2);
+  float4* rs4 = P4;  // staged rows until the prefixes replace them
   float4* X4 = P4 + groupPrefixEntries(maxN);
   float4* W4 = X4 + groupXEntries(maxN);
   float* BH = reinterpret_cast<float*>(W4 + kGroupBlocks);  // [warp block][4]
@@ -131,39 +131,6 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   stageRows4(rs4, t, rows, u, tr, no);
   __syncthreads();
 
-  // Exclusive prefixes of the strength-sorted reach in one pass: thread t
-  // takes positions [8t, 8t + 8); lane totals are scanned within the warp
-  // (uncompensated within a warp's 256 positions) and the warp totals go
-  // to W4 for the compensated pass below. Warps past the list end skip it.
-  const int nbw = (no >> kSpanShift) + 1;  // warp blocks covering 0..no
-  if (warp < nbw) {
-    const int k0 = threadIdx.x * kSpan;
-    float4 v[kSpan];
-    const bool any = k0 <= no;
-    const uint4 o8 = any && k0 < no ? *reinterpret_cast<const uint4*>(ord + k0) : make_uint4(0, 0, 0, 0);
-    const uint16_t* o = reinterpret_cast<const uint16_t*>(&o8);
-#pragma unroll
-    for (int j = 0; j < kSpan; ++j) v[j] = k0 + j < no ? rs4[o[j]] : zero4();
-    float4 pre[kSpan];
-    float4 run = zero4();
-#pragma unroll
-    for (int j = 0; j < kSpan; ++j) {
-      pre[j] = run;
-      run += v[j];
-    }
-    float4 incl = run;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const float4 x = shflUp4(incl, off);
-      if (lane >= off) incl += x;
-    }
-    float4 ex = shflUp4(incl, 1);
-    if (lane == 0) ex = zero4();
-    if (any)
-#pragma unroll
-      for (int j = 0; j < kSpan; ++j) P4[k0 + j] = ex + pre[j];
-    if (lane == 31) W4[warp] = incl;
-  }
   // Card segments, four cards per warp (8 lanes x 8 entries per card):
   // X4[seg[c] + c + k] = reach of the card's first k entries, k = 0..len.
   for (int cb = warp * 4; cb < 52; cb += nw * 4) {
@@ -192,7 +159,41 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
       if (e <= len) xo[e] = base + pre[j];
     }
   }
+  // Exclusive prefixes of the strength-sorted reach in one pass: thread t
+  // takes positions [8t, 8t + 8); lane totals are scanned within the warp
+  // (uncompensated within a warp's 256 positions) and the warp totals go
+  // to W4 for the compensated pass below. The prefixes stay in registers
+  // until every thread has read the staged rows they replace.
+  const int nbw = (no >> kSpanShift) + 1;  // warp blocks covering 0..no
+  const int k0 = threadIdx.x * kSpan;
+  const bool mine = warp < nbw && k0 <= no;
+  float4 pre[kSpan], ex = zero4();
+  if (warp < nbw) {
+    float4 v[kSpan];
+    const uint4 o8 = mine && k0 < no ? *reinterpret_cast<const uint4*>(ord + k0) : make_uint4(0, 0, 0, 0);
+    const uint16_t* o = reinterpret_cast<const uint16_t*>(&o8);
+#pragma unroll
+    for (int j = 0; j < kSpan; ++j) v[j] = k0 + j < no ? rs4[o[j]] : zero4();
+    float4 run = zero4();
+#pragma unroll
+    for (int j = 0; j < kSpan; ++j) {
+      pre[j] = run;
+      run += v[j];
+    }
+    float4 incl = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const float4 x = shflUp4(incl, off);
+      if (lane >= off) incl += x;
+    }
+    ex = shflUp4(incl, 1);
+    if (lane == 0) ex = zero4();
+    if (lane == 31) W4[warp] = incl;
+  }
   __syncthreads();
+  if (mine)
+#pragma unroll
+    for (int j = 0; j < kSpan; ++j) P4[k0 + j] = ex + pre[j];
   // Compensated exclusive prefix of the warp-block totals, one thread per
   // node.
   if (threadIdx.x < 4) {
@@ -228,6 +229,10 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   const float4 TH = BH4[bn], TL = BL4[bn], Pno = P4[no];
   float* out[4];
   outRows4(out, t, rows, u);
+  const float* rr[4];
+#pragma unroll
+  for (int g = 0; g < 4; ++g)
+    rr[g] = u[g] >= 0 ? rows.reach[tr] + (size_t)t.rows[u[g]].reachQ[tr] * 4 : nullptr;
   const int nt4 = quadsOf(nt) * 4;
 #pragma unroll 2
   for (int i = threadIdx.x; i < nt4; i += blockDim.x) {
@@ -243,7 +248,10 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
     const float4 x2le = X4[a2 + (f.z & 0xff)], x2te = X4[a2 + ((f.z >> 8) & 0xff)];
     const float4 x1end = X4[a1 + len1], x2end = X4[a2 + len2];
     const int same = (int)(f.z >> 16) - 1;
-    const float4 sameR = same >= 0 ? rs4[same] : zero4();
+    float4 sameR = zero4();
+    if (same >= 0)  // the identical combo's reach, from the (cached) rows
+      sameR = make_float4(rr[0] ? rr[0][same] : 0.f, rr[1] ? rr[1][same] : 0.f,
+                          rr[2] ? rr[2][same] : 0.f, rr[3] ? rr[3][same] : 0.f);
     const int bl = le >> kSpanShift, bt = te >> kSpanShift;
     const float4 bhl = BH4[bl], bll = BL4[bl], bht = BH4[bt], blt = BL4[bt];
     const float4 ple = P4[le], pte = P4[te];
@@ -335,7 +343,7 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
 // kernel per kind (the showdown tables need 4x the shared memory and more
 // registers; folds fit more CTAs per SM). Internal linkage: this header is
 // included by more than one translation unit, each keeping its own copy.
-static __global__ void __launch_bounds__(kTermThreads, 2)
+static __global__ void __launch_bounds__(kTermThreads, 3)
 sdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
          const int* __restrict__ tasks, int count, int tr, int maxN) {
   extern __shared__ __align__(16) unsigned char smem[];
