@@ -78,6 +78,12 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
   const float pos = c3[0], neg = c3[1], avg = c3[2];
   const float uniform = 1.f / (float)na;
   float val[4] = {0.f, 0.f, 0.f, 0.f}, acc[4] = {0.f, 0.f, 0.f, 0.f};
+  // The children's value rows and the strategy rows are needed only after
+  // the regret pass: start fetching them into L2 now (a hint, no data).
+  for (int a = 0; a < na; ++a) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(str + ((size_t)a * nq + q) * 4));
+  }
   // Streaming form: a row is reloaded (a cache hit) instead of held in
   // registers, which keeps the kernel at 40 registers and 48 warps per SM;
   // the launches are bound by memory latency, not by instruction count.
