@@ -156,5 +156,57 @@ fwdDecideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
     fwdDecideRecord(t, rows, tr, loadRec(recs, tasks[i]));
 }
 
+// ---------------------------------------------------------------------------
+// Level kernels of the default iteration: one launch per level and pass
+// covering the level's decide records and chance tasks (CTA i < nRec: a
+// record; else a chance task word), launched with programmatic dependent
+// launch so consecutive levels overlap: each CTA lets the next level's grid
+// start (launch_dependents), loads its record (static data), then waits
+// until the previous level's grid has finished and its writes are visible
+// (griddepcontrol.wait) before touching rows. Without a programmatic
+// dependency the wait returns at once.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void pdlTrigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+static __global__ void __launch_bounds__(kThreads, 12)
+fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
+             const uint32_t* __restrict__ recTasks, int nRec, const int* __restrict__ chance,
+             int nCh, int tr) {
+  pdlTrigger();
+  for (int i = blockIdx.x; i < nRec + nCh; i += gridDim.x) {
+    if (i < nRec) {
+      const DecRec r = loadRec(recs, recTasks[i]);
+      pdlWait();
+      fwdDecideRecord(t, rows, tr, r);
+    } else {
+      const int w = chance[i - nRec];
+      pdlWait();
+      fwdChanceBranch<float>(t, rows, (int)((unsigned)w >> 8), (w >> 2) & 63, tr);
+    }
+  }
+}
+
+static __global__ void __launch_bounds__(kThreads, 12)
+bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
+             const uint32_t* __restrict__ recTasks, int nRec, const int* __restrict__ chance,
+             int nCh, int tr) {
+  __shared__ __align__(16) unsigned char smem[kChanceScratchBytes];
+  pdlTrigger();
+  for (int i = blockIdx.x; i < nRec + nCh; i += gridDim.x) {
+    if (i < nRec) {
+      const DecRec r = loadRec(recs, recTasks[i]);
+      pdlWait();
+      decideRecord(t, rows, r);
+    } else {
+      const int w = chance[i - nRec];
+      pdlWait();
+      chanceChunk<float>(t, rows, (int)((unsigned)w >> 8), (w >> 2) & 63, tr, smem);
+      __syncthreads();  // the next chance task reuses the pointer tables
+    }
+  }
+}
+
 }  // namespace gb
 }  // namespace pps

@@ -274,20 +274,24 @@ void Engine::buildPlans() {
     h.sd.assign(D, Launch{kSdGroup, tr, ListRef{}, 0.0});
     h.fd.assign(D, Launch{kFdGroup, tr, ListRef{}, 0.0});
     for (int dd = 0; dd < D; ++dd) {
-      if (d.fRec[tr][dd].count)
-        h.fwd[dd].push_back({kFwdRec, tr, d.fRec[tr][dd],
-                             listBytes(kindOnly(L_.fwdTasks[tr][dd], kTaskDecide), tr, true)});
-      if (d.fCh[tr][dd].count)
-        h.fwd[dd].push_back({kFwd, tr, d.fCh[tr][dd], listBytes(L_.fwdChance[tr][dd], tr, true)});
+      if (d.fRec[tr][dd].count || d.fCh[tr][dd].count) {
+        Launch l{kFwdMix, tr, d.fRec[tr][dd],
+                 listBytes(kindOnly(L_.fwdTasks[tr][dd], kTaskDecide), tr, true) +
+                     listBytes(L_.fwdChance[tr][dd], tr, true)};
+        l.list2 = d.fCh[tr][dd];
+        h.fwd[dd].push_back(l);
+      }
       if (d.sdG[dd].count)
         h.sd[dd] = {kSdGroup, tr, d.sdG[dd], groupBytes(L_.sdGroupTasks[dd], tr)};
       if (d.fdG[dd].count)
         h.fd[dd] = {kFdGroup, tr, d.fdG[dd], groupBytes(L_.fdGroupTasks[dd], tr)};
-      if (d.bCh[tr][dd].count)
-        h.bwd[dd].push_back({kBwdInt, tr, d.bCh[tr][dd], listBytes(L_.bwdChance[tr][dd], tr, false)});
-      if (d.bRec[tr][dd].count)
-        h.bwd[dd].push_back({kDecRec, tr, d.bRec[tr][dd],
-                             listBytes(kindOnly(L_.bwdTasks[tr][dd], kTaskDecide), tr, false)});
+      if (d.bRec[tr][dd].count || d.bCh[tr][dd].count) {
+        Launch l{kBwdMix, tr, d.bRec[tr][dd],
+                 listBytes(kindOnly(L_.bwdTasks[tr][dd], kTaskDecide), tr, false) +
+                     listBytes(L_.bwdChance[tr][dd], tr, false)};
+        l.list2 = d.bCh[tr][dd];
+        h.bwd[dd].push_back(l);
+      }
     }
   }
   d.plan[0] = d.staged.flat();
@@ -424,6 +428,20 @@ std::vector<Engine::KernelStat> Engine::profile(int n, bool splitKinds) {
   static const char* kKindName[] = {"bwd_decide", "bwd_chance", "bwd_fold", "bwd_showdown"};
   std::vector<std::pair<Launch, std::string>> P;
   for (const Launch& l : d.plan[engineKind_]) {
+    if (splitKinds && (l.kind == kFwdMix || l.kind == kBwdMix)) {
+      // The level's records and chance tasks as two launches.
+      const bool fwd = l.kind == kFwdMix;
+      double chBytes = 0;
+      for (int j = l.list2.off; j < l.list2.off + l.list2.count; ++j)
+        chBytes += taskBytes(d.hostTasks[j], l.tr, fwd);
+      if (l.list.count)
+        P.push_back({Launch{fwd ? kFwdRec : kDecRec, l.tr, l.list, l.bytes - chBytes},
+                     fwd ? "fwd_decide" : "bwd_decide"});
+      if (l.list2.count)
+        P.push_back({Launch{fwd ? kFwd : kBwdInt, l.tr, l.list2, chBytes},
+                     fwd ? "fwd_chance" : "bwd_chance"});
+      continue;
+    }
     const bool bwd = l.kind == kBwd || l.kind == kBwdTerm || l.kind == kBwdInt;
     if (!bwd || !splitKinds) {
       P.push_back({l, launchName(l.kind)});

@@ -752,12 +752,18 @@ void Forest::iterate(int n) {
       h.sd.assign(D, Launch{kSdGroup, tr, ListRef{}, 0.0});
       h.fd.assign(D, Launch{kFdGroup, tr, ListRef{}, 0.0});
       for (int dd = 0; dd < D; ++dd) {
-        if (ls.fRec[tr][dd].count) h.fwd[dd].push_back({kFwdRec, tr, ls.fRec[tr][dd], 0.0});
-        if (ls.fCh[tr][dd].count) h.fwd[dd].push_back({kFwd, tr, ls.fCh[tr][dd], 0.0});
+        if (ls.fRec[tr][dd].count || ls.fCh[tr][dd].count) {
+          Launch l{kFwdMix, tr, ls.fRec[tr][dd], 0.0};
+          l.list2 = ls.fCh[tr][dd];
+          h.fwd[dd].push_back(l);
+        }
         if (ls.sdG[dd].count) h.sd[dd] = {kSdGroup, tr, ls.sdG[dd], 0.0};
         if (ls.fdG[dd].count) h.fd[dd] = {kFdGroup, tr, ls.fdG[dd], 0.0};
-        if (ls.bCh[tr][dd].count) h.bwd[dd].push_back({kBwdInt, tr, ls.bCh[tr][dd], 0.0});
-        if (ls.bRec[tr][dd].count) h.bwd[dd].push_back({kDecRec, tr, ls.bRec[tr][dd], 0.0});
+        if (ls.bRec[tr][dd].count || ls.bCh[tr][dd].count) {
+          Launch l{kBwdMix, tr, ls.bRec[tr][dd], 0.0};
+          l.list2 = ls.bCh[tr][dd];
+          h.bwd[dd].push_back(l);
+        }
       }
     }
     d.staged.counter = Launch{kCounter, 0, ListRef{}, 0.0};

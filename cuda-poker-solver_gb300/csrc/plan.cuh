@@ -34,11 +34,11 @@ struct ListRef {
 };
 
 enum LaunchKind { kFwd, kBwd, kBwdTerm, kBwdInt, kSdGroup, kFdGroup, kDecRec, kFwdRec,
-                  kCounter };
+                  kFwdMix, kBwdMix, kCounter };
 inline const char* launchName(LaunchKind k) {
   static const char* names[] = {"fwd_level",    "bwd_level", "bwd_terminal", "bwd_interior",
                                 "bwd_showdown", "bwd_fold",  "bwd_decide",   "fwd_decide",
-                                "counter"};
+                                "fwd_level",    "bwd_interior", "counter"};
   return names[k];
 }
 
@@ -48,6 +48,7 @@ struct Launch {
   ListRef list;
   double bytes;           // algorithmic bytes of this launch (f32 rows)
   bool withNext = false;  // independent of the next launch: run both at once
+  ListRef list2{};        // kFwdMix / kBwdMix: the chance words (list: records)
 };
 
 // What the level launches of a plan read: the tree, the f32 rows, the
@@ -106,6 +107,31 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       fwdDecideRecK<<<g, kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
                                            l.list.count, l.tr);
       break;
+    case kFwdMix:
+    case kBwdMix: {
+      // Programmatic dependent launch: the grid may start while the
+      // previous kernel in the stream drains (the kernels wait for it
+      // before touching rows).
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(gridOf(l.list.count + l.list2.count));
+      cfg.blockDim = dim3(kThreads);
+      cfg.dynamicSmemBytes = 0;
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      attr[0].val.programmaticStreamSerializationAllowed = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      const uint32_t* rt = a.recTasks + l.list.off;
+      const int* ch = a.tasks + l.list2.off;
+      if (l.kind == kFwdMix)
+        GB_CK(cudaLaunchKernelEx(&cfg, fwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
+                                 ch, l.list2.count, l.tr));
+      else
+        GB_CK(cudaLaunchKernelEx(&cfg, bwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
+                                 ch, l.list2.count, l.tr));
+      break;
+    }
     case kCounter:
       advanceCounterK<<<(a.spots + 255) / 256, 256, 0, s>>>(a.counter, a.spots);
       break;
