@@ -413,6 +413,21 @@ def main():
     line["w52"] = {"value": max(args.steps, 100) / (w52_ms / 1000.0), "unit": "iters/s",
                    "nodes": sw.num_nodes, "published_rtx4070": "747-807 iters/s"}
     del sw
+    # The reference's flop bench spots (docs/STATUS.md:75-84).
+    line["flop"] = {}
+    for fname, pub in (("flop_164k", "~201 iters/s"), ("flop_615k", "~55 iters/s")):
+        fs = wl.NAMED[fname]()
+        t0 = time.perf_counter()
+        sf = pps.Solver(board=fs.board_text(), oop=fs.oop, ip=fs.ip, pot=fs.pot, stack=fs.stack,
+                        bets=fs.cfg.bet_text(), raises=fs.cfg.raise_text(),
+                        max_raises=fs.cfg.max_raises)
+        compile_s = time.perf_counter() - t0
+        sf.time_iterations(args.warmup)
+        fms = sf.time_iterations(100)
+        line["flop"][fname] = {"value": 100 / (fms / 1000.0), "unit": "iters/s",
+                               "nodes": sf.num_nodes, "compile_upload_s": compile_s,
+                               "published_rtx4070": pub}
+        del sf
     if batched is not None:
         line["batched"] = batched
         if world == 1 and args.served_requests > 0:

@@ -20,6 +20,9 @@ Named spots (pot/stack in chips, bets as pot fractions, "a" = all-in):
   bench_turn.sh:40-41): Qs9h2d7c, 300/1500, bets {0.25,0.5,0.75,1.25},
   raises {2.5,3.0}, ranges "22+,A9s+,KTs+,QJs,JTs,T9s" vs the same plus
   "AQo+" (51,903 nodes).
+* ``flop_164k`` / ``flop_615k``  the reference's flop bench spots
+  (docs/STATUS.md:75-84): Qs9h2d, bets {0.75, a}, raises {2.5, 3}, the
+  wide ranges; pot/stack 200/500 (164,416 nodes) and 300/1500 (615,234).
 * ``turn_api``   the reference's API test spot (python/test_pps.py:18-24).
 * ``turn_tiny``  the reference's known-answer spot (tools/tiny_check.cpp:
   75-79, driven by tools/quality/gpu_postflop_parity.sh:139).
@@ -161,6 +164,23 @@ def turn_w52() -> Spot:
                 BetCfg([0.25, 0.5, 0.75, 1.25], [2.5, 3.0]), iterations=2000)
 
 
+def flop_164k() -> Spot:
+    """The reference's practical flop abstraction (docs/STATUS.md:81-84):
+    Qs9h2d, pot 200, stack 500, bets {0.75, a}, raises {2.5, 3}, the wide
+    bench ranges (164,416 nodes; ~201 it/s on the reference's RTX 4070)."""
+    return Spot("flop_164k", board_ids("Qs9h2d"), "22+,A9s+,KTs+,QJs,JTs,T9s",
+                "22+,A9s+,KTs+,QJs,JTs,T9s,AQo+", 200, 500,
+                BetCfg([0.75], [2.5, 3.0], allin=True), iterations=200)
+
+
+def flop_615k() -> Spot:
+    """The same abstraction at pot 300, stack 1500 (615,234 nodes; the
+    reference's "flop standard", ~55 it/s, docs/STATUS.md:75)."""
+    return Spot("flop_615k", board_ids("Qs9h2d"), "22+,A9s+,KTs+,QJs,JTs,T9s",
+                "22+,A9s+,KTs+,QJs,JTs,T9s,AQo+", 300, 1500,
+                BetCfg([0.75], [2.5, 3.0], allin=True), iterations=200)
+
+
 def turn_api() -> Spot:
     return Spot("turn_api", board_ids("Qs9h2d7c"), "TT+,AKo", "AQ+,KQs", 200,
                 500, BetCfg([0.75], [2.5, 3.0], allin=True), iterations=300)
@@ -230,6 +250,8 @@ NAMED = {
     "turn_c2_uniform": lambda: turn_c2(uniform_config=True),
     "turn_c3": turn_c3,
     "turn_w52": turn_w52,
+    "flop_164k": flop_164k,
+    "flop_615k": flop_615k,
     "turn_api": turn_api,
     "turn_tiny": turn_tiny,
     "turn_short": turn_short,

@@ -156,3 +156,18 @@ def test_full_size_turn_c3_properties():
     assert np.all(np.isfinite(rows)) and np.all(rows >= 0)
     f = s.strategy(3)["freqs"]
     np.testing.assert_allclose(f.sum(axis=0), 1.0, atol=1e-9)
+
+
+def test_flop_164k_rows_match_oracle():
+    """The reference's 164,416-node flop bench spot (two chance streets):
+    rows after one iteration against the FP64 oracle (normwise 5e-5)."""
+    spot = wl.flop_164k()
+    s = solver(spot)
+    assert s.num_nodes == 164416
+    s.solve(1)
+    o64 = oracle(spot, precision=64)
+    o64.iterate(1)
+    for which in (0, 1):
+        g, r = s.read_rows(which), o64.rows(which)
+        scale = max(float(np.max(np.abs(r))), 1e-30)
+        assert float(np.max(np.abs(g.astype(np.float64) - r))) / scale <= 5e-5
