@@ -268,6 +268,7 @@ bool BatchServer::epoch() {
 
   const std::vector<double> ev0 = F.walkValues(done, 0, kModeEV);
   const std::vector<double> ev1 = F.walkValues(done, 1, kModeEV);
+  std::vector<std::vector<float>> rootRows = F.rootRows(done);
   for (size_t i = 0; i < done.size(); ++i) {
     const int slot = done[i];
     BatchResult res;
@@ -288,7 +289,7 @@ bool BatchServer::epoch() {
     res.pairMass = (int64_t)(cs.pairMass * (double)(1LL << 20));
     const Node& root = t.nodes[0];
     if (root.kind == kDecide) {
-      res.rootRows = F.rootRows(slot);
+      res.rootRows = std::move(rootRows[i]);
       res.rootCombos = t.n(0, root.player);
       res.rootFreqs = aggregate(res.rootRows, root.na, res.rootCombos, t.side[root.player].w);
       res.rootActions.assign(t.actions.begin() + root.actBase,
@@ -304,8 +305,10 @@ bool BatchServer::epoch() {
     }
     finish(ticket, std::move(res));
   }
+  F.trim();
   std::lock_guard<std::mutex> lock(m_);
   stats_.retireMs += nowMs() - tChecked;
+  stats_.deviceBytes = (int64_t)F.deviceBytes();
   return true;
 }
 

@@ -651,9 +651,6 @@ std::unique_ptr<CompiledSpot> Forest::retire(int slot) {
   d.live.erase(it);
   d.freeSlots.push_back(slot);
   d.dirty = true;
-  // Give back memory above the pools' new tops (nothing may still run).
-  GB_CK(cudaStreamSynchronize(d.stream));
-  for (int a = 0; a < kArrays; ++a) d.trim(a);
   return s;
 }
 
@@ -862,22 +859,41 @@ std::vector<double> Forest::walkValues(const std::vector<int>& slots, int tr, in
   return out;
 }
 
-std::vector<float> Forest::rootRows(int slot) {
+std::vector<std::vector<float>> Forest::rootRows(const std::vector<int>& slots) {
   Dev& d = *d_;
-  const SlotRec& r = d.live.at(slot);
-  const Tree& t = r.spot->tree;
-  const Node& root = t.nodes[0];
-  if (root.kind != kDecide) return {};
-  const int n = t.n(0, root.player);
-  const size_t stride = quads(n) * 4;
-  std::vector<float> padded(stride * root.na), out((size_t)n * root.na);
-  GB_CK(cudaMemcpyAsync(padded.data(), d.at<float>(aStr, r.rootRegQ),
-                        padded.size() * sizeof(float), cudaMemcpyDeviceToHost, d.stream));
+  // One host staging buffer, every copy queued, one wait.
+  std::vector<size_t> at(slots.size() + 1, 0);
+  for (size_t k = 0; k < slots.size(); ++k) {
+    const Tree& t = d.live.at(slots[k]).spot->tree;
+    const Node& root = t.nodes[0];
+    at[k + 1] = at[k] + (root.kind == kDecide ? quads(t.n(0, root.player)) * 4 * root.na : 0);
+  }
+  std::vector<float> staged(std::max<size_t>(at.back(), 1));
+  for (size_t k = 0; k < slots.size(); ++k)
+    if (at[k + 1] > at[k])
+      GB_CK(cudaMemcpyAsync(staged.data() + at[k], d.at<float>(aStr, d.live.at(slots[k]).rootRegQ),
+                            (at[k + 1] - at[k]) * sizeof(float), cudaMemcpyDeviceToHost,
+                            d.stream));
   GB_CK(cudaStreamSynchronize(d.stream));
-  for (int a = 0; a < root.na; ++a)
-    std::copy(padded.begin() + a * stride, padded.begin() + a * stride + n,
-              out.begin() + (size_t)a * n);
+  std::vector<std::vector<float>> out(slots.size());
+  for (size_t k = 0; k < slots.size(); ++k) {
+    if (at[k + 1] == at[k]) continue;
+    const Tree& t = d.live.at(slots[k]).spot->tree;
+    const Node& root = t.nodes[0];
+    const int n = t.n(0, root.player);
+    const size_t stride = quads(n) * 4;
+    out[k].resize((size_t)n * root.na);
+    for (int a = 0; a < root.na; ++a)
+      std::copy(staged.begin() + at[k] + a * stride, staged.begin() + at[k] + a * stride + n,
+                out[k].begin() + (size_t)a * n);
+  }
   return out;
+}
+
+void Forest::trim() {
+  Dev& d = *d_;
+  GB_CK(cudaStreamSynchronize(d.stream));
+  for (int a = 0; a < kArrays; ++a) d.trim(a);
 }
 
 void Forest::sync() { GB_CK(cudaStreamSynchronize(d_->stream)); }

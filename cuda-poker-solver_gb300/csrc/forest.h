@@ -50,8 +50,10 @@ class Forest {
   // taking ownership; returns -1 (spot untouched) when the forest's device
   // bytes would exceed `budget`.
   int admit(std::unique_ptr<CompiledSpot>& s, size_t budget);
-  // Frees the spot's ranges and returns it.
+  // Frees the spot's ranges and returns it (trim() gives the memory back).
   std::unique_ptr<CompiledSpot> retire(int slot);
+  // Unmaps pool memory above the pools' tops (waits for queued work).
+  void trim();
   std::vector<int> slots() const;  // resident slots, ascending
   const CompiledSpot& spot(int slot) const;
   int iterations(int slot) const;
@@ -64,8 +66,9 @@ class Forest {
   // One FP64 walk (kModeEV or kModeBR) of traverser tr over `slots`;
   // returns each spot's root value divided by its pair mass (chips).
   std::vector<double> walkValues(const std::vector<int>& slots, int tr, int mode);
-  // Average-strategy rows of a spot's root decide node (na x n, dense).
-  std::vector<float> rootRows(int slot);
+  // Cumulative strategy rows of each spot's root decide node (na x n,
+  // dense; empty where the root is not a decision), copied in one batch.
+  std::vector<std::vector<float>> rootRows(const std::vector<int>& slots);
   void sync();
 
   size_t deviceBytes() const;  // pool capacity
