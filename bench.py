@@ -415,16 +415,17 @@ def main():
     del sw
     # The reference's flop bench spots (docs/STATUS.md:75-84).
     line["flop"] = {}
-    for fname, pub in (("flop_164k", "~201 iters/s"), ("flop_615k", "~55 iters/s")):
+    for fname, pub, iters in (("flop_164k", "~201 iters/s", 100), ("flop_615k", "~55 iters/s", 100),
+                              ("flop_wide", "~0.57 iters/s", 10)):
         fs = wl.NAMED[fname]()
         t0 = time.perf_counter()
         sf = pps.Solver(board=fs.board_text(), oop=fs.oop, ip=fs.ip, pot=fs.pot, stack=fs.stack,
                         bets=fs.cfg.bet_text(), raises=fs.cfg.raise_text(),
                         max_raises=fs.cfg.max_raises)
         compile_s = time.perf_counter() - t0
-        sf.time_iterations(args.warmup)
-        fms = sf.time_iterations(100)
-        line["flop"][fname] = {"value": 100 / (fms / 1000.0), "unit": "iters/s",
+        sf.time_iterations(min(args.warmup, 3))
+        fms = sf.time_iterations(iters)
+        line["flop"][fname] = {"value": iters / (fms / 1000.0), "unit": "iters/s",
                                "nodes": sf.num_nodes, "compile_upload_s": compile_s,
                                "published_rtx4070": pub}
         del sf

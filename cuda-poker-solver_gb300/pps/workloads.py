@@ -23,6 +23,8 @@ Named spots (pot/stack in chips, bets as pot fractions, "a" = all-in):
 * ``flop_164k`` / ``flop_615k``  the reference's flop bench spots
   (docs/STATUS.md:75-84): Qs9h2d, bets {0.75, a}, raises {2.5, 3}, the
   wide ranges; pot/stack 200/500 (164,416 nodes) and 300/1500 (615,234).
+* ``flop_wide``  the reference's 11,716,550-node flop (docs/STATUS.md:76):
+  Qs9h2d, 300/1500, bets {0.25, 0.5, 0.75, 1.25}, raises {2.5, 3}.
 * ``turn_api``   the reference's API test spot (python/test_pps.py:18-24).
 * ``turn_tiny``  the reference's known-answer spot (tools/tiny_check.cpp:
   75-79, driven by tools/quality/gpu_postflop_parity.sh:139).
@@ -181,6 +183,15 @@ def flop_615k() -> Spot:
                 BetCfg([0.75], [2.5, 3.0], allin=True), iterations=200)
 
 
+def flop_wide() -> Spot:
+    """The reference's "flop wide" spot (docs/STATUS.md:76): Qs9h2d,
+    300/1500, bets {0.25, 0.5, 0.75, 1.25}, raises {2.5, 3}, the wide
+    ranges (11,716,550 nodes; ~0.57 it/s on the reference's RTX 4070)."""
+    return Spot("flop_wide", board_ids("Qs9h2d"), "22+,A9s+,KTs+,QJs,JTs,T9s",
+                "22+,A9s+,KTs+,QJs,JTs,T9s,AQo+", 300, 1500,
+                BetCfg([0.25, 0.5, 0.75, 1.25], [2.5, 3.0]), iterations=100)
+
+
 def turn_api() -> Spot:
     return Spot("turn_api", board_ids("Qs9h2d7c"), "TT+,AKo", "AQ+,KQs", 200,
                 500, BetCfg([0.75], [2.5, 3.0], allin=True), iterations=300)
@@ -252,6 +263,7 @@ NAMED = {
     "turn_w52": turn_w52,
     "flop_164k": flop_164k,
     "flop_615k": flop_615k,
+    "flop_wide": flop_wide,
     "turn_api": turn_api,
     "turn_tiny": turn_tiny,
     "turn_short": turn_short,
