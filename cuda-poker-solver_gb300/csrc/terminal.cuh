@@ -14,7 +14,8 @@
 //     opponents holding either card (per-card segment prefixes X read at
 //     precomputed counts), plus the identical combo once in the tie band;
 //   fold: (total - card sums of both cards + identical combo) x payoff,
-//     card sums in a fixed order (no atomics).
+//     card sums in a fixed order (no atomics); the total is half the sum
+//     of the 52 card sums (each combo holds two cards).
 #pragma once
 
 #include "kernels.cuh"
@@ -70,9 +71,10 @@ __host__ __device__ inline size_t sdGroupSmem(int maxN) {
   return (size_t)groupTabEntries(maxN) * 2 +
          16 * ((size_t)groupPrefixEntries(maxN) + groupXEntries(maxN) + 3 * kGroupBlocks);
 }
-// Fold groups: tab | rs4 | cs4[53] | warp partials[8].
+// Fold groups: tab | rs4 | cs4[53] | card pairs (u16) | identical-combo slots (i16).
 __host__ __device__ inline size_t fdGroupSmem(int maxN) {
-  return (size_t)groupTabEntries(maxN) * 2 + 16 * ((size_t)4 * ((maxN + 3) / 4) + 53 + 8);
+  return (size_t)groupTabEntries(maxN) * 2 + 16 * ((size_t)4 * ((maxN + 3) / 4) + 53) +
+         (size_t)4 * ((maxN + 7) / 8 * 8);
 }
 
 // Stages the group's opponent reach rows transposed: rs4[j] holds entry j
@@ -278,11 +280,20 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
   uint16_t* csr = reinterpret_cast<uint16_t*>(smem);
   float4* rs4 = reinterpret_cast<float4*>(smem + (size_t)groupTabEntries(maxN) * 2);
   float4* cs4 = rs4 + 4 * ((maxN + 3) / 4);  // [52] card sums, [52] total
-  float4* part = cs4 + 53;                   // [8] warp partial totals
+  uint16_t* cardsS = reinterpret_cast<uint16_t*>(cs4 + 53);
+  int16_t* sameS = reinterpret_cast<int16_t*>(cardsS + (maxN + 7) / 8 * 8);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 
   stageTab(csr, t.poolU16 + st.csrOff[opp], 53 + 2 * no);
   stageRows4(rs4, t, rows, u, tr, no);
+  {  // the traverser's card pairs and identical-combo slots
+    const uint16_t* cards = reinterpret_cast<const uint16_t*>(t.poolU8 + st.cardsOff[tr]);
+    const int16_t* same = t.poolI16 + st.sameOff[tr];
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+      cardsS[i] = cards[i];
+      sameS[i] = same[i];
+    }
+  }
   __syncthreads();
   // Card sums, four cards per warp (8 lanes x 8 entries, then a fixed
   // xor tree over the 8 lanes).
@@ -299,19 +310,14 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
     for (int m = 4; m > 0; m >>= 1) a += shflXor4(a, m, 8);
     if (sub == 0) cs4[c] = a;
   }
-  // Total: strided partial sums, a fixed xor tree per warp, warps in order.
-  {
-    float4 a = zero4();
-    for (int j = threadIdx.x; j < no; j += blockDim.x) a += rs4[j];
+  __syncthreads();
+  // Total: every combo holds two cards, so it is half the 52 card sums'
+  // total (warp 0: card pairs c, c + 26, then a fixed xor tree).
+  if (warp == 0) {
+    float4 a = lane < 26 ? cs4[lane] + cs4[lane + 26] : zero4();
 #pragma unroll
     for (int m = 16; m > 0; m >>= 1) a += shflXor4(a, m);
-    if (lane == 0) part[warp] = a;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float4 s = part[0];
-    for (int w = 1; w < nw; ++w) s += part[w];
-    cs4[52] = s;
+    if (lane == 0) cs4[52] = make_float4(0.5f * a.x, 0.5f * a.y, 0.5f * a.z, 0.5f * a.w);
   }
   __syncthreads();
   const float4 tot = cs4[52];
@@ -319,8 +325,6 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
 #pragma unroll
   for (int g = 0; g < 4; ++g)
     if (u[g] >= 0) v[g] = t.termVal[((size_t)u[g] * 2 + tr) * 4];
-  const uint16_t* cards = reinterpret_cast<const uint16_t*>(t.poolU8 + st.cardsOff[tr]);
-  const int16_t* same = t.poolI16 + st.sameOff[tr];
   float* out[4];
   outRows4(out, t, rows, u);
   const int nt4 = quadsOf(nt) * 4;
@@ -330,7 +334,7 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
       storeOut4(out, i, zero4());
       continue;
     }
-    const int cp = cards[i], sm = same[i];
+    const int cp = cardsS[i], sm = sameS[i];
     float4 w = tot - cs4[cp & 0xff] - cs4[cp >> 8];
     if (sm >= 0) w += rs4[sm];
     w = max0(w);
