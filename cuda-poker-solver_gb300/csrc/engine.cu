@@ -442,7 +442,7 @@ std::vector<Engine::KernelStat> Engine::profile(int n, bool splitKinds) {
                      fwd ? "fwd_chance" : "bwd_chance"});
       continue;
     }
-    const bool bwd = l.kind == kBwd || l.kind == kBwdTerm || l.kind == kBwdInt;
+    const bool bwd = l.kind == kBwdTerm || l.kind == kBwdInt;
     if (!bwd || !splitKinds) {
       P.push_back({l, launchName(l.kind)});
       continue;

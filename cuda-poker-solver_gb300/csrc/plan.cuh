@@ -33,12 +33,12 @@ struct ListRef {
   int off = 0, count = 0;
 };
 
-enum LaunchKind { kFwd, kBwd, kBwdTerm, kBwdInt, kSdGroup, kFdGroup, kDecRec, kFwdRec,
-                  kFwdMix, kBwdMix, kCounter };
+enum LaunchKind { kFwd, kBwdTerm, kBwdInt, kSdGroup, kFdGroup, kDecRec, kFwdRec, kFwdMix,
+                  kBwdMix, kCounter };
 inline const char* launchName(LaunchKind k) {
-  static const char* names[] = {"fwd_level",    "bwd_level", "bwd_terminal", "bwd_interior",
-                                "bwd_showdown", "bwd_fold",  "bwd_decide",   "fwd_decide",
-                                "fwd_level",    "bwd_interior", "counter"};
+  static const char* names[] = {"fwd_level",  "bwd_terminal", "bwd_interior", "bwd_showdown",
+                                "bwd_fold",   "bwd_decide",   "fwd_decide",   "fwd_level",
+                                "bwd_interior", "counter"};
   return names[k];
 }
 
@@ -78,10 +78,6 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
   switch (l.kind) {
     case kFwd:
       fwdLevelK<float><<<g, kThreads, 0, s>>>(a.tree, a.rows, tk, l.list.count, l.tr, 0);
-      break;
-    case kBwd:
-      bwdLevelK<float><<<g, kThreads, a.smem, s>>>(a.tree, a.rows, tk, l.list.count, l.tr,
-                                                   kModeCFR, a.maxN);
       break;
     case kBwdTerm:
       bwdTerminalK<float><<<g, kThreads, a.smem, s>>>(a.tree, a.rows, tk, l.list.count, l.tr,
