@@ -250,10 +250,43 @@ def served_bench(spots, lam, count, seed=7):
             "peak_active": info["peak_active"], "offered_seconds": float(arrivals[-1])}
 
 
+def reference_kernels(steps, warmup):
+    """The reference's own GPU kernels (cuda/gpu_cfr.cu compiled from its
+    source for sm_103a, oracle/ref/ref_gpu.cpp's host runner: the
+    reference's layout, graph and launch sequence) timed on this GPU with
+    CUDA events over graph replays, per spot."""
+    from oracle import ref_gpu
+    if not ref_gpu.fatbin_present():
+        return {"unavailable": "oracle/_ref/gpu_cfr_kernels.fatbin not built (the reference "
+                               "sources are needed to build it)"}
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no GPU"}
+    except ImportError:
+        return {"unavailable": "no torch"}
+    from pps import pps_native as pn
+    from pps import workloads as wl
+    out = {"unit": "iters/s", "kind": "reference kernels on this GPU",
+           "method": "CUDA events over graph replays after warm-up"}
+    for name in ("turn_c3", "turn_w52", "flop_164k"):
+        spot = wl.NAMED[name]()
+        cfg = pn.bet_config(spot.cfg.bet_text(), spot.cfg.raise_text(), spot.cfg.max_raises)
+        exp = pn.compile_export(spot.board, spot.oop, spot.ip, spot.pot, spot.stack, [cfg])
+        r = ref_gpu.RefKernels(exp, spot.pot)
+        n = max(1, min(steps, 300))
+        ms = r.ms_per_iteration(max(3, warmup), n)
+        r.close()
+        out[name] = {"value": 1000.0 / ms, "iterations": n,
+                     "nodes": int(exp["numNodes"][0])}
+    return out
+
+
 def run_reference(args, rank):
-    """--impl reference: the CPU restatement of the reference iteration (the
-    reference's own CPU path does not exist: its CPU river solver was
-    removed, and its GPU engine cannot be built on this machine)."""
+    """--impl reference: the CPU restatement of the reference iteration on
+    the host cores (the reference has no CPU implementation of this path:
+    its CPU river solver was removed). Beside it, ``gpu_kernels`` times the
+    reference's own GPU kernels on the same GPU."""
     if rank != 0:
         return
     from pps import workloads as wl
@@ -285,6 +318,11 @@ def run_reference(args, rank):
                                        % (done, steps, budget)},
             "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    del o
+    try:
+        line["gpu_kernels"] = reference_kernels(args.steps, args.warmup)
+    except Exception as e:  # reported, not fatal: the CPU line above stands
+        line["gpu_kernels"] = {"unavailable": "%s: %s" % (type(e).__name__, e)}
     print(json.dumps(line), flush=True)
 
 

@@ -7,6 +7,11 @@
 #   oracle/_ref/ref_capture  reference tree compiler on a host CUDA stub
 #   oracle/_ref/tiny_check   reference known-answer EV program
 #   oracle/_ref/ref_probe    reference evaluator / betActions / range parser
+#   oracle/_ref/gpu_cfr_kernels.fatbin
+#                            the reference's GPU kernels (cuda/gpu_cfr.cu,
+#                            device code only) for sm_103a, run on the GPU by
+#                            oracle/ref/ref_gpu.cpp as a second checker and
+#                            timed beside the CPU port
 #
 # Only files under /root/reference are compiled; the reference's own build
 # system (CMake/Makefile) is not used.
@@ -29,4 +34,7 @@ g++ -std=c++17 -O2 -w -I"$REF/src" "$REF/tools/tiny_check.cpp" \
   -o "$OUT/tiny_check"
 g++ -std=c++17 -O2 -w -I"$REF/src" "$HERE/ref_probe.cpp" $CORE \
   -o "$OUT/ref_probe"
-echo "built $OUT/ref_capture $OUT/tiny_check $OUT/ref_probe"
+nvcc -std=c++17 -O3 -w -fatbin -gencode arch=compute_103a,code=sm_103a \
+  -I"$REF/src" -I"$REF/cuda" "$REF/cuda/gpu_cfr.cu" -o "$OUT/gpu_cfr_kernels.fatbin"
+"$OUT/ref_capture" --treebuf > "$OUT/treebuf.txt"
+echo "built $OUT/ref_capture $OUT/tiny_check $OUT/ref_probe $OUT/gpu_cfr_kernels.fatbin"

@@ -20,6 +20,7 @@
 #include <array>
 #include <chrono>
 #include <cmath>
+#include <cstddef>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -145,7 +146,26 @@ std::vector<double> parseList(const std::string& s) {
 
 }  // namespace
 
+// `ref_capture --treebuf`: the reference kernels' argument block, TreeBuf
+// (cuda/gpu_cfr.cu:132-201), as "name offset" lines plus "sizeof N".
+int printTreeBuf() {
+  using TB = gpu::TreeBuf;
+#define M(f) std::printf("%s %zu\n", #f, offsetof(TB, f));
+  M(regret) M(regretRW) M(strat) M(stratRW) M(regOff) M(strOff) M(na) M(player)
+  M(foldBy) M(childFlat) M(childBase) M(kind) M(boardId) M(nC0) M(nC1) M(comboOff0)
+  M(comboOff1) M(comboId) M(reachOff) M(cfvOff) M(sc0) M(sc1) M(potBase) M(reach)
+  M(reachRW) M(cfv) M(cfvRW) M(nBranch) M(chanceQ) M(pc0) M(pc1) M(runOffOff)
+  M(runOff) M(ctap) M(ctapBase) M(expOffOff) M(expOff) M(expIdx) M(expIdxBase)
+  M(cards0) M(cards1) M(sameOther0) M(sameOther1) M(brOppSortedOff) M(brOppSorted)
+  M(brLessOff) M(brLessEnd) M(brTieEnd) M(brCardPosOff) M(brCardPosIdx)
+  M(brRevSortedOff) M(brRevSorted) M(foldSonOff) M(foldSon) M(n0Base) M(n1Base) M(pot)
+#undef M
+  std::printf("sizeof %zu\n", sizeof(TB));
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc == 2 && std::strcmp(argv[1], "--treebuf") == 0) return printTreeBuf();
   if (argc != 10) {
     std::fprintf(stderr,
                  "usage: ref_capture <out.bin> <board> <oop> <ip> <pot> "

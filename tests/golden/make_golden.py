@@ -13,6 +13,9 @@ Fixtures:
   eval_keys.npz       reference strength keys of seeded 7-card hands
   bet_actions.json    reference pf::betActions on seeded betting states
   ranges.json         reference parseRange weights for range strings
+  ref_treebuf.json    byte offset of every TreeBuf member (the argument
+                      block of the reference kernels, cuda/gpu_cfr.cu:
+                      132-201) and its size, as compiled from the source
 """
 from __future__ import annotations
 
@@ -91,9 +94,28 @@ def run_probe(mode, lines):
     return p.stdout.strip("\n").split("\n")
 
 
+def treebuf_layout():
+    out = subprocess.run([os.path.join(REF_BIN, "ref_capture"), "--treebuf"],
+                         capture_output=True, text=True, check=True).stdout
+    members, size = [], None
+    for line in out.split("\n"):
+        f = line.split()
+        if len(f) != 2:
+            continue
+        if f[0] == "sizeof":
+            size = int(f[1])
+        else:
+            members.append([f[0], int(f[1])])
+    json.dump({"members": members, "size": size},
+              open(os.path.join(HERE, "ref_treebuf.json"), "w"), indent=0)
+
+
 def main():
     if not os.path.exists(os.path.join(REF_BIN, "ref_capture")):
         raise SystemExit("build the reference tools first: sh oracle/ref/build_ref.sh")
+    treebuf_layout()
+    if sys.argv[1:] == ["--treebuf"]:
+        return
     small = [wl.river_c1(), wl.turn_api(), wl.turn_tiny()] + edge_spots()
     for spot in small:
         arrs = capture(spot)

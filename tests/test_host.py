@@ -131,3 +131,14 @@ def test_batched_distribution():
         assert set(s.cfg.bets) <= {0.25, 0.33, 0.5, 0.75, 1.0, 1.5} and s.cfg.allin
         assert len(s.oop) == 1326 and 0.0 <= min(s.oop) and max(s.oop) < 1.0
     assert [s.board for s in wl.batched(8)] == [s.board for s in spots[:8]]  # seeded
+
+
+def test_reference_kernel_argument_block(golden_dir):
+    """The runner of the reference's own kernels (oracle/ref/ref_gpu.cpp)
+    builds TreeBuf (cuda/gpu_cfr.cu:132-201) with the member order, offsets
+    and size of the struct compiled from the reference source."""
+    from oracle import ref_gpu
+    want = json.load(open(os.path.join(golden_dir, "ref_treebuf.json")))
+    members, size = ref_gpu.args_layout()
+    assert size == want["size"] == 448
+    assert [list(m) for m in members] == want["members"]
