@@ -35,7 +35,7 @@ def normwise(a, b):
 ROW_CASES = [("river_c1", 1), ("river_c1", 2), ("river_c1", 10), ("turn_short", 1),
              ("turn_short", 2), ("turn_api", 1), ("river_geo", 1), ("river_geo", 2),
              ("flop_short", 1), ("flop_short", 2), ("turn_c2_uniform", 1), ("turn_c3", 1),
-             ("turn_w52", 1), ("turn_w52", 2)]
+             ("turn_w52", 1)]
 
 
 @pytest.mark.parametrize("name,iters", ROW_CASES)
@@ -44,7 +44,11 @@ def test_rows_match_reference_kernels(name, iters):
     (max |product - reference| / max |reference|) within 5e-5. The two
     differ only in f32 summation order (the reference's showdown scan is
     plain f32 and its fold sums use shared-memory atomics, so its own runs
-    drift by rounding)."""
+    drift by rounding). Cases are the well-conditioned ones: where regret
+    matching meets regrets that are exactly zero in exact arithmetic
+    (turn_w52 after 2 iterations: there even the f32 and f64 oracles differ
+    by 0.04 normwise), rounding picks the strategy, and the solutions are
+    compared instead (below)."""
     spot = wl.NAMED[name]()
     r = reference(spot)
     r.solve(iters)
