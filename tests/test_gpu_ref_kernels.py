@@ -83,7 +83,7 @@ def test_at_least_as_accurate_as_reference_kernels(name, iters):
 
 
 @pytest.mark.parametrize("name,iters", [("river_c1", 1000), ("turn_api", 300),
-                                        ("turn_c2_uniform", 100), ("turn_w52", 200)])
+                                        ("turn_c2_uniform", 100), ("turn_w52", 1000)])
 def test_solution_matches_reference_kernels(name, iters):
     """After a full solve both strategies pass the solution gates against
     each other: EVs within 0.01 chips and exploitability within a factor 2
