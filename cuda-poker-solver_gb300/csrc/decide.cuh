@@ -15,7 +15,8 @@
 //              the traverser's layout (quads)
 //   [2] n | na << 16 | own << 24   combos of the row's side, actions,
 //              own = 1 when the traverser acts (backward update)
-//   [3] chunk | spot << 16         quad chunk (kChunkQuads quads), spot slot
+//   [3] chunk | spot << 16         quad chunk (kRecQuads quads: one warp's
+//              lanes), spot slot
 //   [4 + a]    action a's child row: backward its value row, forward its
 //              reach row in the traverser's layout (quads)
 // The arithmetic is decideChunk's / fwdDecideChunk's (the reference's
@@ -50,11 +51,11 @@ __device__ __forceinline__ DecRec loadRec(const uint32_t* __restrict__ recs, uin
   return d;
 }
 
-// Backward decide record (CFR mode, f32 rows).
+// Backward decide record (CFR mode, f32 rows), one warp: lane = quad.
 __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<float>& rows,
-                                             const DecRec& r) {
+                                             const DecRec& r, int lane) {
   const int nq = quadsOf(r.n);
-  const int q = r.chunk * kChunkQuads + (int)threadIdx.x;
+  const int q = r.chunk * kRecQuads + lane;
   if (q >= nq) return;
   float* out = rows.cfv + (size_t)r.rowQ * 4;
   bool live[4];
@@ -118,9 +119,9 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
 // Forward decide record (opponent node, CFR mode): child reach = reach x
 // sigma_a from the regrets (regret matching+).
 __device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<float>& rows,
-                                                int tr, const DecRec& r) {
+                                                int tr, const DecRec& r, int lane) {
   const int nq = quadsOf(r.n);
-  const int q = r.chunk * kChunkQuads + (int)threadIdx.x;
+  const int q = r.chunk * kRecQuads + lane;
   if (q >= nq) return;
   const int na = r.na;
   const float* src = t.regret + (size_t)r.regQ * 4;
@@ -141,25 +142,36 @@ __device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<
   }
 }
 
-// One CTA (kThreads threads) per record, one kernel per pass. Internal
-// linkage: included by more than one translation unit.
+// One warp per record (kRecWarps records per CTA), one kernel per pass.
+// A warp's records are independent of its CTA's other warps: no barrier.
+// Internal linkage: included by more than one translation unit.
+constexpr int kRecWarps = kThreads / 32;
+__host__ __device__ inline int recordCtas(int records) {
+  return (records + kRecWarps - 1) / kRecWarps;
+}
+
 static __global__ void __launch_bounds__(kThreads, 12)
 decideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
            const uint32_t* __restrict__ tasks, int count) {
-  for (int i = blockIdx.x; i < count; i += gridDim.x) decideRecord(t, rows, loadRec(recs, tasks[i]));
+  const int lane = (int)threadIdx.x & 31;
+  for (int i = blockIdx.x * kRecWarps + (int)(threadIdx.x >> 5); i < count;
+       i += gridDim.x * kRecWarps)
+    decideRecord(t, rows, loadRec(recs, tasks[i]), lane);
 }
 
 static __global__ void __launch_bounds__(kThreads, 12)
 fwdDecideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
               const uint32_t* __restrict__ tasks, int count, int tr) {
-  for (int i = blockIdx.x; i < count; i += gridDim.x)
-    fwdDecideRecord(t, rows, tr, loadRec(recs, tasks[i]));
+  const int lane = (int)threadIdx.x & 31;
+  for (int i = blockIdx.x * kRecWarps + (int)(threadIdx.x >> 5); i < count;
+       i += gridDim.x * kRecWarps)
+    fwdDecideRecord(t, rows, tr, loadRec(recs, tasks[i]), lane);
 }
 
 // ---------------------------------------------------------------------------
 // Level kernels of the default iteration: one launch per level and pass
-// covering the level's decide records and chance tasks (CTA i < nRec: a
-// record; else a chance task word), launched with programmatic dependent
+// covering the level's decide records and chance tasks (CTA i <
+// recordCtas(nRec): one record per warp; else a chance task word), launched with programmatic dependent
 // launch so consecutive levels overlap: each CTA lets the next level's grid
 // start (launch_dependents), loads its record (static data), then waits
 // until the previous level's grid has finished and its writes are visible
@@ -175,13 +187,16 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
              const uint32_t* __restrict__ recTasks, int nRec, const int* __restrict__ chance,
              int nCh, int tr) {
   pdlTrigger();
-  for (int i = blockIdx.x; i < nRec + nCh; i += gridDim.x) {
-    if (i < nRec) {
-      const DecRec r = loadRec(recs, recTasks[i]);
+  const int nRc = recordCtas(nRec), lane = (int)threadIdx.x & 31;
+  for (int i = blockIdx.x; i < nRc + nCh; i += gridDim.x) {
+    if (i < nRc) {
+      const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
+      if (k >= nRec) continue;
+      const DecRec r = loadRec(recs, recTasks[k]);
       pdlWait();
-      fwdDecideRecord(t, rows, tr, r);
+      fwdDecideRecord(t, rows, tr, r, lane);
     } else {
-      const int w = chance[i - nRec];
+      const int w = chance[i - nRc];
       pdlWait();
       fwdChanceBranch<float>(t, rows, (int)((unsigned)w >> 8), (w >> 2) & 63, tr);
     }
@@ -194,13 +209,16 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
              int nCh, int tr) {
   __shared__ __align__(16) unsigned char smem[kChanceScratchBytes];
   pdlTrigger();
-  for (int i = blockIdx.x; i < nRec + nCh; i += gridDim.x) {
-    if (i < nRec) {
-      const DecRec r = loadRec(recs, recTasks[i]);
+  const int nRc = recordCtas(nRec), lane = (int)threadIdx.x & 31;
+  for (int i = blockIdx.x; i < nRc + nCh; i += gridDim.x) {
+    if (i < nRc) {
+      const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
+      if (k >= nRec) continue;
+      const DecRec r = loadRec(recs, recTasks[k]);
       pdlWait();
-      decideRecord(t, rows, r);
+      decideRecord(t, rows, r, lane);
     } else {
-      const int w = chance[i - nRec];
+      const int w = chance[i - nRc];
       pdlWait();
       chanceChunk<float>(t, rows, (int)((unsigned)w >> 8), (w >> 2) & 63, tr, smem);
       __syncthreads();  // the next chance task reuses the pointer tables

@@ -308,7 +308,7 @@ HostLayout buildLayout(const Tree& t) {
       std::vector<uint32_t> kids(nd.na);
       for (int a = 0; a < nd.na; ++a) kids[a] = L.rows[t.children[nd.childBase + a]].cfvQ;
       const int nTr = t.n(u, tr);
-      const int chunksTr = (int)((quads(nTr) + kChunkQuads - 1) / kChunkQuads);
+      const int chunksTr = (int)((quads(nTr) + kRecQuads - 1) / kRecQuads);
       for (int c = 0; c < chunksTr; ++c)
         L.bwdRecs[tr][nd.depth].push_back(
             addRecord(L.nodes[u].regQ, L.rows[u].cfvQ, nTr, nd.na, nd.player == tr, c, kids));
@@ -316,7 +316,7 @@ HostLayout buildLayout(const Tree& t) {
       for (int a = 0; a < nd.na; ++a)
         kids[a] = L.rows[t.children[nd.childBase + a]].reachQ[tr];
       const int nOpp = t.n(u, 1 - tr);
-      const int chunksOpp = (int)((quads(nOpp) + kChunkQuads - 1) / kChunkQuads);
+      const int chunksOpp = (int)((quads(nOpp) + kRecQuads - 1) / kRecQuads);
       for (int c = 0; c < chunksOpp; ++c)
         L.fwdRecs[tr][nd.depth].push_back(
             addRecord(L.nodes[u].regQ, L.rows[u].reachQ[tr], nOpp, nd.na, 0, c, kids));

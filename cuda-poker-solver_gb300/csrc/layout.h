@@ -38,6 +38,7 @@ inline int packNode(int kind, int player, int foldBy, int na) {
 // 2-7), node (bits 8-31).
 enum TaskKind : int { kTaskDecide = 0, kTaskChance = 1, kTaskFold = 2, kTaskShowdown = 3 };
 constexpr int kChunkQuads = 128;   // row quads per decide task
+constexpr int kRecQuads = 32;      // row quads per decide record (one warp)
 constexpr int kChanceChunk = 128;  // combos per backward chance task
 inline int makeTask(int kind, int sub, int node) { return kind | (sub << 2) | (node << 8); }
 

@@ -96,11 +96,11 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
                                                  l.tr, a.maxN);
       break;
     case kDecRec:
-      decideRecK<<<g, kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
+      decideRecK<<<gridOf(recordCtas(l.list.count)), kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
                                         l.list.count);
       break;
     case kFwdRec:
-      fwdDecideRecK<<<g, kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
+      fwdDecideRecK<<<gridOf(recordCtas(l.list.count)), kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
                                            l.list.count, l.tr);
       break;
     case kFwdMix:
@@ -109,7 +109,7 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       // previous kernel in the stream drains (the kernels wait for it
       // before touching rows).
       cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(gridOf(l.list.count + l.list2.count));
+      cfg.gridDim = dim3(gridOf(recordCtas(l.list.count) + l.list2.count));
       cfg.blockDim = dim3(kThreads);
       cfg.dynamicSmemBytes = 0;
       cfg.stream = s;
