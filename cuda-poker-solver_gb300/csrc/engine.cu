@@ -183,8 +183,7 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
   raiseSmemLimit((const void*)bwdLevelK<float>, d.smemF);
   raiseSmemLimit((const void*)bwdLevelK<double>, d.smemD);
   raiseSmemLimit((const void*)bwdTerminalK<float>, d.smemF);
-  raiseSmemLimit((const void*)sdGroupK, sdGroupSmem(d.maxN));
-  raiseSmemLimit((const void*)fdGroupK, fdGroupSmem(d.maxN));
+  raiseGroupSmem(d.maxN);
   buildPlans();
   engineKind_ = 0;
   zeroRows();

@@ -768,8 +768,7 @@ void Forest::iterate(int n) {
     d.sev.ensure((int)std::max(d.staged.half[0].fwd.size(), d.staged.half[1].fwd.size()));
     const int maxN = d.maxN(all);
     const size_t smemSd = sdGroupSmem(maxN), smemFd = fdGroupSmem(maxN);
-    raiseSmemLimit((const void*)sdGroupK, smemSd);
-    raiseSmemLimit((const void*)fdGroupK, smemFd);
+    raiseGroupSmem(maxN);
     const PlanArgs args{d.tree(), d.rows<float>(aReachF0, aReachF1, aCfvF), d.tasks, d.counter,
                         (int)d.counterCap, maxN, bwdScratchBytes<float>(maxN),
                         static_cast<const int4*>(d.arr[aGroups]), smemSd, smemFd,

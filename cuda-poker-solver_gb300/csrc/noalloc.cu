@@ -236,8 +236,7 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
 
   const int4* groups = reinterpret_cast<const int4*>(base + oGroups);
   const size_t smemSd = sdGroupSmem(L.maxN), smemFd = fdGroupSmem(L.maxN);
-  raiseSmemLimit((const void*)sdGroupK, smemSd);
-  raiseSmemLimit((const void*)fdGroupK, smemFd);
+  raiseGroupSmem(L.maxN);
   auto grid = [](int count) { return (unsigned)std::min(count, 1 << 20); };
   for (int it = 0; it < iterations; ++it) {
     for (int tr = 0; tr < 2; ++tr) {
@@ -247,11 +246,11 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
               tree, rows, dTasks + fwd[tr][d].first, fwd[tr][d].second, tr, 0);
       for (int d = D - 1; d >= 0; --d) {
         if (sdG[d].second)
-          sdGroupK<<<grid(sdG[d].second), kTermThreads, smemSd, stream>>>(
-              tree, rows, groups, dTasks + sdG[d].first, sdG[d].second, tr, L.maxN);
+          launchSdGroups(grid(sdG[d].second), smemSd, stream, tree, rows, groups,
+                         dTasks + sdG[d].first, sdG[d].second, tr, L.maxN);
         if (fdG[d].second)
-          fdGroupK<<<grid(fdG[d].second), kTermThreads, smemFd, stream>>>(
-              tree, rows, groups, dTasks + fdG[d].first, fdG[d].second, tr, L.maxN);
+          launchFdGroups(grid(fdG[d].second), smemFd, stream, tree, rows, groups,
+                         dTasks + fdG[d].first, fdG[d].second, tr, L.maxN);
         if (inner[tr][d].second)
           bwdInteriorK<float><<<grid(inner[tr][d].second), kThreads, 0, stream>>>(
               tree, rows, dTasks + inner[tr][d].first, inner[tr][d].second, tr, kModeCFR);

@@ -88,12 +88,10 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
                                                  kModeCFR);
       break;
     case kSdGroup:
-      sdGroupK<<<g, kTermThreads, a.smemSd, s>>>(a.tree, a.rows, a.groups, tk, l.list.count,
-                                                 l.tr, a.maxN);
+      launchSdGroups(g, a.smemSd, s, a.tree, a.rows, a.groups, tk, l.list.count, l.tr, a.maxN);
       break;
     case kFdGroup:
-      fdGroupK<<<g, kTermThreads, a.smemFd, s>>>(a.tree, a.rows, a.groups, tk, l.list.count,
-                                                 l.tr, a.maxN);
+      launchFdGroups(g, a.smemFd, s, a.tree, a.rows, a.groups, tk, l.list.count, l.tr, a.maxN);
       break;
     case kDecRec:
       decideRecK<<<gridOf(recordCtas(l.list.count)), kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,

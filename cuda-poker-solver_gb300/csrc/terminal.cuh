@@ -56,8 +56,9 @@ __device__ __forceinline__ float comp4(float4 v, int g) {
 
 // ---- shared-memory layout of a group task (maxN: largest list) ----
 // The sorted prefix gives each thread kSpan consecutive positions, so one
-// pass of kTermThreads threads covers every list (kSpan * 256 >= 1327); a
-// warp's 256 positions form one compensation block.
+// pass of kTermThreads threads covers every list (kSpan * 256 >= 1327), and
+// narrower CTAs cover narrower lists (termThreadsFor); a warp's 256
+// positions form one compensation block.
 constexpr int kSpan = 8;
 constexpr int kSpanShift = 8;  // log2(32 * kSpan): position -> warp block
 __host__ __device__ inline int groupTabEntries(int maxN) { return (3 * maxN + 53 + 7) / 8 * 8; }
@@ -347,7 +348,19 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
 // kernel per kind (the showdown tables need 4x the shared memory and more
 // registers; folds fit more CTAs per SM). Internal linkage: this header is
 // included by more than one translation unit, each keeping its own copy.
-static __global__ void __launch_bounds__(kTermThreads, 3)
+//
+// The CTA has kT threads, the fewest whose sorted-prefix pass (kSpan
+// positions a thread) covers positions 0..maxN: narrow ranges (lists of up
+// to 511 combos) take 64-thread CTAs, so a level's groups fit the GPU in
+// one wave instead of holding idle threads.
+__host__ __device__ constexpr int termThreadsFor(int maxN) {
+  return maxN + 1 <= kSpan * 64 ? 64 : maxN + 1 <= kSpan * 128 ? 128 : kTermThreads;
+}
+constexpr int sdMinBlocks(int kT) { return 3 * kTermThreads / kT; }
+constexpr int fdMinBlocks(int kT) { return 4 * kTermThreads / kT; }
+
+template <int kT>
+static __global__ void __launch_bounds__(kT, sdMinBlocks(kT))
 sdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
          const int* __restrict__ tasks, int count, int tr, int maxN) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -359,7 +372,8 @@ sdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
   }
 }
 
-static __global__ void __launch_bounds__(kTermThreads, 4)
+template <int kT>
+static __global__ void __launch_bounds__(kT, fdMinBlocks(kT))
 fdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
          const int* __restrict__ tasks, int count, int tr, int maxN) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -369,6 +383,43 @@ fdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
     foldGroup(t, rows, u, tr, smem, maxN);
     __syncthreads();
   }
+}
+
+void raiseSmemLimit(const void* kernel, size_t bytes);
+
+// Launches one level's showdown (fold) groups with the CTA size of maxN.
+static inline void launchSdGroups(unsigned grid, size_t smem, cudaStream_t s, const DevTree& t,
+                                  const DevRows<float>& rows, const int4* groups,
+                                  const int* tasks, int count, int tr, int maxN) {
+  switch (termThreadsFor(maxN)) {
+    case 64: sdGroupK<64><<<grid, 64, smem, s>>>(t, rows, groups, tasks, count, tr, maxN); break;
+    case 128: sdGroupK<128><<<grid, 128, smem, s>>>(t, rows, groups, tasks, count, tr, maxN); break;
+    default:
+      sdGroupK<kTermThreads><<<grid, kTermThreads, smem, s>>>(t, rows, groups, tasks, count, tr,
+                                                             maxN);
+  }
+}
+static inline void launchFdGroups(unsigned grid, size_t smem, cudaStream_t s, const DevTree& t,
+                                  const DevRows<float>& rows, const int4* groups,
+                                  const int* tasks, int count, int tr, int maxN) {
+  switch (termThreadsFor(maxN)) {
+    case 64: fdGroupK<64><<<grid, 64, smem, s>>>(t, rows, groups, tasks, count, tr, maxN); break;
+    case 128: fdGroupK<128><<<grid, 128, smem, s>>>(t, rows, groups, tasks, count, tr, maxN); break;
+    default:
+      fdGroupK<kTermThreads><<<grid, kTermThreads, smem, s>>>(t, rows, groups, tasks, count, tr,
+                                                             maxN);
+  }
+}
+// Opens the dynamic shared memory the group kernels of maxN need (every CTA
+// size: the translation unit's own copies).
+static inline void raiseGroupSmem(int maxN) {
+  const size_t sd = sdGroupSmem(maxN), fd = fdGroupSmem(maxN);
+  raiseSmemLimit((const void*)sdGroupK<64>, sd);
+  raiseSmemLimit((const void*)sdGroupK<128>, sd);
+  raiseSmemLimit((const void*)sdGroupK<kTermThreads>, sd);
+  raiseSmemLimit((const void*)fdGroupK<64>, fd);
+  raiseSmemLimit((const void*)fdGroupK<128>, fd);
+  raiseSmemLimit((const void*)fdGroupK<kTermThreads>, fd);
 }
 
 }  // namespace gb
