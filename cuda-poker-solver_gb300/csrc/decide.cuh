@@ -82,7 +82,7 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
   // The children's value rows and the strategy rows are needed only after
   // the regret pass: start fetching them into L2 now (a hint, no data).
   for (int a = 0; a < na; ++a) {
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q));
     asm volatile("prefetch.global.L2 [%0];" ::"l"(str + ((size_t)a * nq + q) * 4));
   }
   // Streaming form: a row is reloaded (a cache hit) instead of held in
