@@ -402,6 +402,13 @@ int pps_gb_save(pps_gb_solver* h, const char* path) {
   });
 }
 
+int pps_gb_save_compressed(pps_gb_solver* h, const char* path) {
+  return guarded([&] {
+    if (!path) throw Error{PPS_GB_E_ARG, "null path"};
+    core(h).save(path, true);
+  });
+}
+
 int pps_gb_debug_dump(pps_gb_solver* h) {
   return guarded([&] { core(h).debugDump(); });
 }

@@ -18,6 +18,7 @@
 
 #include "kernels.cuh"
 #include "plan.cuh"
+#include "rowcodec.h"
 #include "terminal.cuh"
 #include "pps_gb.h"
 
@@ -586,6 +587,51 @@ void Engine::setDenseRows(int which, const std::vector<float>& dense) {
     GB_CK(cudaMemcpy(which == 0 ? d_->tree.regret : d_->tree.strat, padded.data(),
                      padded.size() * sizeof(float), cudaMemcpyHostToDevice));
   h2d_ += (int64_t)(padded.size() * sizeof(float));
+}
+
+namespace {
+// Action rows of the decide nodes in dense order: padded device offset,
+// dense offset, length.
+std::vector<RowRef> actionRowTable(const Tree& t, const HostLayout& L) {
+  std::vector<RowRef> tab;
+  int64_t dst = 0;
+  for (int u : t.decideNodes) {
+    const Node& nd = t.nodes[u];
+    const int n = t.n(u, nd.player);
+    const int64_t base = (int64_t)L.nodes[u].regQ * 4, stride = (int64_t)quads(n) * 4;
+    for (int a = 0; a < nd.na; ++a) {
+      tab.push_back(RowRef{base + a * stride, dst, n, 0});
+      dst += n;
+    }
+  }
+  return tab;
+}
+}  // namespace
+
+int64_t Engine::actionRows() const {
+  int64_t k = 0;
+  for (int u : t_.decideNodes) k += t_.nodes[u].na;
+  return k;
+}
+
+void Engine::packRows(int which, std::vector<uint16_t>& codes,
+                      std::vector<float>& scales) const {
+  GB_CK(cudaStreamSynchronize(d_->stream));
+  gb::packRows(which == 0 ? d_->tree.regret : d_->tree.strat, actionRowTable(t_, L_),
+               t_.rowTotal, which == 0, d_->stream, codes, scales);
+  d2h_ += (int64_t)(codes.size() * sizeof(uint16_t) + scales.size() * sizeof(float));
+}
+
+void Engine::unpackRows(int which, const std::vector<uint16_t>& codes,
+                        const std::vector<float>& scales) {
+  if ((int64_t)codes.size() != t_.rowTotal || (int64_t)scales.size() != actionRows())
+    throw Error{PPS_GB_E_ARG, "compressed row table size mismatch"};
+  float* rows = which == 0 ? d_->tree.regret : d_->tree.strat;
+  GB_CK(cudaStreamSynchronize(d_->stream));
+  if (L_.regQuads)
+    GB_CK(cudaMemsetAsync(rows, 0, (size_t)L_.regQuads * 4 * sizeof(float), d_->stream));
+  gb::unpackRows(rows, actionRowTable(t_, L_), which == 0, codes, scales, d_->stream);
+  h2d_ += (int64_t)(codes.size() * sizeof(uint16_t) + scales.size() * sizeof(float));
 }
 
 std::vector<float> Engine::nodeRows(int which, int node) const {

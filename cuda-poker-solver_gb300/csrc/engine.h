@@ -41,6 +41,12 @@ class Engine {
   // layout (decide nodes in node order, na x n, action-major).
   std::vector<float> denseRows(int which) const;
   void setDenseRows(int which, const std::vector<float>& dense);
+  // The same rows as 16-bit codes (dense order) with one scale per action
+  // row (rowcodec.h), coded and decoded on the device.
+  void packRows(int which, std::vector<uint16_t>& codes, std::vector<float>& scales) const;
+  void unpackRows(int which, const std::vector<uint16_t>& codes,
+                  const std::vector<float>& scales);
+  int64_t actionRows() const;
   // One decide node's strategy rows (na x n, dense).
   std::vector<float> nodeRows(int which, int node) const;
 

@@ -295,6 +295,10 @@ TreeStructure GpuPostflopSolver::treeStructure() const {
   return t;
 }
 
+void GpuPostflopSolver::saveCompressed(const std::string& path) const {
+  check(pps_gb_save_compressed(impl_->h, path.c_str()));
+}
+
 void GpuPostflopSolver::save(const std::string& path) const {
   check(pps_gb_save(impl_->h, path.c_str()));
 }

@@ -648,7 +648,11 @@ void SolverCore::debugDump() {
 // ---------------------------------------------------------------------------
 // "PPS1" solution files (cuda/gpu_cfr.cu:2686-2853). Version 1 holds one
 // bet config; version 2 (per-street configs, no reference counterpart)
-// holds three in the same field order.
+// holds three in the same field order. Versions 3 and 4 (no reference
+// counterpart) are 1 and 2 with compressed rows: after the row count, the
+// number of action rows, then for the regrets and then the strategy one
+// f32 scale per action row followed by one 16-bit code per entry
+// (rowcodec.h), about half the size of the f32 rows.
 // ---------------------------------------------------------------------------
 
 namespace {
@@ -721,7 +725,7 @@ struct Reader {
 };
 }  // namespace
 
-void SolverCore::save(const std::string& path) const {
+void SolverCore::save(const std::string& path, bool compressed) const {
   if (!eng_) throw Error{PPS_GB_E_STATE, "cannot save an empty solver"};
   FILE* f = std::fopen(path.c_str(), "wb");
   if (!f) throw Error{PPS_GB_E_IO, "cannot open for writing: " + path};
@@ -729,7 +733,7 @@ void SolverCore::save(const std::string& path) const {
     Writer w{f, path};
     const gpu::PostflopSpot& sp = tree_.spot;
     w.val<uint32_t>(kMagic);
-    w.val<uint32_t>(tree_.perStreet ? 2u : 1u);
+    w.val<uint32_t>((tree_.perStreet ? 2u : 1u) + (compressed ? 2u : 0u));
     w.val<int32_t>(sp.nBoard);
     w.put(sp.board, sizeof(sp.board));
     w.val<int64_t>(sp.pot);
@@ -745,9 +749,20 @@ void SolverCore::save(const std::string& path) const {
     w.val<int32_t>((int32_t)lastAlgo_.size());
     w.put(lastAlgo_.data(), lastAlgo_.size());
     w.val<int64_t>(tree_.rowTotal);
-    const std::vector<float> reg = eng_->denseRows(0), str = eng_->denseRows(1);
-    w.put(reg.data(), reg.size() * sizeof(float));
-    w.put(str.data(), str.size() * sizeof(float));
+    if (compressed) {
+      w.val<int64_t>(eng_->actionRows());
+      for (int which = 0; which < 2; ++which) {
+        std::vector<uint16_t> codes;
+        std::vector<float> scales;
+        eng_->packRows(which, codes, scales);
+        w.put(scales.data(), scales.size() * sizeof(float));
+        w.put(codes.data(), codes.size() * sizeof(uint16_t));
+      }
+    } else {
+      const std::vector<float> reg = eng_->denseRows(0), str = eng_->denseRows(1);
+      w.put(reg.data(), reg.size() * sizeof(float));
+      w.put(str.data(), str.size() * sizeof(float));
+    }
     if (std::fflush(f) != 0) throw Error{PPS_GB_E_IO, "write failed: " + path};
   } catch (...) {
     std::fclose(f);
@@ -761,9 +776,10 @@ std::unique_ptr<SolverCore> SolverCore::load(const std::string& path) {
   if (r.val<uint32_t>() != kMagic)
     throw Error{PPS_GB_E_FORMAT, "not a solution file: " + path};
   const uint32_t ver = r.val<uint32_t>();
-  if (ver != 1 && ver != 2)
+  if (ver < 1 || ver > 4)
     throw Error{PPS_GB_E_FORMAT, "solution file version " + std::to_string(ver) +
-                                     " unsupported (expected 1 or 2): " + path};
+                                     " unsupported (expected 1 to 4): " + path};
+  const bool perStreet = ver == 2 || ver == 4, compressed = ver >= 3;
   gpu::PostflopSpot spot;
   spot.nBoard = r.val<int32_t>();
   if (spot.nBoard < 3 || spot.nBoard > 5)
@@ -774,7 +790,7 @@ std::unique_ptr<SolverCore> SolverCore::load(const std::string& path) {
   r.get(spot.oop.w, sizeof(spot.oop.w));
   r.get(spot.ip.w, sizeof(spot.ip.w));
   gpu::StreetBetConfigs cfgs;
-  if (ver == 2) {
+  if (perStreet) {
     for (int k = 0; k < 3; ++k) cfgs.street[k] = r.cfg();
   } else {
     cfgs.street[0] = r.cfg();
@@ -790,7 +806,7 @@ std::unique_ptr<SolverCore> SolverCore::load(const std::string& path) {
   Schedule sched;
   if (!Schedule::parse(algo, sched))
     throw Error{PPS_GB_E_FORMAT, "solution file corrupt: unknown algo '" + algo + "'"};
-  std::unique_ptr<SolverCore> s(new SolverCore(spot, cfgs, ver == 2));
+  std::unique_ptr<SolverCore> s(new SolverCore(spot, cfgs, perStreet));
   if (s->tree_.empty)
     throw Error{PPS_GB_E_FORMAT,
                 "solution spot compiled to an empty solver (empty or fully "
@@ -803,11 +819,29 @@ std::unique_ptr<SolverCore> SolverCore::load(const std::string& path) {
                     " - different engine version or spot semantics)"};
   if (savedIters < 0 || savedIters > std::numeric_limits<int>::max())
     throw Error{PPS_GB_E_FORMAT, "solution file corrupt: bad iteration count"};
-  std::vector<float> reg((size_t)rowTotal), str((size_t)rowTotal);
-  r.get(reg.data(), reg.size() * sizeof(float));
-  r.get(str.data(), str.size() * sizeof(float));
-  s->eng_->setDenseRows(0, reg);
-  s->eng_->setDenseRows(1, str);
+  if (compressed) {
+    const int64_t nRows = r.val<int64_t>();
+    if (nRows != s->eng_->actionRows())
+      throw Error{PPS_GB_E_FORMAT, "solution file corrupt: action row count " +
+                                       std::to_string(nRows) + " vs " +
+                                       std::to_string(s->eng_->actionRows())};
+    for (int which = 0; which < 2; ++which) {
+      std::vector<float> scales((size_t)nRows);
+      std::vector<uint16_t> codes((size_t)rowTotal);
+      r.get(scales.data(), scales.size() * sizeof(float));
+      r.get(codes.data(), codes.size() * sizeof(uint16_t));
+      for (float m : scales)
+        if (!(m >= 0.f) || !std::isfinite(m))
+          throw Error{PPS_GB_E_FORMAT, "solution file corrupt: bad row scale"};
+      s->eng_->unpackRows(which, codes, scales);
+    }
+  } else {
+    std::vector<float> reg((size_t)rowTotal), str((size_t)rowTotal);
+    r.get(reg.data(), reg.size() * sizeof(float));
+    r.get(str.data(), str.size() * sizeof(float));
+    s->eng_->setDenseRows(0, reg);
+    s->eng_->setDenseRows(1, str);
+  }
   s->eng_->setCounter((int)savedIters);
   s->lastAlgo_ = algo;
   s->sched_ = sched;

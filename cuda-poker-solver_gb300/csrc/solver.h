@@ -52,7 +52,9 @@ class SolverCore {
   int numBaseCombos(int player) const;
   std::vector<double> playerWeights(int player) const;
   gpu::TreeStructure treeStructure() const;
-  void save(const std::string& path) const;
+  // compressed: rows as 16-bit codes with per-action-row scales (file
+  // versions 3 / 4); otherwise f32 rows (versions 1 / 2).
+  void save(const std::string& path, bool compressed = false) const;
   void debugDump();
   // Benchmark helpers: n more iterations continuing the DCFR schedule
   // (CUDA-event timed / profiled launch by launch).

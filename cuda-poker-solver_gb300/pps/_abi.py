@@ -123,6 +123,7 @@ _SIGS = {
     "pps_gb_tree_structure": (C.c_int, [H, P(C.c_uint8), P(C.c_int), P(C.c_int), P(C.c_uint8),
                                         P(C.c_int), P(C.c_int)]),
     "pps_gb_save": (C.c_int, [H, C.c_char_p]),
+    "pps_gb_save_compressed": (C.c_int, [H, C.c_char_p]),
     "pps_gb_debug_dump": (C.c_int, [H]),
     "pps_gb_read_rows": (C.c_int, [H, C.c_int, P(C.c_float), C.c_int64, P(C.c_int64)]),
     "pps_gb_write_rows": (C.c_int, [H, C.c_int, P(C.c_float), C.c_int64]),

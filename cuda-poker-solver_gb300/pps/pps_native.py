@@ -353,8 +353,11 @@ class Solver:
         return {"decider": dec.value, "actions": [_action(acts[a]) for a in range(na.value)],
                 "branches": brs}
 
-    def save(self, path: str) -> None:
-        check(lib.pps_gb_save(self._h, str(path).encode()))
+    def save(self, path: str, compressed: bool = False) -> None:
+        """Writes a solution file; compressed=True stores the rows as 16-bit
+        codes with one scale per action row (about half the size)."""
+        fn = lib.pps_gb_save_compressed if compressed else lib.pps_gb_save
+        check(fn(self._h, str(path).encode()))
 
     def player_cards(self, player: int) -> List[int]:
         buf = (C.c_uint8 * (2 * _abi.COMBOS))()

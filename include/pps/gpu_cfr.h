@@ -145,6 +145,9 @@ class GpuPostflopSolver {
   int maxDepth() const { return maxDepth_; }
 
   void save(const std::string& path) const;
+  // Extension: the same file with compressed rows (16-bit codes, one scale
+  // per action row); the path constructor reads both.
+  void saveCompressed(const std::string& path) const;
   // Debug: non-finite counts of the regret and strategy rows (stderr).
   void debugDump();
 

@@ -199,6 +199,11 @@ int pps_gb_tree_structure(pps_gb_solver* h, uint8_t* kinds, int* child_base,
                           int* n_children);
 /* save(path) - cuda/gpu_cfr.h:246 ("PPS1" file, cuda/gpu_cfr.cu:2686-2785). */
 int pps_gb_save(pps_gb_solver* h, const char* path);
+/* Extension (no reference counterpart): save with compressed rows, each
+ * action row as 16-bit codes plus one f32 scale (file version 3, or 4 with
+ * per-street configs), about half the size; pps_gb_load reads every
+ * version. Decoded entries are within half a code step of the saved ones. */
+int pps_gb_save_compressed(pps_gb_solver* h, const char* path);
 /* debugDump() - cuda/gpu_cfr.h:249. */
 int pps_gb_debug_dump(pps_gb_solver* h);
 

@@ -1,6 +1,7 @@
 """The reference's API invariants (python/test_pps.py:18-239) against this
 solver, through the same pps.Solver surface."""
 import os
+import struct
 import subprocess
 import tempfile
 
@@ -109,6 +110,50 @@ def test_save_load(tmp_path):
         pps.Solver.load(str(tmp_path / "trunc.sol"))
     with pytest.raises(RuntimeError):
         pps.Solver.load(str(tmp_path / "nonexistent.sol"))
+
+
+def test_save_load_compressed(tmp_path):
+    """Compressed solution files (16-bit codes, one f32 scale per action
+    row): about half the size, every entry within half a code step of its
+    row's scale, the loaded solution passes the EV / exploitability gates
+    against the saved one, and solving continues from it."""
+    s = fresh()
+    s.solve(300)
+    full, comp = str(tmp_path / "full.sol"), str(tmp_path / "comp.sol")
+    s.save(full)
+    s.save(comp, compressed=True)
+    assert os.path.getsize(comp) < 0.55 * os.path.getsize(full)
+    t = pps.Solver.load(comp)
+    assert t.num_nodes == s.num_nodes and t.total_iterations == 300
+    for which, q in ((0, 32767.0), (1, 65535.0)):
+        a = np.asarray(s.read_rows(which), dtype=np.float64)
+        b = np.asarray(t.read_rows(which), dtype=np.float64)
+        assert np.max(np.abs(a - b)) <= (0.5 / q + 1e-6) * np.max(np.abs(a))
+    sa, sb = s.stats(), t.stats()
+    close(sa["ev_oop"], sb["ev_oop"], 1e-2, "compressed EV")
+    assert abs(sa["exploitability"] - sb["exploitability"]) < 1e-2
+    s.continue_solve(200)
+    t.continue_solve(200)
+    assert t.total_iterations == 500
+    close(s.stats()["ev_oop"], t.stats()["ev_oop"], 1e-2, "continued EV")
+    raw = open(comp, "rb").read()
+    open(str(tmp_path / "trunc.sol"), "wb").write(raw[:-100])
+    with pytest.raises(RuntimeError, match="truncated"):
+        pps.Solver.load(str(tmp_path / "trunc.sol"))
+
+
+def test_save_load_compressed_per_street(tmp_path):
+    """Version 4: per-street bet configs with compressed rows."""
+    from helpers import solver as spot_solver
+    from pps import workloads as wl
+    s = spot_solver(wl.turn_c2())
+    s.solve(50)
+    path = str(tmp_path / "c2.sol")
+    s.save(path, compressed=True)
+    assert struct.unpack_from("<I", open(path, "rb").read(), 4)[0] == 4
+    t = pps.Solver.load(path)
+    assert t.num_nodes == s.num_nodes == 6333
+    close(s.stats()["ev_oop"], t.stats()["ev_oop"], 1e-2, "per-street compressed EV")
 
 
 def test_errors():
