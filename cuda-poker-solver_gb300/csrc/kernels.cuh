@@ -96,6 +96,24 @@ template <typename T>
 __device__ __forceinline__ T sigmaMass(T x, int sigSrc) {
   return sigSrc == 0 ? (x > T(0) ? x : T(0)) : x;
 }
+// The walks (T = double) normalize with one reciprocal per combo and a
+// product per action: an FP64 division is a multi-instruction sequence,
+// and GB300's FP64 pipe is what bounds the walks. The f32 iteration keeps
+// the reference's x / acc per action (sigmaScale is then unused).
+template <typename T>
+__device__ __forceinline__ T sigmaScale(T acc) {
+  if constexpr (sizeof(T) == 8) return acc > T(0) ? T(1) / acc : T(0);
+  else return acc;
+}
+template <typename T>
+__device__ __forceinline__ T sigmaOfScaled(T x, T acc, T scale, T uniform, int sigSrc) {
+  if constexpr (sizeof(T) == 8) {
+    if (!(acc > T(0))) return uniform;
+    return (sigSrc == 0 ? (x > T(0) ? x : T(0)) : x) * scale;
+  } else {
+    return sigmaOf(x, acc, uniform, sigSrc);
+  }
+}
 
 template <typename T>
 __device__ __forceinline__ T warpSum(T v) {
@@ -168,12 +186,15 @@ __device__ void fwdDecideChunk(const DevTree& t, const DevRows<T>& rows, int u, 
         ldqf(src + ((size_t)a * nq + q) * 4, x[a]);
         for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[a][l], sigSrc);
       }
+    T sc[4];
+    for (int l = 0; l < 4; ++l) sc[l] = sigmaScale(acc[l]);
 #pragma unroll
     for (int a = 0; a < kRegNa; ++a)
       if (a < na) {
         T out[4];
         for (int l = 0; l < 4; ++l)
-          out[l] = 4 * q + l < n ? rr[l] * sigmaOf(x[a][l], acc[l], uniform, sigSrc) : T(0);
+          out[l] = 4 * q + l < n ? rr[l] * sigmaOfScaled(x[a][l], acc[l], sc[l], uniform, sigSrc)
+                                 : T(0);
         stq(rows.reach[tr] + (size_t)t.rows[kids[a]].reachQ[tr] * 4 + 4 * q, out);
       }
     return;
@@ -183,11 +204,14 @@ __device__ void fwdDecideChunk(const DevTree& t, const DevRows<T>& rows, int u, 
     ldqf(src + ((size_t)a * nq + q) * 4, x);
     for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], sigSrc);
   }
+  T sc[4];
+  for (int l = 0; l < 4; ++l) sc[l] = sigmaScale(acc[l]);
   for (int a = 0; a < na; ++a) {
     T x[4], out[4];
     ldqf(src + ((size_t)a * nq + q) * 4, x);
     for (int l = 0; l < 4; ++l)
-      out[l] = 4 * q + l < n ? rr[l] * sigmaOf(x[l], acc[l], uniform, sigSrc) : T(0);
+      out[l] = 4 * q + l < n ? rr[l] * sigmaOfScaled(x[l], acc[l], sc[l], uniform, sigSrc)
+                             : T(0);
     stq(rows.reach[tr] + (size_t)t.rows[kids[a]].reachQ[tr] * 4 + 4 * q, out);
   }
 }
@@ -346,8 +370,23 @@ __device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, in
   }
   __syncthreads();
   // Compensated exclusive prefix of the block totals (nb <= 64: two blocks
-  // per lane of warp 0).
-  if (warp == 0) {
+  // per lane of warp 0). In FP64 (the walks) a plain prefix is exact enough
+  // and spares the FP64 pipe.
+  if (warp == 0 && sizeof(T) == 8) {
+    const int b0 = 2 * lane, b1 = b0 + 1;
+    const T t0 = b0 < nb ? ws.bh[b0] : T(0), t1 = b1 < nb ? ws.bh[b1] : T(0);
+    const T incl = warpInclScan(t0 + t1, lane);
+    T e = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) e = T(0);
+    if (b0 < nb) {
+      ws.bh[b0] = e;
+      ws.bl[b0] = T(0);
+    }
+    if (b1 < nb) {
+      ws.bh[b1] = e + t0;
+      ws.bl[b1] = T(0);
+    }
+  } else if (warp == 0) {
     const int b0 = 2 * lane, b1 = b0 + 1;
     const T t0 = b0 < nb ? ws.bh[b0] : T(0), t1 = b1 < nb ? ws.bh[b1] : T(0);
     T hi = t0, lo = T(0);
@@ -407,9 +446,17 @@ __device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, in
     const int same = (int)(f.z >> 16) - 1;
     const T sameR = same >= 0 ? ws.rs[same] : T(0);
     const int bl = le >> 5, bt = te >> 5;
-    const T below = ws.bh[bl] + (ws.bl[bl] + ws.sl[le]);
-    const T band = (ws.bh[bt] - ws.bh[bl]) + (ws.bl[bt] - ws.bl[bl]) + (ws.sl[te] - ws.sl[le]);
-    const T above = (ws.bh[bn] - ws.bh[bt]) + (ws.bl[bn] - ws.bl[bt]) + (ws.sl[no] - ws.sl[te]);
+    T below, band, above;
+    if constexpr (sizeof(T) == 8) {  // plain FP64 prefixes (bl is zero)
+      const T ple = ws.bh[bl] + ws.sl[le], pte = ws.bh[bt] + ws.sl[te];
+      below = ple;
+      band = pte - ple;
+      above = (ws.bh[bn] + ws.sl[no]) - pte;
+    } else {
+      below = ws.bh[bl] + (ws.bl[bl] + ws.sl[le]);
+      band = (ws.bh[bt] - ws.bh[bl]) + (ws.bl[bt] - ws.bl[bl]) + (ws.sl[te] - ws.sl[le]);
+      above = (ws.bh[bn] - ws.bh[bt]) + (ws.bl[bn] - ws.bl[bt]) + (ws.sl[no] - ws.sl[te]);
+    }
     T lm = below - x1le - x2le;
     T tm = band - (x1te - x1le) - (x2te - x2le) + sameR;
     T gm = above - (ws.X[a1 + len1] - x1te) - (ws.X[a2 + len2] - x2te);
@@ -579,11 +626,13 @@ __device__ void decideChunk(const DevTree& t, const DevRows<T>& rows, int u, int
         ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, cv[a]);
         for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[a][l], sigSrc);
       }
+    T sc[4];
+    for (int l = 0; l < 4; ++l) sc[l] = sigmaScale(acc[l]);
 #pragma unroll
     for (int a = 0; a < kRegNa; ++a)
       if (a < na)
         for (int l = 0; l < 4; ++l) {
-          x[a][l] = live[l] ? sigmaOf(x[a][l], acc[l], uniform, sigSrc) : T(0);
+          x[a][l] = live[l] ? sigmaOfScaled(x[a][l], acc[l], sc[l], uniform, sigSrc) : T(0);
           val[l] += x[a][l] * cv[a][l];
         }
     stq(out + 4 * q, val);
@@ -609,12 +658,14 @@ __device__ void decideChunk(const DevTree& t, const DevRows<T>& rows, int u, int
     ldqf(src + ((size_t)a * nq + q) * 4, x);
     for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], sigSrc);
   }
+  T sc[4];
+  for (int l = 0; l < 4; ++l) sc[l] = sigmaScale(acc[l]);
   for (int a = 0; a < na; ++a) {
     T x[4], c[4];
     ldqf(src + ((size_t)a * nq + q) * 4, x);
     ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, c);
     for (int l = 0; l < 4; ++l)
-      val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, sigSrc) : T(0)) * c[l];
+      val[l] += (live[l] ? sigmaOfScaled(x[l], acc[l], sc[l], uniform, sigSrc) : T(0)) * c[l];
   }
   stq(out + 4 * q, val);
   if (mode != kModeCFR) return;
