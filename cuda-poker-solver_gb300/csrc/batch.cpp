@@ -40,9 +40,9 @@ BatchServer::BatchServer(const BatchConfig& cfg) : cfg_(cfg), t0_(std::chrono::s
     throw Error{PPS_GB_E_ARG, "batch: algo must be a DCFR schedule (dcfr, dcfr-g2, "
                               "dcfr-noreset, dcfr-g2-noreset), got '" + cfg_.algo + "'"};
   if (cfg_.checkEvery <= 0) cfg_.checkEvery = 64;
+  cfg_.checkEvery = (cfg_.checkEvery + kCheckStep - 1) / kCheckStep * kCheckStep;
   if (cfg_.maxIterations <= 0) cfg_.maxIterations = 4096;
-  cfg_.maxIterations =
-      (cfg_.maxIterations + cfg_.checkEvery - 1) / cfg_.checkEvery * cfg_.checkEvery;
+  cfg_.maxIterations = (cfg_.maxIterations + kCheckStep - 1) / kCheckStep * kCheckStep;
   cudaCheck(cudaGetDevice(&device_), "cudaGetDevice");
   budget_ = cfg_.budget;
   if (budget_ <= 0) {
@@ -236,30 +236,55 @@ bool BatchServer::epoch() {
   }
   if (slots.empty()) return admitted;
 
-  F.iterate(cfg_.checkEvery);
-  const std::vector<double> br0 = F.walkValues(slots, 0, kModeBR);
-  const std::vector<double> br1 = F.walkValues(slots, 1, kModeBR);
+  // Iterate until the first resident spot is due (every count and due
+  // point is a multiple of kCheckStep, so no spot passes its check point).
+  const int first = cfg_.fixedChecks ? cfg_.checkEvery : std::min(32, cfg_.checkEvery);
+  int n = cfg_.maxIterations;
+  for (int slot : slots) {
+    auto it = nextCheck_.find(slot);
+    if (it == nextCheck_.end()) it = nextCheck_.emplace(slot, first).first;
+    it->second = std::min(it->second, cfg_.maxIterations);
+    n = std::min(n, it->second - F.iterations(slot));
+  }
+  n = std::max(n, kCheckStep);
+  F.iterate(n);
+  std::vector<int> due;
+  for (int slot : slots)
+    if (F.iterations(slot) >= nextCheck_.at(slot)) due.push_back(slot);
+  const std::vector<double> br0 = F.walkValues(due, 0, kModeBR);
+  const std::vector<double> br1 = F.walkValues(due, 1, kModeBR);
   std::vector<int> done;
   std::vector<double> doneExpl;
-  for (size_t i = 0; i < slots.size(); ++i) {
-    const CompiledSpot& cs = F.spot(slots[i]);
+  for (size_t i = 0; i < due.size(); ++i) {
+    const int slot = due[i];
+    const CompiledSpot& cs = F.spot(slot);
     const double expl = (br0[i] + br1[i] - (double)cs.tree.spot.pot) / 2.0;
     double target;
     {
       std::lock_guard<std::mutex> lock(m_);
-      target = reqs_.at(slotTicket_.at(slots[i])).target;
+      target = reqs_.at(slotTicket_.at(slot)).target;
     }
-    if ((target > 0.0 && expl <= target) || F.iterations(slots[i]) >= cfg_.maxIterations) {
-      done.push_back(slots[i]);
+    const int t = F.iterations(slot);
+    if ((target > 0.0 && expl <= target) || t >= cfg_.maxIterations) {
+      done.push_back(slot);
       doneExpl.push_back(expl);
+      continue;
     }
+    int step = cfg_.checkEvery;
+    if (!cfg_.fixedChecks && target > 0.0 && expl > 0.0) {
+      const double want = (double)t * std::sqrt(expl / target) - (double)t;
+      const int s = (int)std::ceil(std::max(want, 1.0) / kCheckStep) * kCheckStep;
+      step = std::min(cfg_.checkEvery, std::max(kCheckStep, s));
+    }
+    nextCheck_[slot] = t + step;
   }
   const double tChecked = nowMs();
   const double iterMs = F.lastIterateMs();
   {
     std::lock_guard<std::mutex> lock(m_);
     ++stats_.epochs;
-    stats_.spotIterations += (int64_t)slots.size() * cfg_.checkEvery;
+    stats_.spotIterations += (int64_t)slots.size() * n;
+    stats_.checks += (int64_t)due.size();
     stats_.captures = F.captures();
     stats_.iterateMs += iterMs;
     stats_.checkMs += tChecked - tAdmitted;
@@ -296,6 +321,7 @@ bool BatchServer::epoch() {
                              t.actions.begin() + root.actBase + root.na);
     }
     F.retire(slot);
+    nextCheck_.erase(slot);
     res.finishMs = nowMs();
     {
       std::lock_guard<std::mutex> lock(m_);

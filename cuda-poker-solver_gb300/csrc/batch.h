@@ -4,15 +4,23 @@
 // in ticket order and are admitted into the forest while the device memory
 // the forest maps stays within the HBM budget. A driver
 // (run() on the caller's thread, or the thread start() launches) repeats
-// epochs: admit, run `checkEvery` DCFR iterations of every resident spot
-// in one graph, run the FP64 best-response walks, and retire each spot
-// whose exploitability reached its target (or whose iteration cap was
-// reached) after its FP64 EV walks. Spots admitted while others are
-// resident share the same launches, so work of requests that arrive at
-// different times overlaps on the device. Every spot is checked at
-// multiples of `checkEvery` iterations from its admission and its rows
-// depend on nothing but its own inputs, so a result does not depend on
-// which other spots were resident.
+// epochs: admit, run DCFR iterations of every resident spot in one graph
+// until the next spot is due for a check, run the FP64 best-response walks
+// of the spots that are due, and retire each spot whose exploitability
+// reached its target (or whose iteration cap was reached) after its FP64
+// EV walks. Spots admitted while others are resident share the same
+// launches, so work of requests that arrive at different times overlaps on
+// the device.
+//
+// Check schedule (per spot, counted from its admission, in steps of
+// kCheckStep iterations). Adaptive (default): the first check after
+// min(32, checkEvery) iterations; after a check at t with exploitability e
+// above the target, the next one where e ~ 1/t^2 would meet the target,
+// t * sqrt(e / target), but at least kCheckStep and at most checkEvery
+// iterations later. Fixed: every checkEvery iterations. A spot's schedule
+// depends only on its own exploitability values, and its rows on nothing
+// but its own inputs, so a result does not depend on which other spots
+// were resident.
 #pragma once
 
 #include <atomic>
@@ -33,10 +41,13 @@
 namespace pps {
 namespace gb {
 
+constexpr int kCheckStep = 16;  // check granularity (iterations)
+
 struct BatchConfig {
   int64_t budget = 0;        // device bytes for resident spots (0: 80% of free memory)
-  int checkEvery = 64;       // iterations between exploitability checks
-  int maxIterations = 4096;  // per spot, rounded up to a multiple of checkEvery
+  int checkEvery = 64;       // most iterations between two checks of a spot
+  bool fixedChecks = false;  // check every checkEvery iterations (no prediction)
+  int maxIterations = 4096;  // per spot, rounded up to a multiple of kCheckStep
   int threads = 0;           // compile threads (0: hardware threads, at most 16)
   std::string algo = "dcfr";
 };
@@ -63,6 +74,7 @@ struct BatchInfo {
   int64_t usedBytes = 0, deviceBytes = 0, budget = 0;
   int64_t epochs = 0, spotIterations = 0, captures = 0, peakActive = 0, peakUsed = 0;
   int checkEvery = 0, maxIterations = 0;
+  int64_t checks = 0;  // spot checks (best-response walk pairs per spot)
   double admitMs = 0.0, iterateMs = 0.0, checkMs = 0.0, retireMs = 0.0, idleMs = 0.0;
 };
 
@@ -113,6 +125,7 @@ class BatchServer {
   size_t compileHead_ = 0;
   std::map<int64_t, std::unique_ptr<CompiledSpot>> ready_;
   std::map<int, int64_t> slotTicket_;
+  std::map<int, int> nextCheck_;  // slot -> iteration count of its next check
   int64_t nextTicket_ = 1;
   int64_t budget_ = 0;
   int64_t pending_ = 0;  // submitted, not finished

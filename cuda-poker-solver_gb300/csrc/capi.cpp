@@ -493,6 +493,7 @@ void pps_gb_batch_config_default(pps_gb_batch_config* cfg) {
   const pps::gb::BatchConfig d;
   cfg->hbm_budget = d.budget;
   cfg->check_every = d.checkEvery;
+  cfg->fixed_checks = d.fixedChecks ? 1 : 0;
   cfg->max_iterations = d.maxIterations;
   cfg->compile_threads = d.threads;
   std::strncpy(cfg->algo, d.algo.c_str(), sizeof(cfg->algo) - 1);
@@ -506,6 +507,7 @@ int pps_gb_batch_create(const pps_gb_batch_config* cfg, pps_gb_batch** out) {
     if (cfg) {
       c.budget = cfg->hbm_budget;
       c.checkEvery = cfg->check_every;
+      c.fixedChecks = cfg->fixed_checks != 0;
       c.maxIterations = cfg->max_iterations;
       c.threads = cfg->compile_threads;
       const size_t n = strnlen(cfg->algo, sizeof(cfg->algo));

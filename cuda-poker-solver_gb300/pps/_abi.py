@@ -64,8 +64,8 @@ class DecideInfo(C.Structure):
 
 class BatchConfig(C.Structure):
     _fields_ = [("hbm_budget", C.c_int64), ("check_every", C.c_int32),
-                ("max_iterations", C.c_int32), ("compile_threads", C.c_int32),
-                ("algo", C.c_char * 16)]
+                ("fixed_checks", C.c_int32), ("max_iterations", C.c_int32),
+                ("compile_threads", C.c_int32), ("algo", C.c_char * 16)]
 
 
 class BatchResult(C.Structure):

@@ -15,8 +15,11 @@ retired one by one once their FP64 exploitability check reaches the target.
     r = b.result(t)              # {"ev_oop", "ev_ip", "exploitability", ...}
 
 A result does not depend on which other spots shared the device: each spot
-runs the same kernels on its own rows and is checked every ``check_every``
-iterations from its admission.
+runs the same kernels on its own rows, and its checks (first after
+min(32, check_every) iterations, then where its exploitability, taken as
+falling like 1/t^2, would meet the target, at most ``check_every`` apart,
+in steps of 16; every ``check_every`` with ``fixed_checks=True``) depend on
+its own exploitability values only.
 """
 from __future__ import annotations
 
@@ -65,11 +68,12 @@ class Batch:
     """Batched / served DCFR solving on the current CUDA device."""
 
     def __init__(self, hbm_budget: int = 0, check_every: int = 64, max_iterations: int = 4096,
-                 compile_threads: int = 0, algo: str = "dcfr"):
+                 compile_threads: int = 0, algo: str = "dcfr", fixed_checks: bool = False):
         cfg = _abi.BatchConfig()
         lib.pps_gb_batch_config_default(C.byref(cfg))
         cfg.hbm_budget = int(hbm_budget)
         cfg.check_every = int(check_every)
+        cfg.fixed_checks = 1 if fixed_checks else 0
         cfg.max_iterations = int(max_iterations)
         cfg.compile_threads = int(compile_threads)
         cfg.algo = algo.encode()

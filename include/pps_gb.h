@@ -293,8 +293,12 @@ typedef struct pps_gb_batch pps_gb_batch;
 
 typedef struct {
   int64_t hbm_budget;      /* device bytes resident spots may occupy (0: 80% of free) */
-  int32_t check_every;     /* DCFR iterations between checks (0: 64) */
-  int32_t max_iterations;  /* per spot, rounded up to a multiple of check_every (0: 4096) */
+  int32_t check_every;     /* most DCFR iterations between two checks of a spot (0: 64) */
+  int32_t fixed_checks;    /* 1: check every check_every iterations; 0 (default):
+                              adaptive, first check after min(32, check_every), the
+                              next where exploitability ~ 1/t^2 would meet the target,
+                              in steps of 16 iterations */
+  int32_t max_iterations;  /* per spot, rounded up to a multiple of 16 (0: 4096) */
   int32_t compile_threads; /* host compile threads (0: hardware threads, at most 16) */
   char algo[16];           /* "dcfr" (default), "dcfr-g2", "dcfr-noreset", "dcfr-g2-noreset" */
 } pps_gb_batch_config;

@@ -9,7 +9,7 @@ Gates:
 * a batch result equals a lone Solver run for the same number of
   iterations (same tolerances);
 * every converged result is at or below its target, checked at multiples
-  of check_every;
+  of 16 iterations (adaptive schedule) or of check_every (fixed schedule);
 * EVs of river spots are within 0.01 chips of the FP64 CPU oracle run for
   the same iterations;
 * served mode overlaps requests submitted at different times, and an HBM
@@ -93,10 +93,24 @@ def test_batch_converges_to_target(mixed):
     assert info["peak_active"] >= 2  # spots shared the device
     for sp, r in zip(spots, res):
         assert r["status"] == 0, r["error"]
-        assert r["iterations"] % CHECK == 0
+        assert r["iterations"] % 16 == 0
         assert r["converged"], (sp.name, r["exploitability"], r["target"])
         assert r["exploitability"] <= 0.005 * sp.pot + 1e-12
         assert abs(sum(r["root_freqs"]) - 1.0) < 1e-6
+
+
+def test_fixed_check_schedule():
+    """fixed_checks: every spot is checked (and retired) at multiples of
+    check_every. The adaptive default checks at most check_every apart, so
+    it retires a spot within check_every iterations after the fixed
+    schedule's passing check (exploitability falls between the two)."""
+    spots = _spots()[:6]
+    fixed, _, _ = _solve_batch(spots, fixed_checks=True)
+    adaptive, _, _ = _solve_batch(spots)
+    for sp, f, a in zip(spots, fixed, adaptive):
+        assert f["converged"] and f["iterations"] % CHECK == 0, sp.name
+        assert a["converged"] and a["iterations"] % 16 == 0, sp.name
+        assert a["iterations"] <= f["iterations"] + CHECK, (sp.name, a["iterations"], f["iterations"])
 
 
 def test_result_same_alone_and_in_the_mix(mixed):
