@@ -182,24 +182,36 @@ fwdDecideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
 __device__ __forceinline__ void pdlTrigger() { asm volatile("griddepcontrol.launch_dependents;"); }
 __device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// late: each CTA lets the next grid launch only once its own wait has
+// returned (so a grid that has launched implies that the grid two places
+// before it has completed; the fused plan relies on that), instead of at
+// its start.
 static __global__ void __launch_bounds__(kThreads, 12)
 fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
              const uint32_t* __restrict__ recTasks, int nRec, const int* __restrict__ chance,
-             int nCh, int tr) {
-  pdlTrigger();
+             int nCh, int tr, int late) {
+  if (!late) pdlTrigger();
   const int nRc = recordCtas(nRec), lane = (int)threadIdx.x & 31;
+  bool waited = false;
   for (int i = blockIdx.x; i < nRc + nCh; i += gridDim.x) {
     if (i < nRc) {
       const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
       if (k >= nRec) continue;
       const DecRec r = loadRec(recs, recTasks[k]);
       pdlWait();
+      waited = true;
       fwdDecideRecord(t, rows, tr, r, lane);
     } else {
       const int w = chance[i - nRc];
       pdlWait();
+      waited = true;
       fwdChanceBranch<float>(t, rows, (int)((unsigned)w >> 8), (w >> 2) & 63, tr);
     }
+    if (late) pdlTrigger();
+  }
+  if (late && !waited) {  // an idle warp of a record CTA
+    pdlWait();
+    pdlTrigger();
   }
 }
 

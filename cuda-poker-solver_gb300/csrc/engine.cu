@@ -68,7 +68,7 @@ struct Engine::Dev {
   int4* groups = nullptr;
   uint32_t* recs = nullptr;
   uint32_t* recTasks = nullptr;
-  std::vector<Launch> plan[2];  // per engine kind: one iteration (kind 0 flattened)
+  std::vector<Launch> plan[3];  // per engine kind: one iteration (kind 0 flattened)
   StagedPlan staged;           // kind 0 as captured
   StagedEvents sev;
   bool walkReady = false;
@@ -317,6 +317,35 @@ void Engine::buildPlans() {
     }
   }
   P.push_back({kCounter, 0, ListRef{}, 0.0});
+  // Kind 2 (narrow ranges): the staged plan's forward levels, then one
+  // fused launch per backward level (records, chance, showdown and fold
+  // groups of that depth), all on one stream.
+  std::vector<Launch>& F = d.plan[2];
+  F.clear();
+  if (d.maxN <= kFusedMaxN) {
+    for (int tr = 0; tr < 2; ++tr) {
+      const HalfStep& h = d.staged.half[tr];
+      for (int dd = 0; dd < D; ++dd)
+        for (Launch l : h.fwd[dd]) {
+          l.late = true;
+          F.push_back(l);
+        }
+      bool first = true;
+      for (int dd = D - 1; dd >= 0; --dd) {
+        Launch l{kBwdFused, tr, d.bRec[tr][dd], 0.0};
+        l.termWait = first;
+        l.list2 = d.bCh[tr][dd];
+        l.list3 = d.sdG[dd];
+        l.list4 = d.fdG[dd];
+        if (!l.list.count && !l.list2.count && !l.list3.count && !l.list4.count) continue;
+        for (const Launch& b : h.bwd[dd]) l.bytes += b.bytes;
+        l.bytes += h.sd[dd].bytes + h.fd[dd].bytes;
+        F.push_back(l);
+        first = false;
+      }
+    }
+    F.push_back({kCounter, 0, ListRef{}, 0.0});
+  }
 }
 
 void Engine::zeroRows() {
@@ -390,10 +419,37 @@ void Engine::capture() {
 }
 
 void Engine::setEngineKind(int kind) {
-  const int k = kind == 1 ? 1 : 0;
+  if (kind == 2 && d_->plan[2].empty())
+    throw Error{PPS_GB_E_ARG, "engine 2 (fused levels) needs lists of at most " +
+                                  std::to_string(kFusedMaxN) + " combos"};
+  tuned_ = true;
+  const int k = kind == 1 || kind == 2 ? kind : 0;
   if (k == engineKind_ && d_->exec) return;
   engineKind_ = k;
   capture();
+}
+
+void Engine::autotune() {
+  if (tuned_) return;
+  tuned_ = true;
+  if (d_->plan[2].empty()) return;
+  double best = 0.0;
+  int bestKind = 0;
+  for (int k : {0, 2}) {
+    engineKind_ = k;
+    capture();
+    iterate(2);  // warm-up
+    const double ms = timeIterations(6);
+    if (k == 0 || ms < best) {
+      best = ms;
+      bestKind = k;
+    }
+  }
+  if (bestKind != engineKind_) {
+    engineKind_ = bestKind;
+    capture();
+  }
+  zeroRows();
 }
 
 void Engine::iterate(int n) {

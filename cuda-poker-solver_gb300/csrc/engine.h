@@ -66,6 +66,11 @@ class Engine {
   // nodes of one level and board state (default); 1 = one CTA per node.
   // Recaptures on change.
   void setEngineKind(int kind);
+  // Picks the faster of the staged (0) and fused (2) plans for this tree by
+  // timing a few graph replays of each, then zeroes the rows and the
+  // counter (both plans compute identical rows). A no-op once tuned, after
+  // setEngineKind, and where the fused plan does not apply.
+  void autotune();
   int engineKind() const { return engineKind_; }
   int launchesPerIteration() const { return launchesPerIter_; }
   size_t deviceBytes() const { return deviceBytes_; }
@@ -79,6 +84,7 @@ class Engine {
   HostLayout L_;
   std::unique_ptr<Dev> d_;
   int engineKind_ = 0;
+  bool tuned_ = false;
   int launchesPerIter_ = 0;
   size_t deviceBytes_ = 0;
   mutable int64_t h2d_ = 0, d2h_ = 0;

@@ -34,11 +34,11 @@ struct ListRef {
 };
 
 enum LaunchKind { kFwd, kBwdTerm, kBwdInt, kSdGroup, kFdGroup, kDecRec, kFwdRec, kFwdMix,
-                  kBwdMix, kCounter };
+                  kBwdMix, kCounter, kBwdFused };
 inline const char* launchName(LaunchKind k) {
   static const char* names[] = {"fwd_level",  "bwd_terminal", "bwd_interior", "bwd_showdown",
                                 "bwd_fold",   "bwd_decide",   "fwd_decide",   "fwd_level",
-                                "bwd_interior", "counter"};
+                                "bwd_interior", "counter",    "bwd_level"};
   return names[k];
 }
 
@@ -48,7 +48,10 @@ struct Launch {
   ListRef list;
   double bytes;           // algorithmic bytes of this launch (f32 rows)
   bool withNext = false;  // independent of the next launch: run both at once
-  ListRef list2{};        // kFwdMix / kBwdMix: the chance words (list: records)
+  ListRef list2{};        // kFwdMix / kBwdMix / kBwdFused: the chance words (list: records)
+  ListRef list3{}, list4{};  // kBwdFused: the showdown and fold group tasks
+  bool late = false;      // kFwdMix: late triggers (the fused plan)
+  bool termWait = false;  // kBwdFused: its terminal groups wait for the previous grid
 };
 
 // What the level launches of a plan read: the tree, the f32 rows, the
@@ -101,6 +104,25 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       fwdDecideRecK<<<gridOf(recordCtas(l.list.count)), kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
                                            l.list.count, l.tr);
       break;
+    case kBwdFused: {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(gridOf(recordCtas(l.list.count) + l.list2.count + l.list3.count +
+                                l.list4.count));
+      cfg.blockDim = dim3(kThreads);
+      cfg.dynamicSmemBytes = fusedLevelSmem(a.maxN);
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      attr[0].val.programmaticStreamSerializationAllowed = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      GB_CK(cudaLaunchKernelEx(&cfg, bwdLevelFusedK, a.tree, a.rows, a.recs,
+                               a.recTasks + l.list.off, l.list.count, a.tasks + l.list2.off,
+                               l.list2.count, a.groups, a.tasks + l.list3.off, l.list3.count,
+                               a.tasks + l.list4.off, l.list4.count, l.tr, a.maxN,
+                               l.termWait ? 1 : 0));
+      break;
+    }
     case kFwdMix:
     case kBwdMix: {
       // Programmatic dependent launch: the grid may start while the
@@ -120,7 +142,7 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       const int* ch = a.tasks + l.list2.off;
       if (l.kind == kFwdMix)
         GB_CK(cudaLaunchKernelEx(&cfg, fwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
-                                 ch, l.list2.count, l.tr));
+                                 ch, l.list2.count, l.tr, l.late ? 1 : 0));
       else
         GB_CK(cudaLaunchKernelEx(&cfg, bwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
                                  ch, l.list2.count, l.tr));

@@ -118,6 +118,7 @@ void SolverCore::solve(int iterations, const std::string& algo, double target) {
     for (int k = 0; k < 3; ++k) tab[(size_t)t * 3 + k] = (float)c[k];
   }
   eng_->setSchedule(tab, 0);
+  if (iterations >= 32) eng_->autotune();
   replayChunks(iterations, target);
 }
 

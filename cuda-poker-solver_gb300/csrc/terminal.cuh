@@ -18,6 +18,7 @@
 //     of the 52 card sums (each combo holds two cards).
 #pragma once
 
+#include "decide.cuh"
 #include "kernels.cuh"
 
 namespace pps {
@@ -385,6 +386,76 @@ fdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
   }
 }
 
+// Backward level of the fused plan (engine kind 2, narrow ranges: lists of
+// up to 1023 combos): one launch per level covers the level's decide
+// records (four per CTA), chance tasks, showdown groups and fold groups,
+// chained to the previous level by programmatic dependent launch, so the
+// iteration runs on one stream with no cross-stream joins. The group CTAs
+// have kThreads (128) threads. Dynamic shared memory: fusedLevelSmem(maxN).
+//
+// Every kernel of the fused plan lets the next grid launch only after its
+// own wait has returned ("late" triggers), so a grid that has launched
+// implies that the grid two places before it has completed. Terminal
+// groups read only reach rows, written by the forward pass, and write
+// value rows that nothing in the previous grid touches; so, except in the
+// first backward launch of a half-step (termWait: its reach rows come from
+// the grid just before), they start without waiting and run under the
+// previous level's tail. They wait as well where the launch has no record
+// or chance CTA, so that the late-trigger chain is never broken.
+__host__ __device__ inline size_t fusedLevelSmem(int maxN) {
+  size_t s = sdGroupSmem(maxN);
+  if (fdGroupSmem(maxN) > s) s = fdGroupSmem(maxN);
+  return s > kChanceScratchBytes ? s : kChanceScratchBytes;
+}
+constexpr int kFusedMaxN = kSpan * kThreads - 1;  // widest list of a 128-thread group
+
+static __global__ void __launch_bounds__(kThreads, 6)
+bwdLevelFusedK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
+               const uint32_t* __restrict__ recTasks, int nRec, const int* __restrict__ chance,
+               int nCh, const int4* __restrict__ groups, const int* __restrict__ sd, int nSd,
+               const int* __restrict__ fd, int nFd, int tr, int maxN, int termWait) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = (int)threadIdx.x & 31;
+  const int e1 = recordCtas(nRec), e2 = e1 + nCh, e3 = e2 + nSd, e4 = e3 + nFd;
+  const bool groupsWait = termWait || e2 == 0;
+  bool waited = false;
+  for (int i = blockIdx.x; i < e4; i += gridDim.x) {
+    if (i < e1) {
+      const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
+      if (k < nRec) {
+        const DecRec r = loadRec(recs, recTasks[k]);
+        pdlWait();
+        waited = true;
+        decideRecord(t, rows, r, lane);
+      }
+    } else if (i < e2) {
+      const int w = chance[i - e1];
+      pdlWait();
+      waited = true;
+      chanceChunk<float>(t, rows, (int)((unsigned)w >> 8), (w >> 2) & 63, tr, smem);
+      __syncthreads();  // the next task reuses the shared memory
+    } else {
+      const bool show = i < e3;
+      const int4 g = groups[(unsigned)(show ? sd[i - e2] : fd[i - e3]) >> 8];
+      const int u[4] = {g.x, g.y, g.z, g.w};
+      if (groupsWait) {
+        pdlWait();
+        waited = true;
+      }
+      pdlTrigger();
+      if (show) showdownGroup(t, rows, u, tr, smem, maxN);
+      else foldGroup(t, rows, u, tr, smem, maxN);
+      __syncthreads();
+      continue;
+    }
+    if (waited) pdlTrigger();
+  }
+  if (!waited) {  // idle warps of a record CTA
+    pdlWait();
+    pdlTrigger();
+  }
+}
+
 void raiseSmemLimit(const void* kernel, size_t bytes);
 
 // Launches one level's showdown (fold) groups with the CTA size of maxN.
@@ -420,6 +491,7 @@ static inline void raiseGroupSmem(int maxN) {
   raiseSmemLimit((const void*)fdGroupK<64>, fd);
   raiseSmemLimit((const void*)fdGroupK<128>, fd);
   raiseSmemLimit((const void*)fdGroupK<kTermThreads>, fd);
+  if (maxN <= kFusedMaxN) raiseSmemLimit((const void*)bwdLevelFusedK, fusedLevelSmem(maxN));
 }
 
 }  // namespace gb

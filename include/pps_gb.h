@@ -222,10 +222,14 @@ int pps_gb_write_rows(pps_gb_solver* h, int which, const float* in,
  * *value the range-weighted root value in chips. */
 int pps_gb_walk(pps_gb_solver* h, int traverser, int mode, double* root_cfv,
                 double* value);
-/* Extension: backward terminal kernels of the CFR graph. 0 (default) =
- * showdown and fold nodes of one level and board state in groups of four
- * (one CTA each, float4 lanes); 1 = one CTA per terminal node. Both follow
- * the same formulas; rows agree to f32 rounding. */
+/* Extension: the iteration graph's plan. 0 = staged: decide records and
+ * chance tasks per level, showdown and fold nodes of one level and board
+ * state in groups of four (one CTA each, float4 lanes) on side streams; 1 =
+ * one CTA per terminal node; 2 = fused (lists of at most 1023 combos): one
+ * launch per backward level for all its tasks, on one stream. 0 and 2
+ * compute identical rows, 1 agrees to f32 rounding. By default the first
+ * solve of 32 or more iterations times 0 and 2 on the tree and keeps the
+ * faster; setting an engine turns that off. */
 int pps_gb_set_engine(pps_gb_solver* h, int engine);
 
 /* Benchmark helper: enqueues n further DCFR iterations (graph replays that

@@ -171,3 +171,31 @@ def test_flop_164k_rows_match_oracle():
         g, r = s.read_rows(which), o64.rows(which)
         scale = max(float(np.max(np.abs(r))), 1e-30)
         assert float(np.max(np.abs(g.astype(np.float64) - r))) / scale <= 5e-5
+
+
+@pytest.mark.parametrize("name", ["turn_api", "turn_short", "flop_short", "turn_w52"])
+def test_fused_plan_matches_staged_plan(name):
+    """Engine 2 (one fused launch per backward level) runs the same record
+    and group arithmetic as engine 0 in another launch order: the rows are
+    bitwise identical after 1 and 50 iterations. The default (autotuned)
+    solver picks one of the two and matches as well."""
+    spot = wl.NAMED[name]()
+    for iters in (1, 50):
+        a, b, c = solver(spot), solver(spot), solver(spot)
+        a.set_engine(0)
+        b.set_engine(2)
+        a.solve(iters)
+        b.solve(iters)
+        c.solve(iters)
+        assert a.info().engine == 0 and b.info().engine == 2
+        assert c.info().engine in (0, 2)
+        for which in (0, 1):
+            ra = a.read_rows(which)
+            assert np.array_equal(ra, b.read_rows(which)), (name, iters, which)
+            assert np.array_equal(ra, c.read_rows(which)), (name, iters, which)
+
+
+def test_fused_plan_refused_for_wide_lists():
+    s = solver(wl.turn_c2(uniform_config=True))
+    with pytest.raises(RuntimeError, match="engine 2"):
+        s.set_engine(2)
