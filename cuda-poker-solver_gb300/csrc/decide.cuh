@@ -142,6 +142,146 @@ __device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<
   }
 }
 
+// ---------------------------------------------------------------------------
+// Staged records: every row quad a thread needs (the children's value
+// quads, and for the traverser's own node its regret and strategy quads;
+// forward: its reach quad and regret quads) is requested at once with
+// cp.async into shared memory, so a record costs one memory round trip
+// instead of three dependent ones, and the data in flight holds no
+// registers. Each thread reads back only what it copied (cp.async.wait_group
+// waits for the thread's own copies: nothing to spin on). Records with more
+// than kAsyncNa actions (8% of C3's row bytes) use the streaming form.
+// Layout: [row kind][action][thread] float4, conflict-free.
+// ---------------------------------------------------------------------------
+constexpr int kAsyncNa = 4;
+__host__ __device__ constexpr size_t recStageBytes() {
+  return (size_t)3 * kAsyncNa * kThreads * sizeof(float4);
+}
+
+__device__ __forceinline__ void cpAsync16(float4* smem, const float* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpAsyncWaitAll() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+__device__ __forceinline__ void ld4s(const float4* p, float (&x)[4]) {
+  const float4 v = *p;
+  x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+
+// Backward decide record, staged (same arithmetic and order as
+// decideRecord).
+__device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRows<float>& rows,
+                                                   const DecRec& r, int lane, float4* stage) {
+  const int na = r.na;
+  if (na > kAsyncNa) {
+    decideRecord(t, rows, r, lane);
+    return;
+  }
+  const int nq = quadsOf(r.n);
+  const int q = r.chunk * kRecQuads + lane;
+  if (q >= nq) return;
+  const int tid = (int)threadIdx.x;
+  float4* C = stage;
+  float4* R = stage + kAsyncNa * kThreads;
+  float4* S = R + kAsyncNa * kThreads;
+  for (int a = 0; a < na; ++a)
+    cpAsync16(&C[a * kThreads + tid], rows.cfv + (size_t)r.kid[a] * 4 + 4 * q);
+  float* out = rows.cfv + (size_t)r.rowQ * 4;
+  bool live[4];
+  for (int l = 0; l < 4; ++l) live[l] = 4 * q + l < r.n;
+  if (!r.own) {
+    cpAsyncWaitAll();
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int a = 0; a < na; ++a) {
+      float c[4];
+      ld4s(&C[a * kThreads + tid], c);
+      for (int l = 0; l < 4; ++l) v[l] += c[l];
+    }
+    for (int l = 0; l < 4; ++l)
+      if (!live[l]) v[l] = 0.f;
+    stq(out + 4 * q, v);
+    return;
+  }
+  float* reg = t.regret + (size_t)r.regQ * 4;
+  float* str = t.strat + (size_t)r.regQ * 4;
+  for (int a = 0; a < na; ++a) {
+    const size_t o = ((size_t)a * nq + q) * 4;
+    cpAsync16(&R[a * kThreads + tid], reg + o);
+    cpAsync16(&S[a * kThreads + tid], str + o);
+  }
+  const float* c3 = t.coef + (size_t)t.counter[r.spot] * 3;
+  const float pos = c3[0], neg = c3[1], avg = c3[2];
+  const float uniform = 1.f / (float)na;
+  float val[4] = {0.f, 0.f, 0.f, 0.f}, acc[4] = {0.f, 0.f, 0.f, 0.f};
+  cpAsyncWaitAll();
+  for (int a = 0; a < na; ++a) {
+    float x[4];
+    ld4s(&R[a * kThreads + tid], x);
+    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
+  }
+  for (int a = 0; a < na; ++a) {
+    float x[4], c[4];
+    ld4s(&R[a * kThreads + tid], x);
+    ld4s(&C[a * kThreads + tid], c);
+    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, 0) : 0.f) * c[l];
+  }
+  stq(out + 4 * q, val);
+  for (int a = 0; a < na; ++a) {
+    float rg[4], sg[4], c[4];
+    const size_t o = ((size_t)a * nq + q) * 4;
+    ld4s(&R[a * kThreads + tid], rg);
+    ld4s(&S[a * kThreads + tid], sg);
+    ld4s(&C[a * kThreads + tid], c);
+    for (int l = 0; l < 4; ++l) {
+      const float s = live[l] ? sigmaOf(rg[l], acc[l], uniform, 0) : 0.f;
+      sg[l] = sg[l] * avg + s;
+      rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
+    }
+    stq(str + o, sg);
+    stq(reg + o, rg);
+  }
+}
+
+// Forward decide record, staged (same arithmetic and order as
+// fwdDecideRecord).
+__device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const DevRows<float>& rows,
+                                                      int tr, const DecRec& r, int lane,
+                                                      float4* stage) {
+  const int na = r.na;
+  if (na > kAsyncNa) {
+    fwdDecideRecord(t, rows, tr, r, lane);
+    return;
+  }
+  const int nq = quadsOf(r.n);
+  const int q = r.chunk * kRecQuads + lane;
+  if (q >= nq) return;
+  const int tid = (int)threadIdx.x;
+  float4* RR = stage;                     // [thread]
+  float4* R = stage + kThreads;           // [action][thread]
+  const float* src = t.regret + (size_t)r.regQ * 4;
+  cpAsync16(&RR[tid], rows.reach[tr] + (size_t)r.rowQ * 4 + 4 * q);
+  for (int a = 0; a < na; ++a)
+    cpAsync16(&R[a * kThreads + tid], src + ((size_t)a * nq + q) * 4);
+  const float uniform = 1.f / (float)na;
+  float rr[4], acc[4] = {0.f, 0.f, 0.f, 0.f};
+  cpAsyncWaitAll();
+  ld4s(&RR[tid], rr);
+  for (int a = 0; a < na; ++a) {
+    float x[4];
+    ld4s(&R[a * kThreads + tid], x);
+    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
+  }
+  for (int a = 0; a < na; ++a) {
+    float x[4], o[4];
+    ld4s(&R[a * kThreads + tid], x);
+    for (int l = 0; l < 4; ++l)
+      o[l] = 4 * q + l < r.n ? rr[l] * sigmaOf(x[l], acc[l], uniform, 0) : 0.f;
+    stq(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q, o);
+  }
+}
+
 // One warp per record (kRecWarps records per CTA), one kernel per pass.
 // A warp's records are independent of its CTA's other warps: no barrier.
 // Internal linkage: included by more than one translation unit.
@@ -150,22 +290,35 @@ __host__ __device__ inline int recordCtas(int records) {
   return (records + kRecWarps - 1) / kRecWarps;
 }
 
-static __global__ void __launch_bounds__(kThreads, 12)
-decideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
-           const uint32_t* __restrict__ tasks, int count) {
-  const int lane = (int)threadIdx.x & 31;
-  for (int i = blockIdx.x * kRecWarps + (int)(threadIdx.x >> 5); i < count;
-       i += gridDim.x * kRecWarps)
-    decideRecord(t, rows, loadRec(recs, tasks[i]), lane);
+// Dynamic shared memory of the record kernels: the staging buffers
+// (forward: one reach quad and kAsyncNa regret quads per thread).
+__host__ __device__ constexpr size_t fwdStageBytes() {
+  return (size_t)(1 + kAsyncNa) * kThreads * sizeof(float4);
+}
+__host__ __device__ constexpr size_t bwdStageBytes() {
+  return recStageBytes() > kChanceScratchBytes ? recStageBytes() : kChanceScratchBytes;
 }
 
-static __global__ void __launch_bounds__(kThreads, 12)
-fwdDecideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
-              const uint32_t* __restrict__ tasks, int count, int tr) {
+static __global__ void __launch_bounds__(kThreads, 8)
+decideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
+           const uint32_t* __restrict__ tasks, int count) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* stage = reinterpret_cast<float4*>(smem);
   const int lane = (int)threadIdx.x & 31;
   for (int i = blockIdx.x * kRecWarps + (int)(threadIdx.x >> 5); i < count;
        i += gridDim.x * kRecWarps)
-    fwdDecideRecord(t, rows, tr, loadRec(recs, tasks[i]), lane);
+    decideRecordStaged(t, rows, loadRec(recs, tasks[i]), lane, stage);
+}
+
+static __global__ void __launch_bounds__(kThreads, 10)
+fwdDecideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
+              const uint32_t* __restrict__ tasks, int count, int tr) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* stage = reinterpret_cast<float4*>(smem);
+  const int lane = (int)threadIdx.x & 31;
+  for (int i = blockIdx.x * kRecWarps + (int)(threadIdx.x >> 5); i < count;
+       i += gridDim.x * kRecWarps)
+    fwdDecideRecordStaged(t, rows, tr, loadRec(recs, tasks[i]), lane, stage);
 }
 
 // ---------------------------------------------------------------------------
@@ -186,10 +339,12 @@ __device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" 
 // returned (so a grid that has launched implies that the grid two places
 // before it has completed; the fused plan relies on that), instead of at
 // its start.
-static __global__ void __launch_bounds__(kThreads, 12)
+static __global__ void __launch_bounds__(kThreads, 10)
 fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
              const uint32_t* __restrict__ recTasks, int nRec, const int* __restrict__ chance,
              int nCh, int tr, int late) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* stage = reinterpret_cast<float4*>(smem);
   if (!late) pdlTrigger();
   const int nRc = recordCtas(nRec), lane = (int)threadIdx.x & 31;
   bool waited = false;
@@ -200,7 +355,7 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       const DecRec r = loadRec(recs, recTasks[k]);
       pdlWait();
       waited = true;
-      fwdDecideRecord(t, rows, tr, r, lane);
+      fwdDecideRecordStaged(t, rows, tr, r, lane, stage);
     } else {
       const int w = chance[i - nRc];
       pdlWait();
@@ -215,11 +370,11 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
   }
 }
 
-static __global__ void __launch_bounds__(kThreads, 12)
+static __global__ void __launch_bounds__(kThreads, 8)
 bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
              const uint32_t* __restrict__ recTasks, int nRec, const int* __restrict__ chance,
              int nCh, int tr) {
-  __shared__ __align__(16) unsigned char smem[kChanceScratchBytes];
+  extern __shared__ __align__(16) unsigned char smem[];  // bwdStageBytes()
   pdlTrigger();
   const int nRc = recordCtas(nRec), lane = (int)threadIdx.x & 31;
   for (int i = blockIdx.x; i < nRc + nCh; i += gridDim.x) {
@@ -228,7 +383,7 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       if (k >= nRec) continue;
       const DecRec r = loadRec(recs, recTasks[k]);
       pdlWait();
-      decideRecord(t, rows, r, lane);
+      decideRecordStaged(t, rows, r, lane, reinterpret_cast<float4*>(smem));
     } else {
       const int w = chance[i - nRc];
       pdlWait();

@@ -97,11 +97,11 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       launchFdGroups(g, a.smemFd, s, a.tree, a.rows, a.groups, tk, l.list.count, l.tr, a.maxN);
       break;
     case kDecRec:
-      decideRecK<<<gridOf(recordCtas(l.list.count)), kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
+      decideRecK<<<gridOf(recordCtas(l.list.count)), kThreads, bwdStageBytes(), s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
                                         l.list.count);
       break;
     case kFwdRec:
-      fwdDecideRecK<<<gridOf(recordCtas(l.list.count)), kThreads, 0, s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
+      fwdDecideRecK<<<gridOf(recordCtas(l.list.count)), kThreads, fwdStageBytes(), s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
                                            l.list.count, l.tr);
       break;
     case kBwdFused: {
@@ -131,7 +131,7 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(gridOf(recordCtas(l.list.count) + l.list2.count));
       cfg.blockDim = dim3(kThreads);
-      cfg.dynamicSmemBytes = 0;
+      cfg.dynamicSmemBytes = l.kind == kFwdMix ? fwdStageBytes() : bwdStageBytes();
       cfg.stream = s;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;

@@ -405,7 +405,7 @@ fdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
 __host__ __device__ inline size_t fusedLevelSmem(int maxN) {
   size_t s = sdGroupSmem(maxN);
   if (fdGroupSmem(maxN) > s) s = fdGroupSmem(maxN);
-  return s > kChanceScratchBytes ? s : kChanceScratchBytes;
+  return s > bwdStageBytes() ? s : bwdStageBytes();
 }
 constexpr int kFusedMaxN = kSpan * kThreads - 1;  // widest list of a 128-thread group
 
@@ -426,7 +426,7 @@ bwdLevelFusedK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs
         const DecRec r = loadRec(recs, recTasks[k]);
         pdlWait();
         waited = true;
-        decideRecord(t, rows, r, lane);
+        decideRecordStaged(t, rows, r, lane, reinterpret_cast<float4*>(smem));
       }
     } else if (i < e2) {
       const int w = chance[i - e1];
