@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -61,6 +62,8 @@ struct Engine::Dev {
   int* counter = nullptr;
   int* tasks = nullptr;
   std::vector<int> hostTasks;  // host copy of the concatenated task lists
+  int* qTasks = nullptr;       // walkFrom's task lists (grown on demand)
+  size_t qCap = 0;
   std::vector<ListRef> fwd[2], bwd[2];
   std::vector<ListRef> sdG, fdG, inner[2];  // the group plan's backward lists
   std::vector<ListRef> bCh[2], fCh[2];       // its chance word lists
@@ -192,6 +195,7 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
 
 Engine::~Engine() {
   if (!d_) return;
+  if (d_->qTasks) cudaFree(d_->qTasks);
   if (d_->exec) cudaGraphExecDestroy(d_->exec);
   if (d_->graph) cudaGraphDestroy(d_->graph);
   if (d_->stream) cudaStreamSynchronize(d_->stream);
@@ -582,6 +586,90 @@ void Engine::walk(int tr, int mode) {
       bwdLevelK<double><<<gridOf(b.count), kThreads, d.smemD, d.stream>>>(
           d.tree, d.rowsD, d.tasks + b.off, b.count, tr, mode, d.maxN);
   }
+  GB_CK(cudaGetLastError());
+  GB_CK(cudaStreamSynchronize(d.stream));
+}
+
+void Engine::walkFrom(int tr, int mode, int u) {
+  Dev& d = *d_;
+  const int N = (int)t_.nodes.size();
+  if (subEnd_.empty()) {
+    // One past each subtree's last id; -1 marks a tree whose subtrees are
+    // not contiguous id ranges (walkFrom then walks the whole tree).
+    subEnd_.assign(N, 0);
+    std::vector<int> size(N, 1);
+    bool ok = true;
+    for (int v = N - 1; v >= 0; --v) {
+      const Node& nd = t_.nodes[v];
+      int end = v + 1;
+      for (int k = 0; k < nd.nChildren; ++k) {
+        const int c = t_.children[nd.childBase + k];
+        if (c <= v) ok = false;
+        size[v] += size[c];
+        end = std::max(end, subEnd_[c]);
+      }
+      subEnd_[v] = end;
+      if (end - v != size[v]) ok = false;
+    }
+    if (!ok) subEnd_.assign(N, -1);
+  }
+  // PPS_GB_QUERY_FULL_WALKS (tests): walk the whole tree instead.
+  if (u <= 0 || u >= N || subEnd_[u] < 0 || std::getenv("PPS_GB_QUERY_FULL_WALKS")) {
+    walk(tr, mode);
+    return;
+  }
+  ensureWalkBuffers();
+  // Ancestors of u and the child index toward u at each.
+  std::map<int, int> toward;
+  for (int c = u, p = t_.nodes[u].parent; p >= 0; c = p, p = t_.nodes[p].parent) {
+    const Node& pn = t_.nodes[p];
+    for (int k = 0; k < pn.nChildren; ++k)
+      if (t_.children[pn.childBase + k] == c) toward[p] = k;
+  }
+  const int end = subEnd_[u];
+  const int D = (int)L_.fwdTasks[tr].size();
+  std::vector<int> all;
+  std::vector<ListRef> fwd(D), bwd(D);
+  for (int dd = 0; dd < D; ++dd) {
+    fwd[dd].off = (int)all.size();
+    for (int w : L_.fwdTasks[tr][dd]) {
+      const int v = (int)((unsigned)w >> 8);
+      bool keep = v >= u && v < end;
+      if (!keep) {
+        auto it = toward.find(v);
+        keep = it != toward.end() && ((w & 3) != kTaskChance || ((w >> 2) & 63) == it->second);
+      }
+      if (keep) all.push_back(w);
+    }
+    fwd[dd].count = (int)all.size() - fwd[dd].off;
+  }
+  for (int dd = 0; dd < D; ++dd) {
+    bwd[dd].off = (int)all.size();
+    for (int w : L_.bwdTasks[tr][dd]) {
+      const int v = (int)((unsigned)w >> 8);
+      if (v >= u && v < end) all.push_back(w);
+    }
+    bwd[dd].count = (int)all.size() - bwd[dd].off;
+  }
+  if (all.empty()) return;
+  if (all.size() > d.qCap) {
+    if (d.qTasks) cudaFree(d.qTasks);
+    d.qTasks = nullptr;
+    d.qCap = 0;
+    GB_CK(cudaMalloc(&d.qTasks, all.size() * sizeof(int)));
+    d.qCap = all.size();
+  }
+  GB_CK(cudaMemcpyAsync(d.qTasks, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice,
+                        d.stream));
+  h2d_ += (int64_t)(all.size() * sizeof(int));
+  for (int dd = 0; dd < D; ++dd)
+    if (fwd[dd].count)
+      fwdLevelK<double><<<gridOf(fwd[dd].count), kThreads, 0, d.stream>>>(
+          d.tree, d.rowsD, d.qTasks + fwd[dd].off, fwd[dd].count, tr, 1);
+  for (int dd = D - 1; dd >= 0; --dd)
+    if (bwd[dd].count)
+      bwdLevelK<double><<<gridOf(bwd[dd].count), kThreads, d.smemD, d.stream>>>(
+          d.tree, d.rowsD, d.qTasks + bwd[dd].off, bwd[dd].count, tr, mode, d.maxN);
   GB_CK(cudaGetLastError());
   GB_CK(cudaStreamSynchronize(d.stream));
 }

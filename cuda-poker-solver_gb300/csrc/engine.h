@@ -33,6 +33,13 @@ class Engine {
   // Runs one FP64 walk (mode 1 = average-strategy EV, 2 = best response)
   // for traverser tr and waits for it; rows stay readable afterwards.
   void walk(int tr, int mode);
+  // The same walk restricted to what node u's rows depend on: the forward
+  // path from the root to u (each opponent decide ancestor's chunks, each
+  // chance ancestor's branch toward u) and u's subtree (forward and
+  // backward). u's rows and its descendants' come out exactly as after
+  // walk(); other rows are stale. Node ids are DFS pre-order, so a subtree
+  // is the id range [u, subtreeEnd(u)).
+  void walkFrom(int tr, int mode, int u);
   // Rows of the last walk (double): the traverser's value row at `node`
   // (n_tr entries) and the opponent reach row of layout tr (n_opp entries).
   std::vector<double> walkCfv(int node, int tr) const;
@@ -84,6 +91,7 @@ class Engine {
   HostLayout L_;
   std::unique_ptr<Dev> d_;
   int engineKind_ = 0;
+  std::vector<int> subEnd_;  // per node: one past the last id of its subtree (walkFrom)
   bool tuned_ = false;
   int launchesPerIter_ = 0;
   size_t deviceBytes_ = 0;

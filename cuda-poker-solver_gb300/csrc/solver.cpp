@@ -414,7 +414,7 @@ gpu::NodeEv SolverCore::nodeEv(int decideIdx) {
   const std::vector<float> srows = eng_->nodeRows(1, u);
 
   for (int tr = 0; tr < 2; ++tr) {
-    eng_->walk(tr, kModeEV);
+    eng_->walkFrom(tr, kModeEV, u);  // rows of u and its children
     gpu::NodeEv::Side& S = out.side[tr];
     const auto& list = st.list[tr];
     const auto& olist = st.list[1 - tr];
@@ -542,7 +542,7 @@ gpu::RunoutSummary SolverCore::runoutSummary(int decideIdx, int actionIdx) {
   for (int a = 0; a < fm.na; ++a) out.actions.push_back(label(tree_.actions[fm.actBase + a]));
 
   for (int tr = 0; tr < 2; ++tr) {
-    eng_->walk(tr, kModeEV);
+    eng_->walkFrom(tr, kModeEV, ch);  // rows below the deal
     const Side& self = tree_.side[tr];
     const Side& opp = tree_.side[1 - tr];
     for (int br = 0; br < cn.nChildren; ++br) {

@@ -218,6 +218,35 @@ def test_runout_summary_and_tree():
     assert len(ts["boards"]) == 5 * s.num_nodes
 
 
+def test_queries_walk_only_what_they_read(monkeypatch):
+    """node_ev and runout_summary walk the query node's subtree plus the
+    forward path to it; the answers are identical to full-tree walks."""
+    s = fresh()
+    s.solve(200)
+    nodes = s.decide_nodes()
+    ts = s.tree_structure()
+    deals = [(n["index"], a) for n in nodes for a, c in enumerate(n["children"])
+             if ts["kinds"][c] == 3][:3]
+    picks = sorted({1, 2, 5, len(nodes) // 2, len(nodes) - 1})
+
+    def answers():
+        return ([s.node_ev(i) for i in picks], [s.runout_summary(i, a) for i, a in deals])
+
+    sub_ev, sub_run = answers()
+    monkeypatch.setenv("PPS_GB_QUERY_FULL_WALKS", "1")
+    full_ev, full_run = answers()
+    for a, b in zip(sub_ev, full_ev):
+        for side in ("oop", "ip"):
+            for k in ("ev", "mass", "agg_ev"):
+                assert np.array_equal(np.asarray(a["sides"][side][k]),
+                                      np.asarray(b["sides"][side][k])), (side, k)
+        for x, y in zip(a["action_ev"], b["action_ev"]):
+            assert np.array_equal(np.asarray(x["per_combo"]), np.asarray(y["per_combo"]))
+    for a, b in zip(sub_run, full_run):
+        for x, y in zip(a["branches"], b["branches"]):
+            assert x["agg_ev"] == y["agg_ev"] and list(x["freq"]) == list(y["freq"])
+
+
 def test_cli_protocol():
     exe = os.path.join(os.path.dirname(pps.__file__), "gpu_pfflop")
     out = subprocess.run([exe, "postflop", "Qs9h2d7c", "TT+", "99+", "200", "3000", "0.5", "",
