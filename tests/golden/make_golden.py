@@ -13,6 +13,8 @@ Fixtures:
   eval_keys.npz       reference strength keys of seeded 7-card hands
   bet_actions.json    reference pf::betActions on seeded betting states
   ranges.json         reference parseRange weights for range strings
+  api_routes.json     (method, path) of every route of the reference's HTTP
+                      API (python/pps_api.py), read from its source as text
   ref_treebuf.json    byte offset of every TreeBuf member (the argument
                       block of the reference kernels, cuda/gpu_cfr.cu:
                       132-201) and its size, as compiled from the source
@@ -110,10 +112,25 @@ def treebuf_layout():
               open(os.path.join(HERE, "ref_treebuf.json"), "w"), indent=0)
 
 
+def api_routes():
+    import re
+    src = open(os.path.join(os.environ.get("PPS_REFERENCE", "/root/reference"),
+                            "python", "pps_api.py")).read()
+    routes = sorted({(m.upper(), p) for m, p, rest in
+                     re.findall(r'@app\.(get|post|delete|put)\("([^"]+)"([^)]*)\)', src)
+                     if "include_in_schema=False" not in rest})
+    json.dump([list(r) for r in routes], open(os.path.join(HERE, "api_routes.json"), "w"),
+              indent=0)
+
+
 def main():
+    if sys.argv[1:] == ["--api-routes"]:
+        api_routes()
+        return
     if not os.path.exists(os.path.join(REF_BIN, "ref_capture")):
         raise SystemExit("build the reference tools first: sh oracle/ref/build_ref.sh")
     treebuf_layout()
+    api_routes()
     if sys.argv[1:] == ["--treebuf"]:
         return
     small = [wl.river_c1(), wl.turn_api(), wl.turn_tiny()] + edge_spots()
