@@ -63,8 +63,15 @@ __device__ __forceinline__ float comp4(float4 v, int g) {
 constexpr int kSpan = 8;
 constexpr int kSpanShift = 8;  // log2(32 * kSpan): position -> warp block
 __host__ __device__ inline int groupTabEntries(int maxN) { return (3 * maxN + 53 + 7) / 8 * 8; }
-__host__ __device__ inline int groupPrefixEntries(int maxN) { return maxN + kSpan; }
-__host__ __device__ inline int groupXEntries(int maxN) { return 2 * maxN + 52; }
+// The float4 arrays below are padded with one entry after every 8 (entry k
+// lives at pad8(k)): a thread's 8 consecutive positions, and the 8 lanes
+// of a card segment, then fall in 8 different bank groups when they write
+// at stride 8, instead of 8-way conflicts on one bank group (ncu counted
+// conflicts as 62% of the showdown kernel's shared-memory wavefronts).
+__host__ __device__ __forceinline__ int pad8(int k) { return k + (k >> 3); }
+__host__ __device__ inline int groupPrefixEntries(int maxN) { return pad8(maxN + kSpan) + 1; }
+__host__ __device__ inline int groupXEntries(int maxN) { return pad8(2 * maxN + 52) + 1; }
+__host__ __device__ inline int groupRowEntries(int maxN) { return pad8(4 * ((maxN + 3) / 4)) + 1; }
 constexpr int kGroupBlocks = kTermThreads / 32 + 1;  // warp blocks + the total
 
 // Showdown groups: tab | P4 | X4 | W4 | WH | WL. The P4 region first holds
@@ -75,12 +82,12 @@ __host__ __device__ inline size_t sdGroupSmem(int maxN) {
 }
 // Fold groups: tab | rs4 | cs4[53] | card pairs (u16) | identical-combo slots (i16).
 __host__ __device__ inline size_t fdGroupSmem(int maxN) {
-  return (size_t)groupTabEntries(maxN) * 2 + 16 * ((size_t)4 * ((maxN + 3) / 4) + 53) +
+  return (size_t)groupTabEntries(maxN) * 2 + 16 * ((size_t)groupRowEntries(maxN) + 53) +
          (size_t)4 * ((maxN + 7) / 8 * 8);
 }
 
-// Stages the group's opponent reach rows transposed: rs4[j] holds entry j
-// of the four rows (0 for an absent node).
+// Stages the group's opponent reach rows transposed: rs4[pad8(j)] holds
+// entry j of the four rows (0 for an absent node).
 static __device__ __forceinline__ void stageRows4(float4* rs4, const DevTree& t, const DevRows<float>& rows,
                                            const int (&u)[4], int tr, int no) {
   const float* r[4];
@@ -92,10 +99,11 @@ static __device__ __forceinline__ void stageRows4(float4* rs4, const DevTree& t,
 #pragma unroll
     for (int g = 0; g < 4; ++g)
       v[g] = r[g] ? *reinterpret_cast<const float4*>(r[g] + 4 * q) : zero4();
-    rs4[4 * q + 0] = make_float4(v[0].x, v[1].x, v[2].x, v[3].x);
-    rs4[4 * q + 1] = make_float4(v[0].y, v[1].y, v[2].y, v[3].y);
-    rs4[4 * q + 2] = make_float4(v[0].z, v[1].z, v[2].z, v[3].z);
-    rs4[4 * q + 3] = make_float4(v[0].w, v[1].w, v[2].w, v[3].w);
+    float4* d = rs4 + pad8(4 * q);  // the quad's 4 entries share one pad block
+    d[0] = make_float4(v[0].x, v[1].x, v[2].x, v[3].x);
+    d[1] = make_float4(v[0].y, v[1].y, v[2].y, v[3].y);
+    d[2] = make_float4(v[0].z, v[1].z, v[2].z, v[3].z);
+    d[3] = make_float4(v[0].w, v[1].w, v[2].w, v[3].w);
   }
 }
 
@@ -136,7 +144,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   __syncthreads();
 
   // Card segments, four cards per warp (8 lanes x 8 entries per card):
-  // X4[seg[c] + c + k] = reach of the card's first k entries, k = 0..len.
+  // X4[pad8(seg[c] + c + k)] = reach of the card's first k entries, k = 0..len.
   for (int cb = warp * 4; cb < 52; cb += nw * 4) {
     const int c = cb + (lane >> 3), sub = lane & 7;
     const int s0 = seg[c], len = seg[c + 1] - s0;
@@ -146,7 +154,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
     for (int j = 0; j < 8; ++j) {
       const int e = sub * 8 + j;
       pre[j] = run;
-      if (e < len) run += rs4[segSlot[s0 + e]];
+      if (e < len) run += rs4[pad8(segSlot[s0 + e])];
     }
     float4 incl = run;
 #pragma unroll
@@ -156,11 +164,10 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
     }
     float4 base = shflUp4(incl, 1, 8);
     if (sub == 0) base = zero4();
-    float4* xo = X4 + s0 + c;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int e = sub * 8 + j;
-      if (e <= len) xo[e] = base + pre[j];
+      if (e <= len) X4[pad8(s0 + c + e)] = base + pre[j];
     }
   }
   // Exclusive prefixes of the strength-sorted reach in one pass: thread t
@@ -177,7 +184,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
     const uint4 o8 = mine && k0 < no ? *reinterpret_cast<const uint4*>(ord + k0) : make_uint4(0, 0, 0, 0);
     const uint16_t* o = reinterpret_cast<const uint16_t*>(&o8);
 #pragma unroll
-    for (int j = 0; j < kSpan; ++j) v[j] = k0 + j < no ? rs4[o[j]] : zero4();
+    for (int j = 0; j < kSpan; ++j) v[j] = k0 + j < no ? rs4[pad8(o[j])] : zero4();
     float4 run = zero4();
 #pragma unroll
     for (int j = 0; j < kSpan; ++j) {
@@ -197,7 +204,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   __syncthreads();
   if (mine)
 #pragma unroll
-    for (int j = 0; j < kSpan; ++j) P4[k0 + j] = ex + pre[j];
+    for (int j = 0; j < kSpan; ++j) P4[pad8(k0 + j)] = ex + pre[j];
   // Compensated exclusive prefix of the warp-block totals, one thread per
   // node.
   if (threadIdx.x < 4) {
@@ -230,7 +237,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   }
   const ShowdownInfo* info = t.poolSd + st.sdInfoOff[tr];
   const int bn = no >> kSpanShift;
-  const float4 TH = BH4[bn], TL = BL4[bn], Pno = P4[no];
+  const float4 TH = BH4[bn], TL = BL4[bn], Pno = P4[pad8(no)];
   float* out[4];
   outRows4(out, t, rows, u);
   const float* rr[4];
@@ -248,9 +255,9 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
     const int le = f.x & 0xffff, te = f.x >> 16;
     const int len1 = f.y & 0xff, len2 = (f.y >> 8) & 0xff;
     const int a1 = f.w & 0xffff, a2 = f.w >> 16;
-    const float4 x1le = X4[a1 + ((f.y >> 16) & 0xff)], x1te = X4[a1 + (f.y >> 24)];
-    const float4 x2le = X4[a2 + (f.z & 0xff)], x2te = X4[a2 + ((f.z >> 8) & 0xff)];
-    const float4 x1end = X4[a1 + len1], x2end = X4[a2 + len2];
+    const float4 x1le = X4[pad8(a1 + ((f.y >> 16) & 0xff))], x1te = X4[pad8(a1 + (f.y >> 24))];
+    const float4 x2le = X4[pad8(a2 + (f.z & 0xff))], x2te = X4[pad8(a2 + ((f.z >> 8) & 0xff))];
+    const float4 x1end = X4[pad8(a1 + len1)], x2end = X4[pad8(a2 + len2)];
     const int same = (int)(f.z >> 16) - 1;
     float4 sameR = zero4();
     if (same >= 0)  // the identical combo's reach, from the (cached) rows
@@ -258,7 +265,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
                           rr[2] ? rr[2][same] : 0.f, rr[3] ? rr[3][same] : 0.f);
     const int bl = le >> kSpanShift, bt = te >> kSpanShift;
     const float4 bhl = BH4[bl], bll = BL4[bl], bht = BH4[bt], blt = BL4[bt];
-    const float4 ple = P4[le], pte = P4[te];
+    const float4 ple = P4[pad8(le)], pte = P4[pad8(te)];
     const float4 below = bhl + (bll + ple);
     const float4 band = (bht - bhl) + (blt - bll) + (pte - ple);
     const float4 above = (TH - bht) + (TL - blt) + (Pno - pte);
@@ -281,7 +288,7 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
   const int no = st.n[opp], nt = st.n[tr];
   uint16_t* csr = reinterpret_cast<uint16_t*>(smem);
   float4* rs4 = reinterpret_cast<float4*>(smem + (size_t)groupTabEntries(maxN) * 2);
-  float4* cs4 = rs4 + 4 * ((maxN + 3) / 4);  // [52] card sums, [52] total
+  float4* cs4 = rs4 + groupRowEntries(maxN);  // [52] card sums, [52] total
   uint16_t* cardsS = reinterpret_cast<uint16_t*>(cs4 + 53);
   int16_t* sameS = reinterpret_cast<int16_t*>(cardsS + (maxN + 7) / 8 * 8);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -306,7 +313,7 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int e = sub * 8 + j;
-      if (e < len) a += rs4[csr[53 + s0 + e]];
+      if (e < len) a += rs4[pad8(csr[53 + s0 + e])];
     }
 #pragma unroll
     for (int m = 4; m > 0; m >>= 1) a += shflXor4(a, m, 8);
@@ -338,7 +345,7 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
     }
     const int cp = cardsS[i], sm = sameS[i];
     float4 w = tot - cs4[cp & 0xff] - cs4[cp >> 8];
-    if (sm >= 0) w += rs4[sm];
+    if (sm >= 0) w += rs4[pad8(sm)];
     w = max0(w);
     storeOut4(out, i, make_float4(w.x * v[0], w.y * v[1], w.z * v[2], w.w * v[3]));
   }
