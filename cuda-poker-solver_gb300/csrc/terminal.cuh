@@ -365,7 +365,7 @@ __host__ __device__ constexpr int termThreadsFor(int maxN) {
   return maxN + 1 <= kSpan * 64 ? 64 : maxN + 1 <= kSpan * 128 ? 128 : kTermThreads;
 }
 constexpr int sdMinBlocks(int kT) { return 3 * kTermThreads / kT; }
-constexpr int fdMinBlocks(int kT) { return 4 * kTermThreads / kT; }
+constexpr int fdMinBlocks(int kT) { return 5 * kTermThreads / kT; }
 
 template <int kT>
 static __global__ void __launch_bounds__(kT, sdMinBlocks(kT))
