@@ -155,7 +155,8 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
 }
 
 // Streams and events of a plan with up to kSides + 1 concurrent branches.
-constexpr int kSides = 5;
+constexpr int kTermRot = 3;  // side streams per terminal kind, used in turn by depth
+constexpr int kSides = 1 + 2 * kTermRot;
 struct Branches {
   cudaStream_t main = nullptr, side[kSides] = {};
   cudaEvent_t fork = nullptr, join[kSides] = {};
@@ -262,12 +263,11 @@ struct StagedEvents {
   }
 };
 
-// Issues a staged plan: main stream b.main, level partner b.side[2],
-// showdown groups on b.side[0] (even depths) and b.side[3] (odd depths),
-// fold groups on b.side[1] and b.side[4]. Two streams per kind let the
-// groups of consecutive depths run at once: a depth's groups wait for the
-// forward level that wrote their reach rows, not for the previous depth's
-// groups.
+// Issues a staged plan: main stream b.main, level partner b.side[0], the
+// showdown and fold groups of depth d on b.side[1 + 2 (d mod kTermRot)] and
+// the stream after it. Streams used in turn let the groups of consecutive
+// depths run at once: a depth's groups wait for the forward level that
+// wrote their reach rows, not for the previous depth's groups.
 template <typename IssueOne>
 void issueStaged(const StagedPlan& P, const Branches& b, StagedEvents& ev, IssueOne&& one) {
   auto issueSet = [&](const std::vector<Launch>& set) {
@@ -277,10 +277,10 @@ void issueStaged(const StagedPlan& P, const Branches& b, StagedEvents& ev, Issue
       return;
     }
     GB_CK(cudaEventRecord(ev.lfork, b.main));
-    GB_CK(cudaStreamWaitEvent(b.side[2], ev.lfork, 0));
+    GB_CK(cudaStreamWaitEvent(b.side[0], ev.lfork, 0));
     one(set[0], b.main);
-    for (size_t k = 1; k < set.size(); ++k) one(set[k], b.side[2]);
-    GB_CK(cudaEventRecord(ev.ljoin, b.side[2]));
+    for (size_t k = 1; k < set.size(); ++k) one(set[k], b.side[0]);
+    GB_CK(cudaEventRecord(ev.ljoin, b.side[0]));
     GB_CK(cudaStreamWaitEvent(b.main, ev.ljoin, 0));
   };
   for (const HalfStep& h : P.half) {
@@ -292,7 +292,7 @@ void issueStaged(const StagedPlan& P, const Branches& b, StagedEvents& ev, Issue
       for (int k = 0; k < 2; ++k) {
         const Launch& l = k == 0 ? h.sd[d] : h.fd[d];
         if (!l.list.count) continue;
-        cudaStream_t s = b.side[(d & 1) ? 3 + k : k];
+        cudaStream_t s = b.side[1 + 2 * (d % kTermRot) + k];
         GB_CK(cudaStreamWaitEvent(s, d == 0 ? ev.start : ev.fwd[d - 1], 0));
         one(l, s);
         GB_CK(cudaEventRecord(k == 0 ? ev.sd[d] : ev.fd[d], s));
