@@ -155,7 +155,7 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
 }
 
 // Streams and events of a plan with up to kSides + 1 concurrent branches.
-constexpr int kTermRot = 3;  // side streams per terminal kind, used in turn by depth
+constexpr int kTermRot = 4;  // side streams per terminal kind, used in turn by depth
 constexpr int kSides = 1 + 2 * kTermRot;
 struct Branches {
   cudaStream_t main = nullptr, side[kSides] = {};
