@@ -282,9 +282,80 @@ __device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const De
   }
 }
 
-// One warp per record (kRecWarps records per CTA), one kernel per pass.
-// A warp's records are independent of its CTA's other warps: no barrier.
-// Internal linkage: included by more than one translation unit.
+// ---------------------------------------------------------------------------
+// Chance records (layout.cpp): the arithmetic of fwdChanceBranch /
+// chanceChunk (kernels.cuh) with every address resolved on the host. The
+// record header is static data, read before the kernel waits for the
+// previous grid.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 loadChanceHeader(const uint32_t* __restrict__ recs,
+                                                  uint32_t off16) {
+  return *reinterpret_cast<const uint4*>(recs + (size_t)off16 * 4);
+}
+
+// Forward: child reach = parent reach through the child -> parent slot map,
+// scaled by 1 / chanceQ (cuda/gpu_cfr.cu:276-293).
+__device__ __forceinline__ void fwdChanceRecord(const DevTree& t, const DevRows<float>& rows,
+                                                int tr, uint4 h) {
+  const int nc = (int)(h.w & 0xffff);
+  const float inv = 1.f / (float)(h.w >> 16);
+  const uint16_t* up = t.poolU16 + h.z;
+  const float* pr = rows.reach[tr] + (size_t)h.x * 4;
+  float* cr = rows.reach[tr] + (size_t)h.y * 4;
+  for (int q = threadIdx.x; q < quadsOf(nc); q += blockDim.x) {
+    float out[4];
+    for (int l = 0; l < 4; ++l) {
+      const int j = 4 * q + l;
+      out[l] = j < nc ? pr[up[j]] * inv : 0.f;
+    }
+    stq(cr + 4 * q, out);
+  }
+}
+
+// Backward, first part (static data, before the wait): the branch table
+// into shared memory (child value rows and parent -> child slot maps).
+__device__ __forceinline__ void chanceRecordTables(const DevTree& t, const DevRows<float>& rows,
+                                                   const uint32_t* __restrict__ recs, uint4 h,
+                                                   unsigned char* smem) {
+  const int nb = (int)(h.y >> 16);
+  const uint32_t* tab = recs + (size_t)h.w * 4;
+  const float** rowOf = reinterpret_cast<const float**>(smem);
+  const int16_t** downOf = reinterpret_cast<const int16_t**>(smem + 64 * sizeof(void*));
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    rowOf[b] = rows.cfv + (size_t)tab[2 * b] * 4;
+    downOf[b] = t.poolI16 + tab[2 * b + 1];
+  }
+}
+
+// Backward, second part (after __syncthreads and the wait): parent value of
+// one 128-combo chunk = sum over the branches (cuda/gpu_cfr.cu:542-554).
+__device__ __forceinline__ void chanceRecordSum(const DevRows<float>& rows, uint4 h,
+                                                const unsigned char* smem) {
+  const int n = (int)(h.y & 0xffff), nb = (int)(h.y >> 16);
+  const float* const* rowOf = reinterpret_cast<const float* const*>(smem);
+  const int16_t* const* downOf =
+      reinterpret_cast<const int16_t* const*>(smem + 64 * sizeof(void*));
+  float* out = rows.cfv + (size_t)h.x * 4;
+  const int i = (int)h.z * kChanceChunk + (int)threadIdx.x;
+  if (i >= quadsOf(n) * 4) return;
+  float v = 0.f;
+  if (i < n) {
+    for (int b0 = 0; b0 < nb; b0 += 8) {
+      int k[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) k[j] = b0 + j < nb ? downOf[b0 + j][i] : -1;
+      float x[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) x[j] = k[j] >= 0 ? rowOf[b0 + j][k[j]] : 0.f;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v += x[j];
+    }
+  }
+  out[i] = v;
+}
+
+// One warp per record, kRecWarps records per CTA. A warp's records are
+// independent of its CTA's other warps: no barrier.
 constexpr int kRecWarps = kThreads / 32;
 __host__ __device__ inline int recordCtas(int records) {
   return (records + kRecWarps - 1) / kRecWarps;
@@ -299,32 +370,11 @@ __host__ __device__ constexpr size_t bwdStageBytes() {
   return recStageBytes() > kChanceScratchBytes ? recStageBytes() : kChanceScratchBytes;
 }
 
-static __global__ void __launch_bounds__(kThreads, 8)
-decideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
-           const uint32_t* __restrict__ tasks, int count) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  float4* stage = reinterpret_cast<float4*>(smem);
-  const int lane = (int)threadIdx.x & 31;
-  for (int i = blockIdx.x * kRecWarps + (int)(threadIdx.x >> 5); i < count;
-       i += gridDim.x * kRecWarps)
-    decideRecordStaged(t, rows, loadRec(recs, tasks[i]), lane, stage);
-}
-
-static __global__ void __launch_bounds__(kThreads, 10)
-fwdDecideRecK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
-              const uint32_t* __restrict__ tasks, int count, int tr) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  float4* stage = reinterpret_cast<float4*>(smem);
-  const int lane = (int)threadIdx.x & 31;
-  for (int i = blockIdx.x * kRecWarps + (int)(threadIdx.x >> 5); i < count;
-       i += gridDim.x * kRecWarps)
-    fwdDecideRecordStaged(t, rows, tr, loadRec(recs, tasks[i]), lane, stage);
-}
-
 // ---------------------------------------------------------------------------
 // Level kernels of the default iteration: one launch per level and pass
-// covering the level's decide records and chance tasks (CTA i <
-// recordCtas(nRec): one record per warp; else a chance task word), launched with programmatic dependent
+// covering the level's decide records and chance records (CTA i <
+// recordCtas(nRec): one decide record per warp; else one chance record),
+// launched with programmatic dependent
 // launch so consecutive levels overlap: each CTA lets the next level's grid
 // start (launch_dependents), loads its record (static data), then waits
 // until the previous level's grid has finished and its writes are visible
@@ -341,7 +391,7 @@ __device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" 
 // its start.
 static __global__ void __launch_bounds__(kThreads, 10)
 fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
-             const uint32_t* __restrict__ recTasks, int nRec, const int* __restrict__ chance,
+             const uint32_t* __restrict__ recTasks, int nRec, const uint32_t* __restrict__ chance,
              int nCh, int tr, int late) {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* stage = reinterpret_cast<float4*>(smem);
@@ -357,10 +407,10 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       waited = true;
       fwdDecideRecordStaged(t, rows, tr, r, lane, stage);
     } else {
-      const int w = chance[i - nRc];
+      const uint4 h = loadChanceHeader(recs, chance[i - nRc]);
       pdlWait();
       waited = true;
-      fwdChanceBranch<float>(t, rows, (int)((unsigned)w >> 8), (w >> 2) & 63, tr);
+      fwdChanceRecord(t, rows, tr, h);
     }
     if (late) pdlTrigger();
   }
@@ -372,12 +422,15 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
 
 static __global__ void __launch_bounds__(kThreads, 8)
 bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
-             const uint32_t* __restrict__ recTasks, int nRec, const int* __restrict__ chance,
+             const uint32_t* __restrict__ recTasks, int nRec, const uint32_t* __restrict__ chance,
              int nCh, int tr) {
   extern __shared__ __align__(16) unsigned char smem[];  // bwdStageBytes()
   pdlTrigger();
   const int nRc = recordCtas(nRec), lane = (int)threadIdx.x & 31;
   for (int i = blockIdx.x; i < nRc + nCh; i += gridDim.x) {
+    // A CTA that runs more than one task (grids past 2^20 CTAs) must not
+    // overwrite shared memory that its warps still read for the last one.
+    if (i != (int)blockIdx.x) __syncthreads();
     if (i < nRc) {
       const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
       if (k >= nRec) continue;
@@ -385,9 +438,11 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       pdlWait();
       decideRecordStaged(t, rows, r, lane, reinterpret_cast<float4*>(smem));
     } else {
-      const int w = chance[i - nRc];
+      const uint4 h = loadChanceHeader(recs, chance[i - nRc]);
+      chanceRecordTables(t, rows, recs, h, smem);
+      __syncthreads();
       pdlWait();
-      chanceChunk<float>(t, rows, (int)((unsigned)w >> 8), (w >> 2) & 63, tr, smem);
+      chanceRecordSum(rows, h, smem);
       __syncthreads();  // the next chance task reuses the pointer tables
     }
   }

@@ -167,12 +167,12 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
   std::vector<uint32_t> recTasks;
   for (int tr = 0; tr < 2; ++tr)
     for (int dd = 0; dd < D; ++dd) {
-      d.bCh[tr].push_back(addList(L_.bwdChance[tr][dd]));
-      d.fCh[tr].push_back(addList(L_.fwdChance[tr][dd]));
-      for (auto* pr : {&d.bRec[tr], &d.fRec[tr]}) {
-        const auto& v = pr == &d.bRec[tr] ? L_.bwdRecs[tr][dd] : L_.fwdRecs[tr][dd];
-        pr->push_back(ListRef{(int)recTasks.size(), (int)v.size()});
-        recTasks.insert(recTasks.end(), v.begin(), v.end());
+      const std::vector<uint32_t>* src[4] = {&L_.bwdRecs[tr][dd], &L_.fwdRecs[tr][dd],
+                                             &L_.bwdChanceRecs[tr][dd], &L_.fwdChanceRecs[tr][dd]};
+      std::vector<ListRef>* dst[4] = {&d.bRec[tr], &d.fRec[tr], &d.bCh[tr], &d.fCh[tr]};
+      for (int k = 0; k < 4; ++k) {
+        dst[k]->push_back(ListRef{(int)recTasks.size(), (int)src[k]->size()});
+        recTasks.insert(recTasks.end(), src[k]->begin(), src[k]->end());
       }
     }
   d.recs = upload(d, L_.recPool, B, h2d_);
@@ -283,6 +283,7 @@ void Engine::buildPlans() {
                  listBytes(kindOnly(L_.fwdTasks[tr][dd], kTaskDecide), tr, true) +
                      listBytes(L_.fwdChance[tr][dd], tr, true)};
         l.list2 = d.fCh[tr][dd];
+        l.bytes2 = listBytes(L_.fwdChance[tr][dd], tr, true);
         h.fwd[dd].push_back(l);
       }
       if (d.sdG[dd].count)
@@ -294,6 +295,7 @@ void Engine::buildPlans() {
                  listBytes(kindOnly(L_.bwdTasks[tr][dd], kTaskDecide), tr, false) +
                      listBytes(L_.bwdChance[tr][dd], tr, false)};
         l.list2 = d.bCh[tr][dd];
+        l.bytes2 = listBytes(L_.bwdChance[tr][dd], tr, false);
         h.bwd[dd].push_back(l);
       }
     }
@@ -489,17 +491,21 @@ std::vector<Engine::KernelStat> Engine::profile(int n, bool splitKinds) {
   std::vector<std::pair<Launch, std::string>> P;
   for (const Launch& l : d.plan[engineKind_]) {
     if (splitKinds && (l.kind == kFwdMix || l.kind == kBwdMix)) {
-      // The level's records and chance tasks as two launches.
+      // The level's records and chance records as two launches of the
+      // same kernel.
       const bool fwd = l.kind == kFwdMix;
-      double chBytes = 0;
-      for (int j = l.list2.off; j < l.list2.off + l.list2.count; ++j)
-        chBytes += taskBytes(d.hostTasks[j], l.tr, fwd);
-      if (l.list.count)
-        P.push_back({Launch{fwd ? kFwdRec : kDecRec, l.tr, l.list, l.bytes - chBytes},
-                     fwd ? "fwd_decide" : "bwd_decide"});
-      if (l.list2.count)
-        P.push_back({Launch{fwd ? kFwd : kBwdInt, l.tr, l.list2, chBytes},
-                     fwd ? "fwd_chance" : "bwd_chance"});
+      if (l.list.count) {
+        Launch r = l;
+        r.list2 = ListRef{};
+        r.bytes = l.bytes - l.bytes2;
+        P.push_back({r, fwd ? "fwd_decide" : "bwd_decide"});
+      }
+      if (l.list2.count) {
+        Launch c = l;
+        c.list = ListRef{};
+        c.bytes = l.bytes2;
+        P.push_back({c, fwd ? "fwd_chance" : "bwd_chance"});
+      }
       continue;
     }
     const bool bwd = l.kind == kBwdTerm || l.kind == kBwdInt;

@@ -261,7 +261,8 @@ struct SlotRec {
   // keep the layout's order (terminal tasks first). The iteration uses the
   // terminal group lists (group ids relocated) and the interior lists.
   std::vector<std::vector<int>> fwd[2], bwd[2], inner[2];
-  std::vector<std::vector<int>> sdG, fdG, bCh[2], fCh[2];
+  std::vector<std::vector<int>> sdG, fdG;
+  std::vector<std::vector<uint32_t>> bCh[2], fCh[2];  // chance record offsets, relocated
   std::vector<std::vector<uint32_t>> bRec[2], fRec[2];  // record offsets, relocated
 };
 
@@ -572,6 +573,32 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
           for (int a = 0; a < na; ++a) r[4 + a] += rowOff;
         }
     }
+  // Chance records and their branch tables: rows, maps, table offsets.
+  const uint32_t recShift16 = (uint32_t)(off[rRec] / 4);
+  for (int tr = 0; tr < 2; ++tr) {
+    const uint32_t reachOff = (uint32_t)off[tr ? rReach1 : rReach0];
+    for (const auto& v : L.fwdChanceRecs[tr])
+      for (uint32_t o : v) {
+        uint32_t* r = &L.recPool[(size_t)o * 4];
+        r[0] += reachOff;
+        r[1] += reachOff;
+        r[2] += (uint32_t)off[rU16];
+      }
+    for (const auto& v : L.bwdChanceRecs[tr])
+      for (uint32_t o : v) {
+        uint32_t* r = &L.recPool[(size_t)o * 4];
+        r[0] += (uint32_t)off[rCfv];
+        r[3] += recShift16;
+      }
+  }
+  for (int tr = 0; tr < 2; ++tr)
+    for (const auto& tb : L.chanceTables[tr]) {
+      uint32_t* e = &L.recPool[(size_t)tb.first * 4];
+      for (int b = 0; b < tb.second; ++b) {
+        e[2 * b] += (uint32_t)off[rCfv];
+        e[2 * b + 1] += (uint32_t)off[rI16];
+      }
+    }
   put(aRecs, off[rRec], L.recPool.data(), L.recPool.size() * sizeof(uint32_t));
   for (int a : {aReg, aStr, aCfvF, aCfvD, aReachF0, aReachD0, aReachF1, aReachD1}) {
     const Region r = kArray[a].region;
@@ -607,14 +634,11 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   for (int tr = 0; tr < 2; ++tr) {
     rec.bRec[tr] = std::move(L.bwdRecs[tr]);
     rec.fRec[tr] = std::move(L.fwdRecs[tr]);
-    rec.bCh[tr] = std::move(L.bwdChance[tr]);
-    rec.fCh[tr] = std::move(L.fwdChance[tr]);
-    for (auto* lists : {&rec.bRec[tr], &rec.fRec[tr]})
+    rec.bCh[tr] = std::move(L.bwdChanceRecs[tr]);
+    rec.fCh[tr] = std::move(L.fwdChanceRecs[tr]);
+    for (auto* lists : {&rec.bRec[tr], &rec.fRec[tr], &rec.bCh[tr], &rec.fCh[tr]})
       for (auto& v : *lists)
         for (uint32_t& o : v) o += recShift;
-    for (auto* lists : {&rec.bCh[tr], &rec.fCh[tr]})
-      for (auto& v : *lists)
-        for (int& task : v) task = (int)((unsigned)task + nodeShift);
   }
   const unsigned groupShift = (unsigned)off[rGroup] << 8;
   rec.sdG = std::move(L.sdGroupTasks);
@@ -704,8 +728,8 @@ Lists gather(const std::map<int, SlotRec>& live, const std::vector<int>& slots, 
   for (int tr = 0; tr < 2; ++tr)
     for (int dd = 0; dd < D; ++dd) {
       if (iteration) {
-        out.fCh[tr].push_back(cat([&](const SlotRec& r) { return at(r.fCh[tr], dd); }));
-        out.bCh[tr].push_back(cat([&](const SlotRec& r) { return at(r.bCh[tr], dd); }));
+        out.fCh[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.fCh[tr], dd); }));
+        out.bCh[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.bCh[tr], dd); }));
         out.fRec[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.fRec[tr], dd); }));
         out.bRec[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.bRec[tr], dd); }));
       } else {

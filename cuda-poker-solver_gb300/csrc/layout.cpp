@@ -2,6 +2,7 @@
 #include "layout.h"
 
 #include <algorithm>
+#include <map>
 #include <numeric>
 #include <stdexcept>
 
@@ -320,6 +321,56 @@ HostLayout buildLayout(const Tree& t) {
       for (int c = 0; c < chunksOpp; ++c)
         L.fwdRecs[tr][nd.depth].push_back(
             addRecord(L.nodes[u].regQ, L.rows[u].reachQ[tr], nOpp, nd.na, 0, c, kids));
+    }
+  }
+  // Chance records: every row and table address a chance task needs, so a
+  // CTA reaches its data in two dependent loads.
+  //   forward, per branch: [parent reach row, child reach row (quads, the
+  //     traverser's layout), child -> parent slot map (u16 pool), n_child |
+  //     chanceQ << 16]
+  //   backward, per 128-combo chunk: [value row, n | branches << 16, chunk,
+  //     branch table (16-byte units)]; the table holds per branch [child
+  //     value row, parent -> child slot map (i16 pool)], once per node.
+  for (int tr = 0; tr < 2; ++tr) {
+    const int opp = 1 - tr;
+    L.fwdChanceRecs[tr].assign(D, {});
+    L.bwdChanceRecs[tr].assign(D, {});
+    L.chanceTables[tr].clear();
+    std::map<int, uint32_t> table;  // node -> its branch table
+    for (int d = 0; d < D; ++d) {
+      for (int w : L.fwdChance[tr][d]) {
+        const int u = (int)((unsigned)w >> 8), br = (w >> 2) & 63;
+        const int ch = t.children[t.nodes[u].childBase + br];
+        const StateDev& cs = L.states[t.nodes[ch].state];
+        const uint32_t off = (uint32_t)(L.recPool.size() / 4);
+        L.recPool.push_back(L.rows[u].reachQ[tr]);
+        L.recPool.push_back(L.rows[ch].reachQ[tr]);
+        L.recPool.push_back((uint32_t)cs.upOff[opp]);
+        L.recPool.push_back((uint32_t)cs.n[opp] | ((uint32_t)L.rows[u].chanceQ << 16));
+        L.fwdChanceRecs[tr][d].push_back(off);
+      }
+      for (int w : L.bwdChance[tr][d]) {
+        const int u = (int)((unsigned)w >> 8), chunk = (w >> 2) & 63;
+        const Node& nd = t.nodes[u];
+        auto it = table.find(u);
+        if (it == table.end()) {
+          const uint32_t toff = (uint32_t)(L.recPool.size() / 4);
+          for (int b = 0; b < nd.nChildren; ++b) {
+            const int ch = t.children[nd.childBase + b];
+            L.recPool.push_back(L.rows[ch].cfvQ);
+            L.recPool.push_back((uint32_t)L.states[t.nodes[ch].state].downOff[tr]);
+          }
+          while (L.recPool.size() % 4) L.recPool.push_back(0);
+          it = table.emplace(u, toff).first;
+          L.chanceTables[tr].push_back({toff, nd.nChildren});
+        }
+        const uint32_t off = (uint32_t)(L.recPool.size() / 4);
+        L.recPool.push_back(L.rows[u].cfvQ);
+        L.recPool.push_back((uint32_t)L.states[nd.state].n[tr] | ((uint32_t)nd.nChildren << 16));
+        L.recPool.push_back((uint32_t)chunk);
+        L.recPool.push_back(it->second);
+        L.bwdChanceRecs[tr][d].push_back(off);
+      }
     }
   }
   if (N >= (1 << 24)) throw Error{PPS_GB_E_MEMORY, "tree too large for 24-bit task node ids"};

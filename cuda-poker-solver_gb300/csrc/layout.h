@@ -121,6 +121,11 @@ struct HostLayout {
   // units); the chance tasks of those levels as task words.
   std::vector<uint32_t> recPool;
   std::vector<std::vector<uint32_t>> bwdRecs[2], fwdRecs[2];
+  // Chance records in the same pool (decide.cuh): forward one per branch,
+  // backward one per 128-combo chunk pointing at a per-node branch table.
+  std::vector<std::vector<uint32_t>> fwdChanceRecs[2], bwdChanceRecs[2];
+  // Branch tables: offset (16-byte units) and branch count.
+  std::vector<std::pair<uint32_t, int>> chanceTables[2];
   std::vector<std::vector<int>> bwdChance[2], fwdChance[2];
   int maxN = 0;        // largest list size (either side)
   int maxCardSeg = 0;  // longest card segment of any list

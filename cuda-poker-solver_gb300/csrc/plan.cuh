@@ -33,12 +33,12 @@ struct ListRef {
   int off = 0, count = 0;
 };
 
-enum LaunchKind { kFwd, kBwdTerm, kBwdInt, kSdGroup, kFdGroup, kDecRec, kFwdRec, kFwdMix,
-                  kBwdMix, kCounter, kBwdFused };
+enum LaunchKind { kFwd, kBwdTerm, kBwdInt, kSdGroup, kFdGroup, kFwdMix, kBwdMix, kCounter,
+                  kBwdFused };
 inline const char* launchName(LaunchKind k) {
-  static const char* names[] = {"fwd_level",  "bwd_terminal", "bwd_interior", "bwd_showdown",
-                                "bwd_fold",   "bwd_decide",   "fwd_decide",   "fwd_level",
-                                "bwd_interior", "counter",    "bwd_level"};
+  static const char* names[] = {"fwd_level", "bwd_terminal", "bwd_interior", "bwd_showdown",
+                                "bwd_fold",  "fwd_level",    "bwd_interior", "counter",
+                                "bwd_level"};
   return names[k];
 }
 
@@ -48,8 +48,9 @@ struct Launch {
   ListRef list;
   double bytes;           // algorithmic bytes of this launch (f32 rows)
   bool withNext = false;  // independent of the next launch: run both at once
-  ListRef list2{};        // kFwdMix / kBwdMix / kBwdFused: the chance words (list: records)
+  ListRef list2{};        // kFwdMix / kBwdMix / kBwdFused: chance records (list: decide records)
   ListRef list3{}, list4{};  // kBwdFused: the showdown and fold group tasks
+  double bytes2 = 0.0;    // list2's share of bytes (profile split)
   bool late = false;      // kFwdMix: late triggers (the fused plan)
   bool termWait = false;  // kBwdFused: its terminal groups wait for the previous grid
 };
@@ -67,7 +68,7 @@ struct PlanArgs {
   const int4* groups;     // terminal groups (TermGroup)
   size_t smemSd, smemFd;  // sdGroupSmem / fdGroupSmem(maxN)
   const uint32_t* recs;      // decide record pool
-  const uint32_t* recTasks;  // record offsets (kDecRec / kFwdRec lists index these)
+  const uint32_t* recTasks;  // record offsets (the record and chance lists index these)
 };
 
 inline unsigned gridOf(int count) { return (unsigned)std::min(count, 1 << 20); }
@@ -96,14 +97,6 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
     case kFdGroup:
       launchFdGroups(g, a.smemFd, s, a.tree, a.rows, a.groups, tk, l.list.count, l.tr, a.maxN);
       break;
-    case kDecRec:
-      decideRecK<<<gridOf(recordCtas(l.list.count)), kThreads, bwdStageBytes(), s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
-                                        l.list.count);
-      break;
-    case kFwdRec:
-      fwdDecideRecK<<<gridOf(recordCtas(l.list.count)), kThreads, fwdStageBytes(), s>>>(a.tree, a.rows, a.recs, a.recTasks + l.list.off,
-                                           l.list.count, l.tr);
-      break;
     case kBwdFused: {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(gridOf(recordCtas(l.list.count) + l.list2.count + l.list3.count +
@@ -117,7 +110,7 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       cfg.attrs = attr;
       cfg.numAttrs = 1;
       GB_CK(cudaLaunchKernelEx(&cfg, bwdLevelFusedK, a.tree, a.rows, a.recs,
-                               a.recTasks + l.list.off, l.list.count, a.tasks + l.list2.off,
+                               a.recTasks + l.list.off, l.list.count, a.recTasks + l.list2.off,
                                l.list2.count, a.groups, a.tasks + l.list3.off, l.list3.count,
                                a.tasks + l.list4.off, l.list4.count, l.tr, a.maxN,
                                l.termWait ? 1 : 0));
@@ -139,7 +132,7 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       cfg.attrs = attr;
       cfg.numAttrs = 1;
       const uint32_t* rt = a.recTasks + l.list.off;
-      const int* ch = a.tasks + l.list2.off;
+      const uint32_t* ch = a.recTasks + l.list2.off;  // chance record offsets
       if (l.kind == kFwdMix)
         GB_CK(cudaLaunchKernelEx(&cfg, fwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
                                  ch, l.list2.count, l.tr, l.late ? 1 : 0));

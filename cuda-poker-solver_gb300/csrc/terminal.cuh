@@ -418,7 +418,7 @@ constexpr int kFusedMaxN = kSpan * kThreads - 1;  // widest list of a 128-thread
 
 static __global__ void __launch_bounds__(kThreads, 6)
 bwdLevelFusedK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
-               const uint32_t* __restrict__ recTasks, int nRec, const int* __restrict__ chance,
+               const uint32_t* __restrict__ recTasks, int nRec, const uint32_t* __restrict__ chance,
                int nCh, const int4* __restrict__ groups, const int* __restrict__ sd, int nSd,
                const int* __restrict__ fd, int nFd, int tr, int maxN, int termWait) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -427,6 +427,7 @@ bwdLevelFusedK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs
   const bool groupsWait = termWait || e2 == 0;
   bool waited = false;
   for (int i = blockIdx.x; i < e4; i += gridDim.x) {
+    if (i != (int)blockIdx.x) __syncthreads();  // shared memory of the last task
     if (i < e1) {
       const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
       if (k < nRec) {
@@ -436,10 +437,12 @@ bwdLevelFusedK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs
         decideRecordStaged(t, rows, r, lane, reinterpret_cast<float4*>(smem));
       }
     } else if (i < e2) {
-      const int w = chance[i - e1];
+      const uint4 h = loadChanceHeader(recs, chance[i - e1]);
+      chanceRecordTables(t, rows, recs, h, smem);
+      __syncthreads();
       pdlWait();
       waited = true;
-      chanceChunk<float>(t, rows, (int)((unsigned)w >> 8), (w >> 2) & 63, tr, smem);
+      chanceRecordSum(rows, h, smem);
       __syncthreads();  // the next task reuses the shared memory
     } else {
       const bool show = i < e3;
