@@ -283,6 +283,146 @@ __device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const De
 }
 
 // ---------------------------------------------------------------------------
+// Backward records staged by the bulk-copy engine: lane 0 of the warp asks
+// for every row segment of its record (up to 32 quads of each child value
+// row, and for the traverser's own node of each regret and strategy row)
+// with cp.async.bulk, counted on the warp's mbarrier; the lanes wait on the
+// barrier and compute from shared memory as decideRecordStaged does. The
+// wait is bounded: after kBarSpins polls the warp records an error in the
+// device error word and leaves the record, so a wait can never hang; once
+// the word is set, later records skip the copies and the wait altogether.
+// Layout per warp: [row kind][action][32 quads], contiguous segments.
+// ---------------------------------------------------------------------------
+constexpr int kBarSpins = 1 << 16;
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void barInit(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smemAddr(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void barExpect(unsigned long long* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulkLoad(void* dst, const float* src, uint32_t bytes,
+                                         unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smemAddr(dst)),
+      "l"(src), "r"(bytes), "r"(smemAddr(bar))
+      : "memory");
+}
+// True once the barrier's phase `parity` completed; false after kBarSpins
+// polls (each poll may itself wait a little: try_wait has a time limit).
+__device__ __forceinline__ bool barWait(unsigned long long* bar, uint32_t parity) {
+  for (int i = 0; i < kBarSpins; ++i) {
+    uint32_t done = 0;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smemAddr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// stage: this warp's segments; bar: this warp's barrier; phase: the
+// barrier's next parity (flipped here).
+__device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows<float>& rows,
+                                                 const DecRec& r, int lane, float4* stage,
+                                                 unsigned long long* bar, uint32_t& phase) {
+  const int na = r.na;
+  if (na > kAsyncNa) {
+    decideRecord(t, rows, r, lane);
+    return;
+  }
+  const int nq = quadsOf(r.n);
+  const int q0 = r.chunk * kRecQuads;
+  const int segQ = nq - q0 < kRecQuads ? nq - q0 : kRecQuads;  // >= 1: the record exists
+  const uint32_t segBytes = (uint32_t)segQ * 16u;
+  float4* C = stage;
+  float4* R = stage + kAsyncNa * kRecQuads;
+  float4* S = R + kAsyncNa * kRecQuads;
+  float* reg = t.regret + (size_t)r.regQ * 4;
+  float* str = t.strat + (size_t)r.regQ * 4;
+  int failed = lane == 0 && t.err ? *reinterpret_cast<volatile int*>(t.err) : 0;
+  if (__shfl_sync(0xffffffffu, failed, 0)) return;  // the same answer for every lane
+  __syncwarp();  // the lanes' reads of the last record's segments are done
+  if (lane == 0) {
+    // Earlier reads of the stage (generic proxy) before the copies (async proxy).
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    barExpect(bar, segBytes * (uint32_t)(r.own ? 3 * na : na));
+    for (int a = 0; a < na; ++a)
+      bulkLoad(&C[a * kRecQuads], rows.cfv + ((size_t)r.kid[a] + q0) * 4, segBytes, bar);
+    if (r.own)
+      for (int a = 0; a < na; ++a) {
+        const size_t o = ((size_t)a * nq + q0) * 4;
+        bulkLoad(&R[a * kRecQuads], reg + o, segBytes, bar);
+        bulkLoad(&S[a * kRecQuads], str + o, segBytes, bar);
+      }
+  }
+  const bool ok = barWait(bar, phase);
+  phase ^= 1u;
+  if (!ok) {
+    if (lane == 0 && t.err) atomicOr(t.err, 1);
+    return;
+  }
+  const int q = q0 + lane;
+  if (q >= nq) return;
+  float* out = rows.cfv + (size_t)r.rowQ * 4;
+  bool live[4];
+  for (int l = 0; l < 4; ++l) live[l] = 4 * q + l < r.n;
+  if (!r.own) {
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int a = 0; a < na; ++a) {
+      float c[4];
+      ld4s(&C[a * kRecQuads + lane], c);
+      for (int l = 0; l < 4; ++l) v[l] += c[l];
+    }
+    for (int l = 0; l < 4; ++l)
+      if (!live[l]) v[l] = 0.f;
+    stq(out + 4 * q, v);
+    return;
+  }
+  const float* c3 = t.coef + (size_t)t.counter[r.spot] * 3;
+  const float pos = c3[0], neg = c3[1], avg = c3[2];
+  const float uniform = 1.f / (float)na;
+  float val[4] = {0.f, 0.f, 0.f, 0.f}, acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int a = 0; a < na; ++a) {
+    float x[4];
+    ld4s(&R[a * kRecQuads + lane], x);
+    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
+  }
+  for (int a = 0; a < na; ++a) {
+    float x[4], c[4];
+    ld4s(&R[a * kRecQuads + lane], x);
+    ld4s(&C[a * kRecQuads + lane], c);
+    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, 0) : 0.f) * c[l];
+  }
+  stq(out + 4 * q, val);
+  for (int a = 0; a < na; ++a) {
+    float rg[4], sg[4], c[4];
+    const size_t o = ((size_t)a * nq + q) * 4;
+    ld4s(&R[a * kRecQuads + lane], rg);
+    ld4s(&S[a * kRecQuads + lane], sg);
+    ld4s(&C[a * kRecQuads + lane], c);
+    for (int l = 0; l < 4; ++l) {
+      const float s = live[l] ? sigmaOf(rg[l], acc[l], uniform, 0) : 0.f;
+      sg[l] = sg[l] * avg + s;
+      rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
+    }
+    stq(str + o, sg);
+    stq(reg + o, rg);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Chance records (layout.cpp): the arithmetic of fwdChanceBranch /
 // chanceChunk (kernels.cuh) with every address resolved on the host. The
 // record header is static data, read before the kernel waits for the
@@ -366,8 +506,10 @@ __host__ __device__ inline int recordCtas(int records) {
 __host__ __device__ constexpr size_t fwdStageBytes() {
   return (size_t)(1 + kAsyncNa) * kThreads * sizeof(float4);
 }
+// Backward: the staging buffers, then one mbarrier per warp.
 __host__ __device__ constexpr size_t bwdStageBytes() {
-  return recStageBytes() > kChanceScratchBytes ? recStageBytes() : kChanceScratchBytes;
+  return (recStageBytes() > kChanceScratchBytes ? recStageBytes() : kChanceScratchBytes) +
+         kRecWarps * sizeof(unsigned long long);
 }
 
 // ---------------------------------------------------------------------------
@@ -427,6 +569,12 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
   extern __shared__ __align__(16) unsigned char smem[];  // bwdStageBytes()
   pdlTrigger();
   const int nRc = recordCtas(nRec), lane = (int)threadIdx.x & 31;
+  const int warp = (int)(threadIdx.x >> 5);
+  unsigned long long* bar =
+      reinterpret_cast<unsigned long long*>(smem + bwdStageBytes()) - kRecWarps + warp;
+  if (lane == 0) barInit(bar);
+  __syncwarp();
+  uint32_t phase = 0;
   for (int i = blockIdx.x; i < nRc + nCh; i += gridDim.x) {
     // A CTA that runs more than one task (grids past 2^20 CTAs) must not
     // overwrite shared memory that its warps still read for the last one.
@@ -436,7 +584,9 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       if (k >= nRec) continue;
       const DecRec r = loadRec(recs, recTasks[k]);
       pdlWait();
-      decideRecordStaged(t, rows, r, lane, reinterpret_cast<float4*>(smem));
+      decideRecordBulk(t, rows, r, lane,
+                       reinterpret_cast<float4*>(smem) + warp * 3 * kAsyncNa * kRecQuads, bar,
+                       phase);
     } else {
       const uint4 h = loadChanceHeader(recs, chance[i - nRc]);
       chanceRecordTables(t, rows, recs, h, smem);

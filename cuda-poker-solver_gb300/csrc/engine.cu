@@ -135,6 +135,8 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
   d.coef = d.own(alloc<float>(d.coefCap * 3, B));
   d.tree.counter = d.counter;
   d.tree.coef = d.coef;
+  d.tree.err = d.own(alloc<int>(1, B));
+  GB_CK(cudaMemset(d.tree.err, 0, sizeof(int)));
 
   // Root reach rows: the opponent's range weights (padding zero).
   for (int tr = 0; tr < 2; ++tr) {
@@ -464,7 +466,20 @@ void Engine::iterate(int n) {
   for (int i = 0; i < n; ++i) GB_CK(cudaGraphLaunch(d.exec, d.stream));
 }
 
-void Engine::sync() { GB_CK(cudaStreamSynchronize(d_->stream)); }
+void Engine::sync() {
+  GB_CK(cudaStreamSynchronize(d_->stream));
+  checkDeviceError();
+}
+
+// A bounded wait in a kernel gave up (its results are not valid).
+void Engine::checkDeviceError() {
+  int e = 0;
+  GB_CK(cudaMemcpy(&e, d_->tree.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    GB_CK(cudaMemset(d_->tree.err, 0, sizeof(int)));
+    throw Error{PPS_GB_E_CUDA, "a device wait timed out (bulk copy never completed)"};
+  }
+}
 
 double Engine::timeIterations(int n) {
   Dev& d = *d_;
@@ -480,6 +495,7 @@ double Engine::timeIterations(int n) {
   GB_CK(cudaEventElapsedTime(&ms, a, b));
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  checkDeviceError();
   return ms;
 }
 

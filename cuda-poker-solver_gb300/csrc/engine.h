@@ -30,6 +30,7 @@ class Engine {
   // Enqueues n iterations (graph replays); returns without waiting.
   void iterate(int n);
   void sync();
+  void checkDeviceError();
   // Runs one FP64 walk (mode 1 = average-strategy EV, 2 = best response)
   // for traverser tr and waits for it; rows stay readable afterwards.
   void walk(int tr, int mode);

@@ -280,6 +280,7 @@ struct Forest::Dev {
   int coefEntries = 0;
   int* counter = nullptr;
   size_t counterCap = 0;
+  int* err = nullptr;  // device error word (a bounded wait gave up)
   std::vector<int> freeSlots;
   int nextSlot = 0;
   std::map<int, SlotRec> live;
@@ -323,6 +324,7 @@ struct Forest::Dev {
     t.strat = static_cast<float*>(arr[aStr]);
     t.coef = coef;
     t.counter = counter;
+    t.err = err;
     return t;
   }
   template <typename T>
@@ -420,6 +422,8 @@ Forest::Forest(const std::vector<float>& coef, size_t maxBytes) : d_(new Dev()) 
     d.arr[a] = reinterpret_cast<void*>(d.va[a].base);
   }
   GB_CK(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
+  GB_CK(cudaMalloc(&d.err, sizeof(int)));
+  GB_CK(cudaMemset(d.err, 0, sizeof(int)));
   d.br.create(d.stream);
   GB_CK(cudaEventCreate(&d.evA));
   GB_CK(cudaEventCreate(&d.evB));
@@ -449,6 +453,7 @@ Forest::~Forest() {
   cudaFree(d.counter);
   cudaFree(d.tasks);
   cudaFree(d.recTasks);
+  cudaFree(d.err);
   cudaFree(d.wTasks);
   cudaFree(d.info);
   cudaFree(d.vals);
@@ -826,6 +831,12 @@ double Forest::lastIterateMs() {
   GB_CK(cudaEventSynchronize(d.evB));
   float ms = 0.0f;
   GB_CK(cudaEventElapsedTime(&ms, d.evA, d.evB));
+  int e = 0;
+  GB_CK(cudaMemcpy(&e, d.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    GB_CK(cudaMemset(d.err, 0, sizeof(int)));
+    throw Error{PPS_GB_E_CUDA, "forest: a device wait timed out (bulk copy never completed)"};
+  }
   return ms;
 }
 

@@ -46,6 +46,7 @@ struct DevTree {
   const float* coef;     // 3 floats per iteration: pos, neg, avg
   const int* counter;    // current iteration index, per spot (node meta
                          // bits 16-31; a lone spot is spot 0)
+  int* err;              // device error word: a bounded wait gave up (0: none)
 };
 
 template <typename T>
