@@ -121,3 +121,56 @@ def test_oneshot_served_by_the_batch(svc):
     own = svc.solve_oneshot(dict(SPOT, max_iters=200, strategy_nodes=[0], root_ev=True))
     assert own["served_by"] == "solver" and "0" in {str(k) for k in own["strategies"]}
     assert "root_ev" in own
+
+
+def test_paths_navigation_and_runouts(svc):
+    """The reference API's navigation behaviour (python/test_pps_api.py:
+    165-276): action paths with card-labelled deals, node-nav labels, a
+    flop deal with 49 runouts (card 2c included, none on the board), and a
+    runout summary consistent with node_ev at each branch."""
+    sid = svc.create_solver(SPOT)["id"]
+    svc.solve(sid, {"max_iters": 200})
+    paths = [n["path"] for n in svc.decide_nodes(sid, 0, 50)["nodes"]]
+    assert paths[0] == "(root)" and paths[1].startswith("check")
+    deals = [p for p in paths if "deal" in p]
+    assert deals
+    for p in deals:
+        for step in p.split(" — "):
+            if step.startswith("deal "):
+                card = step[5:]
+                assert len(card) == 2 and card[0] in "23456789TJQKA" and card[1] in "cdhs"
+    assert svc.decide_nodes(sid, 1, 1)["nodes"][0]["index"] == 1
+    nav = svc.node_nav(sid, 0)
+    assert {a["label"] for a in nav["actions"]} == {"check", "bet 150", "all-in"}
+    assert next(a for a in nav["actions"] if a["label"] == "check")["next_decide"] == 1
+    nav1 = {a["kind"]: a for a in svc.node_nav(sid, 1)["actions"]}
+    assert "fold" not in nav1 and nav1["check"]["next_decide"] is not None
+    rng = svc.range(sid, 0)
+    assert all(len(c) == 4 for c in rng["combos"]) and sum(rng["weights"]) > 0
+    st, ev0 = svc.stats(sid), svc.node_ev(sid, 0)
+    assert abs(ev0["sides"]["oop"]["agg_ev"] - st["ev_oop"]) < 1e-4
+    assert abs(ev0["sides"]["ip"]["agg_ev"] - st["ev_ip"]) < 1e-4
+    with pytest.raises(ServiceError) as e:
+        svc.node_ev(sid, 99999)
+    assert e.value.status == 400
+
+    fid = svc.create_solver(dict(SPOT, board="Qs9h2d"))["id"]
+    svc.solve(fid, {"max_iters": 100})
+    nav = svc.node_nav(fid, 1)
+    check = next(a for a in nav["actions"] if a["kind"] == "check")
+    assert check["child_kind"] == "chance"
+    cards = [b["card"] for b in check["branches"]]
+    assert len(cards) == len(set(cards)) == 49 and "2c" in cards and "?" not in cards
+    assert not set(cards) & {"Qs", "9h", "2d"}
+    rs = svc.runout_summary(fid, 1, [a["kind"] for a in nav["actions"]].index("check"))
+    assert rs["decider"] == 0 and [b["card"] for b in rs["branches"]] == cards
+    live = [b for b in rs["branches"] if b["next_decide"] >= 0]
+    assert len(live) == 49
+    for b in live:
+        assert len(b["freq"]) == len(rs["actions"]) and abs(sum(b["freq"]) - 1.0) < 1e-5
+    first = live[0]
+    nev = svc.node_ev(fid, first["next_decide"])
+    assert abs(nev["sides"]["oop"]["agg_ev"] - first["agg_ev"]["oop"]) < 1e-3
+    with pytest.raises(ServiceError) as e:
+        svc.runout_summary(fid, 0, 0)  # not a deal
+    assert e.value.status == 400
