@@ -292,8 +292,20 @@ __device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const De
 // device error word and leaves the record, so a wait can never hang; once
 // the word is set, later records skip the copies and the wait altogether.
 // Layout per warp: [row kind][action][32 quads], contiguous segments.
+//
+// The record waits for the previous level itself (griddepcontrol.wait),
+// between its two groups of copies. The regret and strategy rows of the
+// traverser's own node are written by this pass at this level only, in an
+// earlier iteration, and every iteration ends with a launch that has no
+// programmatic dependency (advanceCounterK), so those writes are complete
+// when the record starts: their copies go out before the wait and overlap
+// the previous level's tail. The child value rows are the previous level's
+// output: their copies go out after the wait.
 // ---------------------------------------------------------------------------
 constexpr int kBarSpins = 1 << 16;
+
+__device__ __forceinline__ void pdlTrigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 __device__ __forceinline__ uint32_t smemAddr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -339,6 +351,7 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
                                                  unsigned long long* bar, uint32_t& phase) {
   const int na = r.na;
   if (na > kAsyncNa) {
+    pdlWait();
     decideRecord(t, rows, r, lane);
     return;
   }
@@ -358,8 +371,6 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
     // Earlier reads of the stage (generic proxy) before the copies (async proxy).
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     barExpect(bar, segBytes * (uint32_t)(r.own ? 3 * na : na));
-    for (int a = 0; a < na; ++a)
-      bulkLoad(&C[a * kRecQuads], rows.cfv + ((size_t)r.kid[a] + q0) * 4, segBytes, bar);
     if (r.own)
       for (int a = 0; a < na; ++a) {
         const size_t o = ((size_t)a * nq + q0) * 4;
@@ -367,6 +378,10 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
         bulkLoad(&S[a * kRecQuads], str + o, segBytes, bar);
       }
   }
+  pdlWait();
+  if (lane == 0)
+    for (int a = 0; a < na; ++a)
+      bulkLoad(&C[a * kRecQuads], rows.cfv + ((size_t)r.kid[a] + q0) * 4, segBytes, bar);
   const bool ok = barWait(bar, phase);
   phase ^= 1u;
   if (!ok) {
@@ -521,11 +536,10 @@ __host__ __device__ constexpr size_t bwdStageBytes() {
 // start (launch_dependents), loads its record (static data), then waits
 // until the previous level's grid has finished and its writes are visible
 // (griddepcontrol.wait) before touching rows. Without a programmatic
-// dependency the wait returns at once.
+// dependency the wait returns at once. A backward decide record also asks
+// for its own node's regret and strategy rows before the wait
+// (decideRecordBulk).
 // ---------------------------------------------------------------------------
-
-__device__ __forceinline__ void pdlTrigger() { asm volatile("griddepcontrol.launch_dependents;"); }
-__device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // late: each CTA lets the next grid launch only once its own wait has
 // returned (so a grid that has launched implies that the grid two places
@@ -583,8 +597,7 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
       if (k >= nRec) continue;
       const DecRec r = loadRec(recs, recTasks[k]);
-      pdlWait();
-      decideRecordBulk(t, rows, r, lane,
+      decideRecordBulk(t, rows, r, lane,  // waits for the previous level itself
                        reinterpret_cast<float4*>(smem) + warp * 3 * kAsyncNa * kRecQuads, bar,
                        phase);
     } else {
