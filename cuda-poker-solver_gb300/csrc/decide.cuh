@@ -244,11 +244,27 @@ __device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRo
   }
 }
 
+// Forward decide record, first part: the copies of the node's regret rows
+// into the staging buffer (a no-op for records that are not staged).
+__device__ __forceinline__ void fwdRecordRegrets(const DevTree& t, const DecRec& r, int lane,
+                                                 float4* stage) {
+  const int na = r.na;
+  if (na > kAsyncNa) return;
+  const int nq = quadsOf(r.n);
+  const int q = r.chunk * kRecQuads + lane;
+  if (q >= nq) return;
+  float4* R = stage + kThreads;  // [action][thread]
+  const float* src = t.regret + (size_t)r.regQ * 4;
+  for (int a = 0; a < na; ++a)
+    cpAsync16(&R[a * kThreads + (int)threadIdx.x], src + ((size_t)a * nq + q) * 4);
+}
+
 // Forward decide record, staged (same arithmetic and order as
-// fwdDecideRecord).
+// fwdDecideRecord). regretsIssued: fwdRecordRegrets already ran for this
+// record.
 __device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const DevRows<float>& rows,
                                                       int tr, const DecRec& r, int lane,
-                                                      float4* stage) {
+                                                      float4* stage, bool regretsIssued) {
   const int na = r.na;
   if (na > kAsyncNa) {
     fwdDecideRecord(t, rows, tr, r, lane);
@@ -260,10 +276,8 @@ __device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const De
   const int tid = (int)threadIdx.x;
   float4* RR = stage;                     // [thread]
   float4* R = stage + kThreads;           // [action][thread]
-  const float* src = t.regret + (size_t)r.regQ * 4;
   cpAsync16(&RR[tid], rows.reach[tr] + (size_t)r.rowQ * 4 + 4 * q);
-  for (int a = 0; a < na; ++a)
-    cpAsync16(&R[a * kThreads + tid], src + ((size_t)a * nq + q) * 4);
+  if (!regretsIssued) fwdRecordRegrets(t, r, lane, stage);
   const float uniform = 1.f / (float)na;
   float rr[4], acc[4] = {0.f, 0.f, 0.f, 0.f};
   cpAsyncWaitAll();
@@ -545,10 +559,16 @@ __host__ __device__ constexpr size_t bwdStageBytes() {
 // returned (so a grid that has launched implies that the grid two places
 // before it has completed; the fused plan relies on that), instead of at
 // its start.
+// early: the records ask for their regret rows before the wait. Only for
+// the first half-step of an iteration (traverser 0): the regrets it reads
+// are the other player's, written by the second half-step of an earlier
+// iteration, and every iteration ends with a launch that has no
+// programmatic dependency (advanceCounterK). The second half-step reads
+// regrets that the first one has just written.
 static __global__ void __launch_bounds__(kThreads, 10)
 fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
              const uint32_t* __restrict__ recTasks, int nRec, const uint32_t* __restrict__ chance,
-             int nCh, int tr, int late) {
+             int nCh, int tr, int late, int early) {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* stage = reinterpret_cast<float4*>(smem);
   if (!late) pdlTrigger();
@@ -559,9 +579,10 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
       if (k >= nRec) continue;
       const DecRec r = loadRec(recs, recTasks[k]);
+      if (early) fwdRecordRegrets(t, r, lane, stage);
       pdlWait();
       waited = true;
-      fwdDecideRecordStaged(t, rows, tr, r, lane, stage);
+      fwdDecideRecordStaged(t, rows, tr, r, lane, stage, early != 0);
     } else {
       const uint4 h = loadChanceHeader(recs, chance[i - nRc]);
       pdlWait();

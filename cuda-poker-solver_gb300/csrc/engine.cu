@@ -286,6 +286,7 @@ void Engine::buildPlans() {
                      listBytes(L_.fwdChance[tr][dd], tr, true)};
         l.list2 = d.fCh[tr][dd];
         l.bytes2 = listBytes(L_.fwdChance[tr][dd], tr, true);
+        l.early = tr == 0;  // the first half-step of the iteration
         h.fwd[dd].push_back(l);
       }
       if (d.sdG[dd].count)

@@ -781,6 +781,7 @@ void Forest::iterate(int n) {
         if (ls.fRec[tr][dd].count || ls.fCh[tr][dd].count) {
           Launch l{kFwdMix, tr, ls.fRec[tr][dd], 0.0};
           l.list2 = ls.fCh[tr][dd];
+          l.early = tr == 0;  // the first half-step of the iteration
           h.fwd[dd].push_back(l);
         }
         if (ls.sdG[dd].count) h.sd[dd] = {kSdGroup, tr, ls.sdG[dd], 0.0};

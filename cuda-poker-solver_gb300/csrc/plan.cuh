@@ -52,6 +52,7 @@ struct Launch {
   ListRef list3{}, list4{};  // kBwdFused: the showdown and fold group tasks
   double bytes2 = 0.0;    // list2's share of bytes (profile split)
   bool late = false;      // kFwdMix: late triggers (the fused plan)
+  bool early = false;     // kFwdMix: regret copies before the wait (first half-step only)
   bool termWait = false;  // kBwdFused: its terminal groups wait for the previous grid
 };
 
@@ -135,7 +136,7 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       const uint32_t* ch = a.recTasks + l.list2.off;  // chance record offsets
       if (l.kind == kFwdMix)
         GB_CK(cudaLaunchKernelEx(&cfg, fwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
-                                 ch, l.list2.count, l.tr, l.late ? 1 : 0));
+                                 ch, l.list2.count, l.tr, l.late ? 1 : 0, l.early ? 1 : 0));
       else
         GB_CK(cudaLaunchKernelEx(&cfg, bwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
                                  ch, l.list2.count, l.tr));
