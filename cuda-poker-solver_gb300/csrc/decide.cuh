@@ -170,8 +170,33 @@ __device__ __forceinline__ void ld4s(const float4* p, float (&x)[4]) {
   x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
 }
 
+// Backward decide record, staged, first part: the copies of the regret and
+// strategy rows of the traverser's own node (nothing for another node or a
+// record that is not staged). Those rows are written only by the backward
+// pass of this level in an earlier iteration, so the copies may go out
+// before the wait for the previous level.
+__device__ __forceinline__ void decideRecordOwnRows(const DevTree& t, const DecRec& r, int lane,
+                                                    float4* stage) {
+  const int na = r.na;
+  if (na > kAsyncNa || !r.own) return;
+  const int nq = quadsOf(r.n);
+  const int q = r.chunk * kRecQuads + lane;
+  if (q >= nq) return;
+  const int tid = (int)threadIdx.x;
+  float4* R = stage + kAsyncNa * kThreads;
+  float4* S = R + kAsyncNa * kThreads;
+  const float* reg = t.regret + (size_t)r.regQ * 4;
+  const float* str = t.strat + (size_t)r.regQ * 4;
+  for (int a = 0; a < na; ++a) {
+    const size_t o = ((size_t)a * nq + q) * 4;
+    cpAsync16(&R[a * kThreads + tid], reg + o);
+    cpAsync16(&S[a * kThreads + tid], str + o);
+  }
+}
+
 // Backward decide record, staged (same arithmetic and order as
-// decideRecord).
+// decideRecord), after decideRecordOwnRows and the wait for the previous
+// level: the child value copies, then the update.
 __device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRows<float>& rows,
                                                    const DecRec& r, int lane, float4* stage) {
   const int na = r.na;
@@ -206,11 +231,6 @@ __device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRo
   }
   float* reg = t.regret + (size_t)r.regQ * 4;
   float* str = t.strat + (size_t)r.regQ * 4;
-  for (int a = 0; a < na; ++a) {
-    const size_t o = ((size_t)a * nq + q) * 4;
-    cpAsync16(&R[a * kThreads + tid], reg + o);
-    cpAsync16(&S[a * kThreads + tid], str + o);
-  }
   const float* c3 = t.coef + (size_t)t.counter[r.spot] * 3;
   const float pos = c3[0], neg = c3[1], avg = c3[2];
   const float uniform = 1.f / (float)na;

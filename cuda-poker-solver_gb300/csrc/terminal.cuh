@@ -432,6 +432,7 @@ bwdLevelFusedK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs
       const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
       if (k < nRec) {
         const DecRec r = loadRec(recs, recTasks[k]);
+        decideRecordOwnRows(t, r, lane, reinterpret_cast<float4*>(smem));
         pdlWait();
         waited = true;
         decideRecordStaged(t, rows, r, lane, reinterpret_cast<float4*>(smem));
