@@ -483,12 +483,32 @@ __device__ __forceinline__ uint4 loadChanceHeader(const uint32_t* __restrict__ r
 }
 
 // Forward: child reach = parent reach through the child -> parent slot map,
-// scaled by 1 / chanceQ (cuda/gpu_cfr.cu:276-293).
+// scaled by 1 / chanceQ (cuda/gpu_cfr.cu:276-293). The slot map is static:
+// before the wait for the previous level, each thread copies its own
+// entries of it into shared memory (fwdChanceSlots); after the wait, one
+// dependent load per entry remains.
+__device__ __forceinline__ bool fwdChanceStaged(uint4 h, size_t stageBytes) {
+  return (size_t)quadsOf((int)(h.w & 0xffff)) * 4 * sizeof(uint16_t) <= stageBytes;
+}
+// Thread t copies the entries of the quads it writes in fwdChanceRecord
+// (quads t, t + blockDim.x, ...), so it reads back only its own copies.
+__device__ __forceinline__ void fwdChanceSlots(const DevTree& t, uint4 h, uint16_t* upS) {
+  const int nc = (int)(h.w & 0xffff);
+  const uint16_t* up = t.poolU16 + h.z;
+  for (int q = threadIdx.x; q < quadsOf(nc); q += blockDim.x) {
+    uint16_t v[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) v[l] = 4 * q + l < nc ? up[4 * q + l] : (uint16_t)0;
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+      if (4 * q + l < nc) upS[4 * q + l] = v[l];
+  }
+}
 __device__ __forceinline__ void fwdChanceRecord(const DevTree& t, const DevRows<float>& rows,
-                                                int tr, uint4 h) {
+                                                int tr, uint4 h, const uint16_t* upS) {
   const int nc = (int)(h.w & 0xffff);
   const float inv = 1.f / (float)(h.w >> 16);
-  const uint16_t* up = t.poolU16 + h.z;
+  const uint16_t* up = upS ? upS : t.poolU16 + h.z;
   const float* pr = rows.reach[tr] + (size_t)h.x * 4;
   float* cr = rows.reach[tr] + (size_t)h.y * 4;
   for (int q = threadIdx.x; q < quadsOf(nc); q += blockDim.x) {
@@ -503,6 +523,10 @@ __device__ __forceinline__ void fwdChanceRecord(const DevTree& t, const DevRows<
 
 // Backward, first part (static data, before the wait): the branch table
 // into shared memory (child value rows and parent -> child slot maps).
+// Layout: rowOf[64] | downOf[64] | slot[64][kChanceChunk] (int16).
+constexpr int kChanceMaxBranches = 64;  // a chance node has at most 49 branches
+constexpr size_t kChanceStageBytes =
+    kChanceScratchBytes + (size_t)kChanceMaxBranches * kChanceChunk * sizeof(int16_t);
 __device__ __forceinline__ void chanceRecordTables(const DevTree& t, const DevRows<float>& rows,
                                                    const uint32_t* __restrict__ recs, uint4 h,
                                                    unsigned char* smem) {
@@ -516,28 +540,49 @@ __device__ __forceinline__ void chanceRecordTables(const DevTree& t, const DevRo
   }
 }
 
-// Backward, second part (after __syncthreads and the wait): parent value of
-// one 128-combo chunk = sum over the branches (cuda/gpu_cfr.cu:542-554).
+// Backward, second part (static data, after a __syncthreads, still before
+// the wait): each thread's slot in every branch's child row, slot[b][thread]
+// (-1: the branch blocks the combo). A thread reads back only its own
+// column.
+__device__ __forceinline__ void chanceRecordSlots(uint4 h, unsigned char* smem) {
+  const int n = (int)(h.y & 0xffff), nb = (int)(h.y >> 16);
+  const int16_t* const* downOf =
+      reinterpret_cast<const int16_t* const*>(smem + 64 * sizeof(void*));
+  int16_t* slot = reinterpret_cast<int16_t*>(smem + kChanceScratchBytes);
+  const int i = (int)h.z * kChanceChunk + (int)threadIdx.x;
+  if (i >= n) return;
+  for (int b0 = 0; b0 < nb; b0 += 16) {  // 16 loads in flight, then their stores
+    int16_t v[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = b0 + j < nb ? downOf[b0 + j][i] : (int16_t)-1;
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      if (b0 + j < nb) slot[(b0 + j) * kChanceChunk + threadIdx.x] = v[j];
+  }
+}
+
+// Backward, last part (after the wait): parent value of one 128-combo
+// chunk = sum over the branches in branch order (cuda/gpu_cfr.cu:542-554),
+// 16 branch loads in flight per thread.
 __device__ __forceinline__ void chanceRecordSum(const DevRows<float>& rows, uint4 h,
                                                 const unsigned char* smem) {
   const int n = (int)(h.y & 0xffff), nb = (int)(h.y >> 16);
   const float* const* rowOf = reinterpret_cast<const float* const*>(smem);
-  const int16_t* const* downOf =
-      reinterpret_cast<const int16_t* const*>(smem + 64 * sizeof(void*));
+  const int16_t* slot = reinterpret_cast<const int16_t*>(smem + kChanceScratchBytes);
   float* out = rows.cfv + (size_t)h.x * 4;
   const int i = (int)h.z * kChanceChunk + (int)threadIdx.x;
   if (i >= quadsOf(n) * 4) return;
   float v = 0.f;
   if (i < n) {
-    for (int b0 = 0; b0 < nb; b0 += 8) {
-      int k[8];
+    for (int b0 = 0; b0 < nb; b0 += 16) {
+      float x[16];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) k[j] = b0 + j < nb ? downOf[b0 + j][i] : -1;
-      float x[8];
+      for (int j = 0; j < 16; ++j) {
+        const int k = b0 + j < nb ? slot[(b0 + j) * kChanceChunk + threadIdx.x] : -1;
+        x[j] = k >= 0 ? rowOf[b0 + j][k] : 0.f;
+      }
 #pragma unroll
-      for (int j = 0; j < 8; ++j) x[j] = k[j] >= 0 ? rowOf[b0 + j][k[j]] : 0.f;
-#pragma unroll
-      for (int j = 0; j < 8; ++j) v += x[j];
+      for (int j = 0; j < 16; ++j) v += x[j];
     }
   }
   out[i] = v;
@@ -555,9 +600,10 @@ __host__ __device__ inline int recordCtas(int records) {
 __host__ __device__ constexpr size_t fwdStageBytes() {
   return (size_t)(1 + kAsyncNa) * kThreads * sizeof(float4);
 }
-// Backward: the staging buffers, then one mbarrier per warp.
+// Backward: the staging buffers (records, or a chance chunk's tables),
+// then one mbarrier per warp.
 __host__ __device__ constexpr size_t bwdStageBytes() {
-  return (recStageBytes() > kChanceScratchBytes ? recStageBytes() : kChanceScratchBytes) +
+  return (recStageBytes() > kChanceStageBytes ? recStageBytes() : kChanceStageBytes) +
          kRecWarps * sizeof(unsigned long long);
 }
 
@@ -605,9 +651,13 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       fwdDecideRecordStaged(t, rows, tr, r, lane, stage, early != 0);
     } else {
       const uint4 h = loadChanceHeader(recs, chance[i - nRc]);
+      const bool st = fwdChanceStaged(h, fwdStageBytes());
+      uint16_t* upS = reinterpret_cast<uint16_t*>(smem);
+      if (i != (int)blockIdx.x) __syncthreads();  // the last task's slots are read
+      if (st) fwdChanceSlots(t, h, upS);
       pdlWait();
       waited = true;
-      fwdChanceRecord(t, rows, tr, h);
+      fwdChanceRecord(t, rows, tr, h, st ? upS : nullptr);
     }
     if (late) pdlTrigger();
   }
@@ -645,6 +695,7 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       const uint4 h = loadChanceHeader(recs, chance[i - nRc]);
       chanceRecordTables(t, rows, recs, h, smem);
       __syncthreads();
+      chanceRecordSlots(h, smem);
       pdlWait();
       chanceRecordSum(rows, h, smem);
       __syncthreads();  // the next chance task reuses the pointer tables

@@ -354,6 +354,8 @@ HostLayout buildLayout(const Tree& t) {
         const Node& nd = t.nodes[u];
         auto it = table.find(u);
         if (it == table.end()) {
+          // The record kernels hold one slot column per branch (64 at most).
+          if (nd.nChildren > 64) throw Error{PPS_GB_E_ARG, "chance node with more than 64 branches"};
           const uint32_t toff = (uint32_t)(L.recPool.size() / 4);
           for (int b = 0; b < nd.nChildren; ++b) {
             const int ch = t.children[nd.childBase + b];

@@ -441,6 +441,7 @@ bwdLevelFusedK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs
       const uint4 h = loadChanceHeader(recs, chance[i - e1]);
       chanceRecordTables(t, rows, recs, h, smem);
       __syncthreads();
+      chanceRecordSlots(h, smem);
       pdlWait();
       waited = true;
       chanceRecordSum(rows, h, smem);
