@@ -609,8 +609,9 @@ __host__ __device__ constexpr size_t bwdStageBytes() {
 
 // ---------------------------------------------------------------------------
 // Level kernels of the default iteration: one launch per level and pass
-// covering the level's decide records and chance records (CTA i <
-// recordCtas(nRec): one decide record per warp; else one chance record),
+// covering the level's chance records and decide records (CTA i < nCh: one
+// chance record, started first because its chain of loads is the longest;
+// else one decide record per warp),
 // launched with programmatic dependent
 // launch so consecutive levels overlap: each CTA lets the next level's grid
 // start (launch_dependents), loads its record (static data), then waits
@@ -640,9 +641,12 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
   if (!late) pdlTrigger();
   const int nRc = recordCtas(nRec), lane = (int)threadIdx.x & 31;
   bool waited = false;
-  for (int i = blockIdx.x; i < nRc + nCh; i += gridDim.x) {
-    if (i < nRc) {
-      const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
+  for (int i = blockIdx.x; i < nCh + nRc; i += gridDim.x) {
+    // A CTA that runs more than one task (grids past 2^20 CTAs) must not
+    // overwrite shared memory that its threads still read for the last one.
+    if (i != (int)blockIdx.x) __syncthreads();
+    if (i >= nCh) {
+      const int k = (i - nCh) * kRecWarps + (int)(threadIdx.x >> 5);
       if (k >= nRec) continue;
       const DecRec r = loadRec(recs, recTasks[k]);
       if (early) fwdRecordRegrets(t, r, lane, stage);
@@ -650,10 +654,9 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       waited = true;
       fwdDecideRecordStaged(t, rows, tr, r, lane, stage, early != 0);
     } else {
-      const uint4 h = loadChanceHeader(recs, chance[i - nRc]);
+      const uint4 h = loadChanceHeader(recs, chance[i]);
       const bool st = fwdChanceStaged(h, fwdStageBytes());
       uint16_t* upS = reinterpret_cast<uint16_t*>(smem);
-      if (i != (int)blockIdx.x) __syncthreads();  // the last task's slots are read
       if (st) fwdChanceSlots(t, h, upS);
       pdlWait();
       waited = true;
@@ -680,19 +683,19 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
   if (lane == 0) barInit(bar);
   __syncwarp();
   uint32_t phase = 0;
-  for (int i = blockIdx.x; i < nRc + nCh; i += gridDim.x) {
+  for (int i = blockIdx.x; i < nCh + nRc; i += gridDim.x) {
     // A CTA that runs more than one task (grids past 2^20 CTAs) must not
     // overwrite shared memory that its warps still read for the last one.
     if (i != (int)blockIdx.x) __syncthreads();
-    if (i < nRc) {
-      const int k = i * kRecWarps + (int)(threadIdx.x >> 5);
+    if (i >= nCh) {
+      const int k = (i - nCh) * kRecWarps + (int)(threadIdx.x >> 5);
       if (k >= nRec) continue;
       const DecRec r = loadRec(recs, recTasks[k]);
       decideRecordBulk(t, rows, r, lane,  // waits for the previous level itself
                        reinterpret_cast<float4*>(smem) + warp * 3 * kAsyncNa * kRecQuads, bar,
                        phase);
     } else {
-      const uint4 h = loadChanceHeader(recs, chance[i - nRc]);
+      const uint4 h = loadChanceHeader(recs, chance[i]);
       chanceRecordTables(t, rows, recs, h, smem);
       __syncthreads();
       chanceRecordSlots(h, smem);
