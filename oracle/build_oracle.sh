@@ -1,6 +1,6 @@
 #!/bin/sh
-# Builds the CPU oracle (test infrastructure: the checker of the GPU
-# solver and the bench's CPU baseline) into oracle/_build/liboracle.so, and
+# Builds the CPU oracle (test infrastructure: the reference against which
+# the GPU solver is tested, and the bench's CPU baseline) into oracle/_build/liboracle.so, and
 # the host runner of the reference's own GPU kernels (oracle/ref/ref_gpu.cpp,
 # test and measurement infrastructure) into oracle/_build/libref_gpu.so.
 set -e

@@ -1,8 +1,8 @@
 """ctypes wrapper of the CPU oracle (oracle/oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline / reference legs as the checker. It never backs the
-product path.
+bench.py's CPU-baseline / reference legs, to check the GPU solver against.
+It never backs the product path.
 """
 from __future__ import annotations
 

@@ -1,7 +1,7 @@
 // CPU ORACLE - test infrastructure only.
 //
 // A plain recursive restatement of the reference's DCFR solve for one
-// postflop spot. It is the checker for the GPU solver (tests/), the
+// postflop spot. The GPU solver is tested against it (tests/), and it backs the
 // smoke check (__graft_entry__.smoke) and the CPU baseline leg of
 // bench.py; no product code links or calls it.
 //
