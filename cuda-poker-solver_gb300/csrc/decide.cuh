@@ -150,7 +150,8 @@ __device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<
 // instead of three dependent ones, and the data in flight holds no
 // registers. Each thread reads back only what it copied (cp.async.wait_group
 // waits for the thread's own copies: nothing to spin on). Records with more
-// than kAsyncNa actions (8% of C3's row bytes) use the streaming form.
+// than kAsyncNa actions (8% of the row bytes of the 48,255-node turn spot)
+// use the streaming form.
 // Layout: [row kind][action][thread] float4, conflict-free.
 // ---------------------------------------------------------------------------
 constexpr int kAsyncNa = 4;

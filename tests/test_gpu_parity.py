@@ -140,7 +140,7 @@ def test_terminal_groups_match_per_node_kernels(name):
 
 
 def test_full_size_turn_c3_properties():
-    """The 48,255-node C3 tree: FP64 EVs sum to the pot, exploitability
+    """The 48,255-node turn tree (turn_c3): FP64 EVs sum to the pot, exploitability
     falls with iterations, rows stay finite and the strategy normalizes."""
     spot = wl.turn_c3()
     s = solver(spot)

@@ -101,7 +101,7 @@ def test_bad_inputs_rejected_on_host():
 
 def test_batch_footprint_host_only():
     """pps_gb_batch_footprint compiles on the host: footprints grow with
-    the tree and the 48,255-node C3 spot needs ~1.7 GB (f32 rows, FP64 walk
+    the tree and the 48,255-node turn spot (turn_c3) needs ~1.7 GB (f32 rows, FP64 walk
     rows, tables, groups, records)."""
     from pps import batch as pb
     from pps import workloads as wl
