@@ -213,14 +213,16 @@ class SolverService:
             e.job["running"] = False
 
     def _start_job(self, sid: str, e: _Entry, kind: str, p: Dict[str, Any]) -> Dict[str, Any]:
-        if e.job and e.job["running"]:
-            raise ServiceError(409, "a solve job is already running on this solver "
-                                    "(POST /solvers/{id}/cancel first)")
-        e.job = {"running": True, "status": "running", "kind": kind, "done": 0, "start": 0,
-                 "total": p["max_iters"], "target": p.get("target"), "error": None,
-                 "cancel": False}
+        with self._mu:  # check and claim at once: two requests cannot both start a job
+            if e.job and e.job["running"]:
+                raise ServiceError(409, "a solve job is already running on this solver "
+                                        "(POST /solvers/{id}/cancel first)")
+            e.job = {"running": True, "status": "running", "kind": kind, "done": 0,
+                     "start": 0, "total": p["max_iters"], "target": p.get("target"),
+                     "error": None, "cancel": False}
+            job = dict(e.job)
         threading.Thread(target=self._job_worker, args=(e, kind, p), daemon=True).start()
-        return {"id": sid, "job": dict(e.job)}
+        return {"id": sid, "job": job}
 
     def _busy(self, e: _Entry) -> None:
         if e.job and e.job["running"]:
