@@ -2,9 +2,13 @@
 #include "layout.h"
 
 #include <algorithm>
+#include <atomic>
+#include <exception>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <stdexcept>
+#include <thread>
 
 #include "pps_gb.h"
 
@@ -37,6 +41,153 @@ int slotOf(const std::vector<uint16_t>& list, int base) {
   return it != list.end() && *it == base ? (int)(it - list.begin()) : -1;
 }
 
+// One board state's tables (see StateDev), before they go into the pools.
+struct StateParts {
+  std::vector<uint8_t> cards[2];
+  std::vector<int> starts[2], entries[2], same[2], up[2], down[2];
+  int maxCardSeg = 0;
+  std::vector<int> ord[2], segStart[2], segSlot[2];  // river states
+  std::vector<ShowdownInfo> info[2];
+};
+
+void buildStateParts(const Tree& t, int s, StateParts& P) {
+  const BoardState& st = t.states[s];
+  for (int p = 0; p < 2; ++p) {
+    const Side& side = t.side[p];
+    const auto& list = st.list[p];
+    const int n = (int)list.size();
+    P.cards[p].reserve(2 * (size_t)n);
+    for (uint16_t b : list) {
+      P.cards[p].push_back(side.cards[2 * b]);
+      P.cards[p].push_back(side.cards[2 * b + 1]);
+    }
+    // Card segments: per card, the slots holding it in ascending order
+    // (one counting pass, one filling pass).
+    std::vector<int> count(52, 0);
+    for (int j = 0; j < n; ++j) {
+      ++count[side.cards[2 * list[j]]];
+      ++count[side.cards[2 * list[j] + 1]];
+    }
+    std::vector<int>& starts = P.starts[p];
+    starts.assign(53, 0);
+    for (int c = 0; c < 52; ++c) {
+      starts[c + 1] = starts[c] + count[c];
+      P.maxCardSeg = std::max(P.maxCardSeg, count[c]);
+    }
+    P.entries[p].assign(starts[52], 0);
+    std::vector<int> fill(starts.begin(), starts.begin() + 52);
+    for (int j = 0; j < n; ++j) {
+      P.entries[p][fill[side.cards[2 * list[j]]]++] = j;
+      P.entries[p][fill[side.cards[2 * list[j] + 1]]++] = j;
+    }
+    P.same[p].assign(n, -1);
+    for (int j = 0; j < n; ++j) {
+      const int so = side.sameOther[list[j]];
+      if (so >= 0) P.same[p][j] = slotOf(st.list[1 - p], so);
+    }
+    if (st.parent >= 0) {
+      const auto& plist = t.states[st.parent].list[p];
+      std::vector<int>& up = P.up[p];
+      std::vector<int>& down = P.down[p];
+      up.assign(n, 0);
+      down.assign(plist.size(), -1);
+      size_t i = 0;
+      for (int j = 0; j < n; ++j) {
+        while (plist[i] != list[j]) ++i;
+        up[j] = (int)i;
+        down[i] = j;
+      }
+    }
+  }
+  if (st.nBoard != 5) return;
+
+  // River strength tables over this state's own lists.
+  std::vector<uint64_t> keyBase[2] = {strengthKeys(t, 0, st.board),
+                                      strengthKeys(t, 1, st.board)};
+  for (int tr = 0; tr < 2; ++tr) {
+    const int opp = 1 - tr;
+    const auto& ol = st.list[opp];
+    const auto& tl = st.list[tr];
+    const int no = (int)ol.size();
+    std::vector<int>& ord = P.ord[tr];
+    ord.resize(no);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      return keyBase[opp][ol[a]] < keyBase[opp][ol[b]];
+    });
+    std::vector<uint64_t> sortedKey(no);
+    for (int k = 0; k < no; ++k) sortedKey[k] = keyBase[opp][ol[ord[k]]];
+    std::vector<int>& segStart = P.segStart[tr];
+    std::vector<int>& segSlot = P.segSlot[tr];
+    segStart.assign(53, 0);
+    std::vector<std::vector<int>> posOfCard(52);
+    for (int k = 0; k < no; ++k) {
+      const int b = ol[ord[k]];
+      posOfCard[t.side[opp].cards[2 * b]].push_back(k);
+      posOfCard[t.side[opp].cards[2 * b + 1]].push_back(k);
+    }
+    for (int c = 0; c < 52; ++c) {
+      segStart[c] = (int)segSlot.size();
+      for (int k : posOfCard[c]) segSlot.push_back(ord[k]);
+    }
+    segStart[52] = (int)segSlot.size();
+    P.info[tr].reserve(tl.size());
+    for (int i = 0; i < (int)tl.size(); ++i) {
+      const int b = tl[i];
+      const uint64_t key = keyBase[tr][b];
+      const int le = (int)(std::lower_bound(sortedKey.begin(), sortedKey.end(), key) -
+                           sortedKey.begin());
+      const int te = (int)(std::upper_bound(sortedKey.begin(), sortedKey.end(), key) -
+                           sortedKey.begin());
+      const int c1 = t.side[tr].cards[2 * b], c2 = t.side[tr].cards[2 * b + 1];
+      auto below = [&](int c, int pos) {
+        const auto& v = posOfCard[c];
+        return (int)(std::lower_bound(v.begin(), v.end(), pos) - v.begin());
+      };
+      const int so = t.side[tr].sameOther[b];
+      const int same = so >= 0 ? slotOf(ol, so) : -1;
+      const int len1 = (int)posOfCard[c1].size(), len2 = (int)posOfCard[c2].size();
+      ShowdownInfo info;
+      info.x = (uint32_t)le | ((uint32_t)te << 16);
+      info.y = (uint32_t)len1 | ((uint32_t)len2 << 8) | ((uint32_t)below(c1, le) << 16) |
+               ((uint32_t)below(c1, te) << 24);
+      info.z = (uint32_t)below(c2, le) | ((uint32_t)below(c2, te) << 8) |
+               ((uint32_t)(same + 1) << 16);
+      info.w = (uint32_t)(segStart[c1] + c1) | ((uint32_t)(segStart[c2] + c2) << 16);
+      P.info[tr].push_back(info);
+    }
+  }
+}
+
+// Runs f(0 .. n-1) on up to 16 host threads; the first exception is
+// rethrown after every thread has finished.
+template <typename F>
+void parallelFor(int n, F&& f) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int nt = std::min(n, (int)std::min(hw ? hw : 1u, 16u));
+  if (nt <= 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::exception_ptr err;
+  std::mutex m;
+  auto work = [&] {
+    try {
+      for (int i = next++; i < n; i = next++) f(i);
+    } catch (...) {
+      std::lock_guard<std::mutex> lock(m);
+      if (!err) err = std::current_exception();
+      next = n;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int k = 1; k < nt; ++k) pool.emplace_back(work);
+  work();
+  for (std::thread& th : pool) th.join();
+  if (err) std::rethrow_exception(err);
+}
+
 }  // namespace
 
 HostLayout buildLayout(const Tree& t) {
@@ -45,112 +196,54 @@ HostLayout buildLayout(const Tree& t) {
   const int S = (int)t.states.size();
 
   // ---- board-state tables ----
+  // States are independent: their tables are built in parallel, then
+  // appended to the pools in state order (the same bytes as a serial build).
+  std::vector<StateParts> parts(S);
+  parallelFor(S, [&](int s) { buildStateParts(t, s, parts[s]); });
+  size_t nU8 = 0, nU16 = 0, nI16 = 0, nSd = 0;
+  for (const StateParts& P : parts)
+    for (int p = 0; p < 2; ++p) {
+      nU8 += P.cards[p].size();
+      nU16 += P.starts[p].size() + P.entries[p].size() + P.up[p].size() + P.ord[p].size() +
+              P.segStart[p].size() + P.segSlot[p].size() + 16;  // + alignment
+      nI16 += P.same[p].size() + P.down[p].size();
+      nSd += P.info[p].size();
+    }
+  L.poolU8.reserve(L.poolU8.size() + nU8);
+  L.poolU16.reserve(L.poolU16.size() + nU16);
+  L.poolI16.reserve(L.poolI16.size() + nI16);
+  L.poolSd.reserve(L.poolSd.size() + nSd);
   L.states.resize(S);
   for (int s = 0; s < S; ++s) {
     const BoardState& st = t.states[s];
+    const StateParts& P = parts[s];
     StateDev& sd = L.states[s];
     for (int p = 0; p < 2; ++p) {
-      const Side& side = t.side[p];
-      const auto& list = st.list[p];
-      const int n = (int)list.size();
+      const int n = (int)st.list[p].size();
       sd.n[p] = n;
       L.maxN = std::max(L.maxN, n);
       sd.cardsOff[p] = (int)L.poolU8.size();
-      for (uint16_t b : list) {
-        L.poolU8.push_back(side.cards[2 * b]);
-        L.poolU8.push_back(side.cards[2 * b + 1]);
-      }
-      std::vector<int> starts(53, 0), entries;
-      for (int c = 0; c < 52; ++c) {
-        starts[c] = (int)entries.size();
-        for (int j = 0; j < n; ++j)
-          if (side.cards[2 * list[j]] == c || side.cards[2 * list[j] + 1] == c)
-            entries.push_back(j);
-        L.maxCardSeg = std::max(L.maxCardSeg, (int)entries.size() - starts[c]);
-      }
-      starts[52] = (int)entries.size();
+      L.poolU8.insert(L.poolU8.end(), P.cards[p].begin(), P.cards[p].end());
       alignU16(L.poolU16);
-      sd.csrOff[p] = appendU16(L.poolU16, starts);
-      appendU16(L.poolU16, entries);
-      std::vector<int> same(n, -1);
-      for (int j = 0; j < n; ++j) {
-        const int so = side.sameOther[list[j]];
-        if (so >= 0) same[j] = slotOf(st.list[1 - p], so);
-      }
-      sd.sameOff[p] = appendI16(L.poolI16, same);
+      sd.csrOff[p] = appendU16(L.poolU16, P.starts[p]);
+      appendU16(L.poolU16, P.entries[p]);
+      sd.sameOff[p] = appendI16(L.poolI16, P.same[p]);
       sd.upOff[p] = sd.downOff[p] = -1;
       if (st.parent >= 0) {
-        const auto& plist = t.states[st.parent].list[p];
-        std::vector<int> up(n), down(plist.size(), -1);
-        size_t i = 0;
-        for (int j = 0; j < n; ++j) {
-          while (plist[i] != list[j]) ++i;
-          up[j] = (int)i;
-          down[i] = j;
-        }
-        sd.upOff[p] = appendU16(L.poolU16, up);
-        sd.downOff[p] = appendI16(L.poolI16, down);
+        sd.upOff[p] = appendU16(L.poolU16, P.up[p]);
+        sd.downOff[p] = appendI16(L.poolI16, P.down[p]);
       }
       sd.sdOff[p] = sd.sdInfoOff[p] = -1;
     }
+    L.maxCardSeg = std::max(L.maxCardSeg, P.maxCardSeg);
     if (st.nBoard != 5) continue;
-
-    // River strength tables over this state's own lists.
-    std::vector<uint64_t> keyBase[2] = {strengthKeys(t, 0, st.board),
-                                        strengthKeys(t, 1, st.board)};
     for (int tr = 0; tr < 2; ++tr) {
-      const int opp = 1 - tr;
-      const auto& ol = st.list[opp];
-      const auto& tl = st.list[tr];
-      const int no = (int)ol.size();
-      std::vector<int> ord(no);
-      std::iota(ord.begin(), ord.end(), 0);
-      std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
-        return keyBase[opp][ol[a]] < keyBase[opp][ol[b]];
-      });
-      std::vector<uint64_t> sortedKey(no);
-      for (int k = 0; k < no; ++k) sortedKey[k] = keyBase[opp][ol[ord[k]]];
-      std::vector<int> segStart(53, 0), segSlot;
-      std::vector<std::vector<int>> posOfCard(52);
-      for (int k = 0; k < no; ++k) {
-        const int b = ol[ord[k]];
-        posOfCard[t.side[opp].cards[2 * b]].push_back(k);
-        posOfCard[t.side[opp].cards[2 * b + 1]].push_back(k);
-      }
-      for (int c = 0; c < 52; ++c) {
-        segStart[c] = (int)segSlot.size();
-        for (int k : posOfCard[c]) segSlot.push_back(ord[k]);
-      }
-      segStart[52] = (int)segSlot.size();
       alignU16(L.poolU16);
-      sd.sdOff[tr] = appendU16(L.poolU16, ord);
-      appendU16(L.poolU16, segStart);
-      appendU16(L.poolU16, segSlot);
+      sd.sdOff[tr] = appendU16(L.poolU16, P.ord[tr]);
+      appendU16(L.poolU16, P.segStart[tr]);
+      appendU16(L.poolU16, P.segSlot[tr]);
       sd.sdInfoOff[tr] = (int)L.poolSd.size();
-      for (int i = 0; i < (int)tl.size(); ++i) {
-        const int b = tl[i];
-        const uint64_t key = keyBase[tr][b];
-        const int le = (int)(std::lower_bound(sortedKey.begin(), sortedKey.end(), key) -
-                             sortedKey.begin());
-        const int te = (int)(std::upper_bound(sortedKey.begin(), sortedKey.end(), key) -
-                             sortedKey.begin());
-        const int c1 = t.side[tr].cards[2 * b], c2 = t.side[tr].cards[2 * b + 1];
-        auto below = [&](int c, int pos) {
-          const auto& v = posOfCard[c];
-          return (int)(std::lower_bound(v.begin(), v.end(), pos) - v.begin());
-        };
-        const int so = t.side[tr].sameOther[b];
-        const int same = so >= 0 ? slotOf(ol, so) : -1;
-        const int len1 = (int)posOfCard[c1].size(), len2 = (int)posOfCard[c2].size();
-        ShowdownInfo info;
-        info.x = (uint32_t)le | ((uint32_t)te << 16);
-        info.y = (uint32_t)len1 | ((uint32_t)len2 << 8) | ((uint32_t)below(c1, le) << 16) |
-                 ((uint32_t)below(c1, te) << 24);
-        info.z = (uint32_t)below(c2, le) | ((uint32_t)below(c2, te) << 8) |
-                 ((uint32_t)(same + 1) << 16);
-        info.w = (uint32_t)(segStart[c1] + c1) | ((uint32_t)(segStart[c2] + c2) << 16);
-        L.poolSd.push_back(info);
-      }
+      L.poolSd.insert(L.poolSd.end(), P.info[tr].begin(), P.info[tr].end());
     }
   }
   // The showdown kernel scans one card segment per warp, two entries per
@@ -291,36 +384,63 @@ HostLayout buildLayout(const Tree& t) {
         if ((w & 3) == kTaskChance) L.fwdChance[tr][d].push_back(w);
     }
   }
-  auto addRecord = [&](uint32_t regQ, uint32_t rowQ, int n, int na, int own, int chunk,
-                       const std::vector<uint32_t>& kids) {
-    const uint32_t off = (uint32_t)(L.recPool.size() / 4);
-    L.recPool.push_back(regQ);
-    L.recPool.push_back(rowQ);
-    L.recPool.push_back((uint32_t)n | ((uint32_t)na << 16) | ((uint32_t)own << 24));
-    L.recPool.push_back((uint32_t)chunk);
-    L.recPool.insert(L.recPool.end(), kids.begin(), kids.end());
-    while (L.recPool.size() % 4) L.recPool.push_back(0);
+  // Decide records: [own regret row, value or reach row, n | na << 16 |
+  // own << 24, chunk, child rows[na]], padded to 16 bytes. One pass counts
+  // them, one writes them into the pool sized once.
+  auto recWords = [](int na) { return (size_t)(4 + na + 3) / 4 * 4; };
+  auto chunksOf = [](int n) { return (int)((quads(n) + kRecQuads - 1) / kRecQuads); };
+  size_t words = L.recPool.size();
+  std::vector<size_t> nBwd[2] = {std::vector<size_t>(D, 0), std::vector<size_t>(D, 0)};
+  std::vector<size_t> nFwd[2] = {std::vector<size_t>(D, 0), std::vector<size_t>(D, 0)};
+  for (int u = 0; u < N; ++u) {
+    const Node& nd = t.nodes[u];
+    if (nd.kind != kDecide) continue;
+    for (int tr = 0; tr < 2; ++tr) {
+      const int cb = chunksOf(t.n(u, tr));
+      nBwd[tr][nd.depth] += cb;
+      words += cb * recWords(nd.na);
+      if (nd.player == tr) continue;
+      const int cf = chunksOf(t.n(u, 1 - tr));
+      nFwd[tr][nd.depth] += cf;
+      words += cf * recWords(nd.na);
+    }
+  }
+  for (int tr = 0; tr < 2; ++tr)
+    for (int d = 0; d < D; ++d) {
+      L.bwdRecs[tr][d].reserve(nBwd[tr][d]);
+      L.fwdRecs[tr][d].reserve(nFwd[tr][d]);
+    }
+  size_t w = L.recPool.size();
+  L.recPool.resize(words, 0u);
+  std::vector<uint32_t> kids;
+  auto addRecord = [&](uint32_t regQ, uint32_t rowQ, int n, int na, int own, int chunk) {
+    const uint32_t off = (uint32_t)(w / 4);
+    uint32_t* r = L.recPool.data() + w;
+    r[0] = regQ;
+    r[1] = rowQ;
+    r[2] = (uint32_t)n | ((uint32_t)na << 16) | ((uint32_t)own << 24);
+    r[3] = (uint32_t)chunk;
+    for (int a = 0; a < na; ++a) r[4 + a] = kids[a];
+    w += recWords(na);
     return off;
   };
   for (int u = 0; u < N; ++u) {
     const Node& nd = t.nodes[u];
     if (nd.kind != kDecide) continue;
+    kids.resize(nd.na);
     for (int tr = 0; tr < 2; ++tr) {
-      std::vector<uint32_t> kids(nd.na);
       for (int a = 0; a < nd.na; ++a) kids[a] = L.rows[t.children[nd.childBase + a]].cfvQ;
       const int nTr = t.n(u, tr);
-      const int chunksTr = (int)((quads(nTr) + kRecQuads - 1) / kRecQuads);
-      for (int c = 0; c < chunksTr; ++c)
+      for (int c = 0, cb = chunksOf(nTr); c < cb; ++c)
         L.bwdRecs[tr][nd.depth].push_back(
-            addRecord(L.nodes[u].regQ, L.rows[u].cfvQ, nTr, nd.na, nd.player == tr, c, kids));
+            addRecord(L.nodes[u].regQ, L.rows[u].cfvQ, nTr, nd.na, nd.player == tr, c));
       if (nd.player == tr) continue;
       for (int a = 0; a < nd.na; ++a)
         kids[a] = L.rows[t.children[nd.childBase + a]].reachQ[tr];
       const int nOpp = t.n(u, 1 - tr);
-      const int chunksOpp = (int)((quads(nOpp) + kRecQuads - 1) / kRecQuads);
-      for (int c = 0; c < chunksOpp; ++c)
+      for (int c = 0, cf = chunksOf(nOpp); c < cf; ++c)
         L.fwdRecs[tr][nd.depth].push_back(
-            addRecord(L.nodes[u].regQ, L.rows[u].reachQ[tr], nOpp, nd.na, 0, c, kids));
+            addRecord(L.nodes[u].regQ, L.rows[u].reachQ[tr], nOpp, nd.na, 0, c));
     }
   }
   // Chance records: every row and table address a chance task needs, so a
