@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <utility>
 
 #include "pps_gb.h"
@@ -37,24 +38,20 @@ class Builder {
       t_.nodes[idx].kind = kChance;
       uint64_t onBoard = 0;
       for (int i = 0; i < nBoard; ++i) onBoard |= 1ull << t_.states[state].board[i];
+      int kids[52];
+      int nk = 0;
       for (int c = 0; c < 52; ++c) {
         if ((onBoard >> c) & 1ull) continue;
         const int cs = childState(state, c);
-        const int child = build(cs, potBase + sc0 + sc1, 0, 0, 0, false,
-                                false, depth + 1, pc0 + sc0, pc1 + sc1, 0, idx);
-        kids_[idx].push_back(child);
+        kids[nk++] = build(cs, potBase + sc0 + sc1, 0, 0, 0, false, false, depth + 1,
+                           pc0 + sc0, pc1 + sc1, 0, idx);
       }
+      setKids(idx, kids, nk);
       return idx;
     }
 
-    const auto acts = pf::betActions(potBase, stack - pc0, t_.cfgFor(nBoard),
-                                     sc0, sc1, actor, afterAllin, numBets,
-                                     6 - nBoard);
-    if ((int)acts.size() > kMaxActions)
-      throw Error{PPS_GB_E_TOO_WIDE,
-                  "bet config too wide (max actions " +
-                      std::to_string(acts.size()) + " > " +
-                      std::to_string(kMaxActions) + ")"};
+    const std::vector<pf::TreeAction>& acts =
+        actionsFor(potBase, stack - pc0, nBoard, sc0, sc1, actor, afterAllin, numBets);
     {
       Node& nd = t_.nodes[idx];
       nd.kind = kDecide;
@@ -65,6 +62,8 @@ class Builder {
     t_.maxNa = std::max<int>(t_.maxNa, (int)acts.size());
     t_.actions.insert(t_.actions.end(), acts.begin(), acts.end());
 
+    int kids[kMaxActions];
+    int nk = 0;
     for (const pf::TreeAction& act : acts) {
       int64_t nsc0 = sc0, nsc1 = sc1;
       bool nAfterAllin = afterAllin;
@@ -101,24 +100,66 @@ class Builder {
                       false, depth + 1, pc0, pc1,
                       act.kind == pf::ActionKind::Check ? numBets : numBets + 1,
                       idx);
-      kids_[idx].push_back(child);
+      kids[nk++] = child;
     }
+    setKids(idx, kids, nk);
     return idx;
   }
 
   void flattenChildren() {
     t_.children.clear();
+    t_.children.reserve(kidFlat_.size());
     for (size_t u = 0; u < t_.nodes.size(); ++u) {
       t_.nodes[u].childBase = (int)t_.children.size();
-      t_.nodes[u].nChildren = (int)kids_[u].size();
-      t_.children.insert(t_.children.end(), kids_[u].begin(), kids_[u].end());
+      t_.nodes[u].nChildren = kidCnt_[u];
+      t_.children.insert(t_.children.end(), kidFlat_.begin() + kidOff_[u],
+                         kidFlat_.begin() + kidOff_[u] + kidCnt_[u]);
     }
   }
 
  private:
+  // The action list of a betting state. The same states recur under every
+  // runout, so each distinct argument tuple is computed once.
+  struct ActKey {
+    int64_t potBase, stack, sc0, sc1;
+    int nBoard, actor, numBets;
+    bool afterAllin;
+    bool operator<(const ActKey& o) const {
+      return std::tie(potBase, stack, sc0, sc1, nBoard, actor, numBets, afterAllin) <
+             std::tie(o.potBase, o.stack, o.sc0, o.sc1, o.nBoard, o.actor, o.numBets,
+                      o.afterAllin);
+    }
+  };
+  const std::vector<pf::TreeAction>& actionsFor(int64_t potBase, int64_t stack, int nBoard,
+                                                int64_t sc0, int64_t sc1, int actor,
+                                                bool afterAllin, int numBets) {
+    const ActKey key{potBase, stack, sc0, sc1, nBoard, actor, numBets, afterAllin};
+    auto it = acts_.find(key);
+    if (it != acts_.end()) return it->second;
+    std::vector<pf::TreeAction> acts = pf::betActions(
+        potBase, stack, t_.cfgFor(nBoard), sc0, sc1, actor, afterAllin, numBets, 6 - nBoard);
+    if ((int)acts.size() > kMaxActions)
+      throw Error{PPS_GB_E_TOO_WIDE,
+                  "bet config too wide (max actions " +
+                      std::to_string(acts.size()) + " > " +
+                      std::to_string(kMaxActions) + ")"};
+    return acts_.emplace(key, std::move(acts)).first->second;
+  }
+
+  // Children are recorded when a node's subtree is complete (post-order)
+  // and put back in node order by flattenChildren.
+  void setKids(int idx, const int* kids, int nk) {
+    kidOff_[idx] = (int64_t)kidFlat_.size();
+    kidCnt_[idx] = nk;
+    kidFlat_.insert(kidFlat_.end(), kids, kids + nk);
+  }
+
   Tree& t_;
-  std::vector<std::vector<int>> kids_;
-  std::map<std::pair<int, int>, int> dealt_;
+  std::vector<int> kidFlat_, kidCnt_;
+  std::vector<int64_t> kidOff_;
+  std::map<ActKey, std::vector<pf::TreeAction>> acts_;
+  std::vector<int> dealt_;  // [state * 52 + card] -> dealt state, or -1
+  int rivers_ = -1;         // river states so far (counted on first use)
 
   int newNode(int state, int64_t potBase, int64_t sc0, int64_t sc1,
               int64_t pc0, int64_t pc1, int depth, int parent) {
@@ -132,16 +173,17 @@ class Builder {
     nd.depth = depth;
     nd.parent = parent;
     t_.nodes.push_back(nd);
-    kids_.emplace_back();
+    kidOff_.push_back(0);
+    kidCnt_.push_back(0);
     return (int)t_.nodes.size() - 1;
   }
 
   // The state reached by dealing `card` from state `ps` (interned): its
   // lists are the parent's minus every combo holding the card.
   int childState(int ps, int card) {
-    const auto key = std::make_pair(ps, card);
-    auto it = dealt_.find(key);
-    if (it != dealt_.end()) return it->second;
+    const size_t key = (size_t)ps * 52 + (size_t)card;
+    if (dealt_.size() < t_.states.size() * 52) dealt_.resize(t_.states.size() * 52, -1);
+    if (dealt_[key] >= 0) return dealt_[key];
     BoardState s;
     s.parent = ps;
     s.dealt = card;
@@ -155,9 +197,11 @@ class Builder {
           s.list[p].push_back(slot);
     }
     if (s.nBoard == 5) {
-      int rivers = 0;
-      for (const BoardState& o : t_.states) rivers += o.nBoard == 5;
-      s.riverIndex = rivers;
+      if (rivers_ < 0) {
+        rivers_ = 0;
+        for (const BoardState& o : t_.states) rivers_ += o.nBoard == 5;
+      }
+      s.riverIndex = rivers_++;
     }
     t_.states.push_back(std::move(s));
     const int id = (int)t_.states.size() - 1;
