@@ -106,6 +106,62 @@ class Builder {
     return idx;
   }
 
+  // The number of nodes build() creates from the same arguments, so the
+  // node arrays are sized once (a runout's subtree depends only on the
+  // betting state, so equal states are counted once). Any mismatch would
+  // only cost growth; the tree itself comes from build().
+  int64_t count(int nBoard, int64_t potBase, int64_t sc0, int64_t sc1, int actor,
+                bool afterAllin, bool closed, int64_t pc0, int64_t pc1, int numBets) {
+    const int64_t stack = t_.spot.stack;
+    if (!closed && stack - pc0 <= 0) closed = true;
+    const auto key = std::make_tuple(nBoard, potBase, sc0, sc1, actor, afterAllin, closed, pc0,
+                                     pc1, numBets);
+    auto it = counts_.find(key);
+    if (it != counts_.end()) return it->second;
+    int64_t n = 1;
+    if (closed) {
+      if (nBoard < 5)
+        n += (int64_t)(52 - nBoard) * count(nBoard + 1, potBase + sc0 + sc1, 0, 0, 0, false,
+                                            false, pc0 + sc0, pc1 + sc1, 0);
+    } else {
+      const std::vector<pf::TreeAction>& acts =
+          actionsFor(potBase, stack - pc0, nBoard, sc0, sc1, actor, afterAllin, numBets);
+      for (const pf::TreeAction& act : acts) {
+        int64_t nsc0 = sc0, nsc1 = sc1;
+        switch (act.kind) {
+          case pf::ActionKind::Check:
+            n += actor == 0 ? count(nBoard, potBase, sc0, sc1, 1, afterAllin, false, pc0, pc1,
+                                    numBets)
+                            : count(nBoard, potBase, sc0, sc1, 0, false, true, pc0, pc1, 0);
+            break;
+          case pf::ActionKind::Fold:
+            n += 1;
+            break;
+          case pf::ActionKind::Call:
+            (actor == 0 ? nsc0 : nsc1) = std::max(sc0, sc1);
+            n += count(nBoard, potBase, nsc0, nsc1, 0, false, true, pc0, pc1, 0);
+            break;
+          default:
+            (actor == 0 ? nsc0 : nsc1) = act.amount;
+            n += count(nBoard, potBase, nsc0, nsc1, actor ^ 1,
+                       afterAllin || act.kind == pf::ActionKind::AllIn, false, pc0, pc1,
+                       numBets + 1);
+            break;
+        }
+      }
+    }
+    counts_.emplace(key, n);
+    return n;
+  }
+
+  void reserve(int64_t nodes) {
+    if (nodes <= 0 || nodes > (int64_t)1 << 31) return;
+    t_.nodes.reserve((size_t)nodes);
+    kidOff_.reserve((size_t)nodes);
+    kidCnt_.reserve((size_t)nodes);
+    kidFlat_.reserve((size_t)nodes);
+  }
+
   void flattenChildren() {
     t_.children.clear();
     t_.children.reserve(kidFlat_.size());
@@ -158,6 +214,9 @@ class Builder {
   std::vector<int> kidFlat_, kidCnt_;
   std::vector<int64_t> kidOff_;
   std::map<ActKey, std::vector<pf::TreeAction>> acts_;
+  std::map<std::tuple<int, int64_t, int64_t, int64_t, int, bool, bool, int64_t, int64_t, int>,
+           int64_t>
+      counts_;
   std::vector<int> dealt_;  // [state * 52 + card] -> dealt state, or -1
   int rivers_ = -1;         // river states so far (counted on first use)
 
@@ -271,6 +330,7 @@ Tree compileTree(const gpu::PostflopSpot& spot,
   t.states.push_back(std::move(root));
 
   Builder b(t);
+  b.reserve(b.count(spot.nBoard, spot.pot, 0, 0, 0, false, false, 0, 0, 0));
   b.build(0, spot.pot, 0, 0, 0, false, false, 0, 0, 0, 0, -1);
   b.flattenChildren();
 
