@@ -627,6 +627,16 @@ int pps_gb_batch_footprint(const pps_gb_spot* spot, const pps_gb_bet_config* cfg
   });
 }
 
+int pps_gb_layout_digest(const pps_gb_spot* spot, const pps_gb_bet_config* cfgs, int n_cfgs,
+                         uint64_t* digest) {
+  return guarded([&] {
+    if (!spot || !digest) throw Error{PPS_GB_E_ARG, "null argument"};
+    const pps::gb::Tree t = pps::gb::compileTree(toSpot(*spot), toConfigs(cfgs, n_cfgs),
+                                                 n_cfgs == 3);
+    *digest = t.empty ? 0 : pps::gb::layoutDigest(pps::gb::buildLayout(t));
+  });
+}
+
 int pps_gb_compile_export(const pps_gb_spot* spot, const pps_gb_bet_config* cfgs, int n_cfgs,
                           pps_gb_array_cb cb, void* user) {
   return guarded([&] {

@@ -500,5 +500,72 @@ HostLayout buildLayout(const Tree& t) {
   return L;
 }
 
+namespace {
+
+struct Fnv {
+  uint64_t h = 1469598103934665603ull;
+  void bytes(const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) {
+      h ^= b[i];
+      h *= 1099511628211ull;
+    }
+  }
+  template <typename T>
+  void vec(const std::vector<T>& v) {
+    const uint64_t n = v.size();
+    bytes(&n, sizeof n);
+    if (n) bytes(v.data(), n * sizeof(T));
+  }
+  template <typename T>
+  void vecs(const std::vector<std::vector<T>>& v) {
+    const uint64_t n = v.size();
+    bytes(&n, sizeof n);
+    for (const auto& x : v) vec(x);
+  }
+};
+
+}  // namespace
+
+uint64_t layoutDigest(const HostLayout& L) {
+  Fnv f;
+  f.vec(L.nodes);
+  f.vec(L.rows);
+  f.vec(L.termVal);
+  f.vec(L.children);
+  f.vec(L.states);
+  f.vec(L.poolU8);
+  f.vec(L.poolU16);
+  f.vec(L.poolI16);
+  f.vec(L.poolSd);
+  f.bytes(&L.regQuads, sizeof L.regQuads);
+  f.bytes(&L.cfvQuads, sizeof L.cfvQuads);
+  f.bytes(L.reachQuads, sizeof L.reachQuads);
+  for (int tr = 0; tr < 2; ++tr) {
+    f.vecs(L.fwdTasks[tr]);
+    f.vecs(L.bwdTasks[tr]);
+    f.vecs(L.innerTasks[tr]);
+  }
+  f.vec(L.groups);
+  f.vecs(L.sdGroupTasks);
+  f.vecs(L.fdGroupTasks);
+  f.vec(L.recPool);
+  for (int tr = 0; tr < 2; ++tr) {
+    f.vecs(L.bwdRecs[tr]);
+    f.vecs(L.fwdRecs[tr]);
+    f.vecs(L.fwdChanceRecs[tr]);
+    f.vecs(L.bwdChanceRecs[tr]);
+    for (const auto& c : L.chanceTables[tr]) {
+      f.bytes(&c.first, sizeof c.first);
+      f.bytes(&c.second, sizeof c.second);
+    }
+    f.vecs(L.bwdChance[tr]);
+    f.vecs(L.fwdChance[tr]);
+  }
+  f.bytes(&L.maxN, sizeof L.maxN);
+  f.bytes(&L.maxCardSeg, sizeof L.maxCardSeg);
+  return f.h;
+}
+
 }  // namespace gb
 }  // namespace pps

@@ -133,6 +133,10 @@ struct HostLayout {
 
 HostLayout buildLayout(const Tree& t);
 
+// FNV-1a digest of every array and scalar of a layout, in a fixed order
+// (tests pin layouts with it: equal digests, byte-identical layouts).
+uint64_t layoutDigest(const HostLayout& L);
+
 inline uint32_t quads(int n) { return (uint32_t)((n + 3) / 4); }
 
 }  // namespace gb

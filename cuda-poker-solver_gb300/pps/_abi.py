@@ -149,6 +149,7 @@ _SIGS = {
                                          P(C.c_int64)]),
     "pps_gb_batch_get_info": (C.c_int, [H, P(BatchInfo)]),
     "pps_gb_batch_footprint": (C.c_int, [P(Spot), P(BetConfig), C.c_int, P(C.c_int64)]),
+    "pps_gb_layout_digest": (C.c_int, [P(Spot), P(BetConfig), C.c_int, P(C.c_uint64)]),
     "pps_gb_compile_export": (C.c_int, [P(Spot), P(BetConfig), C.c_int, ARRAY_CB, C.c_void_p]),
     "pps_gb_hand_keys": (C.c_int, [P(C.c_uint8), C.c_int, P(C.c_uint64)]),
     "pps_gb_bet_actions": (C.c_int, [C.c_int64, C.c_int64, P(BetConfig), C.c_int64, C.c_int64,

@@ -455,6 +455,16 @@ def compile_export(board: Sequence[int], oop: Any, ip: Any, pot: int, stack: int
     return out
 
 
+def layout_digest(board: Sequence[int], oop: Any, ip: Any, pot: int, stack: int,
+                  cfgs: Sequence[_abi.BetConfig]) -> int:
+    """Host-only: digest of the device layout built for the spot (tests)."""
+    spot = make_spot(board, _range_arg(oop), _range_arg(ip), pot, stack, filter_board=False)
+    arr = (_abi.BetConfig * len(cfgs))(*cfgs)
+    d = C.c_uint64()
+    check(lib.pps_gb_layout_digest(C.byref(spot), arr, len(cfgs), C.byref(d)))
+    return int(d.value)
+
+
 def bet_config(bets: Any, raises: Any, max_raises: int = 0) -> _abi.BetConfig:
     return _bet_config(bets, raises, max_raises)
 

@@ -374,6 +374,13 @@ int pps_gb_batch_footprint(const pps_gb_spot* spot,
                            const pps_gb_bet_config* cfgs, int n_cfgs,
                            int64_t* bytes);
 
+/* Host only (tests): a 64-bit FNV-1a digest of the device layout the
+ * library builds for a spot (every node, row, table, task list and record
+ * array), 0 for an empty spot. Equal digests mean byte-identical layouts. */
+int pps_gb_layout_digest(const pps_gb_spot* spot,
+                         const pps_gb_bet_config* cfgs, int n_cfgs,
+                         uint64_t* digest);
+
 /* Host-only compile (no device use): runs the tree compiler and reports
  * every artifact in the reference's own layout (cuda/gpu_cfr.cu:1331-1827)
  * through cb(user, name, dtype, data, count); dtype 'i' int32, 'q' int64,

@@ -142,3 +142,18 @@ def test_reference_kernel_argument_block(golden_dir):
     members, size = ref_gpu.args_layout()
     assert size == want["size"] == 448
     assert [list(m) for m in members] == want["members"]
+
+
+def test_layout_is_pinned_and_deterministic(golden_dir):
+    """The device layout (tables built on several host threads, then merged
+    in state order) is byte-identical run to run and equal to the committed
+    digests, which the serial builder produced."""
+    from pps import workloads as wl
+    from helpers import abi_cfgs
+    with open(os.path.join(golden_dir, "layout_digests.json")) as f:
+        want = json.load(f)["digests"]
+    for name, hexd in want.items():
+        sp = wl.NAMED[name]()
+        args = (sp.board, sp.oop, sp.ip, sp.pot, sp.stack, abi_cfgs(sp))
+        got = [pn.layout_digest(*args) for _ in range(2)]
+        assert got[0] == got[1] == int(hexd, 16), name
