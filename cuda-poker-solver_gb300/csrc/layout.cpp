@@ -159,16 +159,30 @@ void buildStateParts(const Tree& t, int s, StateParts& P) {
   }
 }
 
-// Runs f(0 .. n-1) on up to 16 host threads; the first exception is
-// rethrown after every thread has finished.
+// Helper threads running across all parallelFor calls of the process: a
+// call borrows only the cores that others leave, so that many concurrent
+// compiles (a batch's compile workers) do not oversubscribe the host.
+std::atomic<int> gHelpers{0};
+
+// Runs f(0 .. n-1) on the calling thread and up to 15 helpers; the first
+// exception is rethrown after every thread has finished.
 template <typename F>
 void parallelFor(int n, F&& f) {
-  const unsigned hw = std::thread::hardware_concurrency();
-  const int nt = std::min(n, (int)std::min(hw ? hw : 1u, 16u));
-  if (nt <= 1) {
+  const unsigned hwu = std::thread::hardware_concurrency();
+  const int hw = hwu ? (int)hwu : 1;
+  const int want = std::min(n, std::min(hw, 16)) - 1;
+  int got = 0;
+  if (want > 0) {
+    int cur = gHelpers.load();
+    do {
+      got = std::max(0, std::min(want, hw - 1 - cur));
+    } while (got > 0 && !gHelpers.compare_exchange_weak(cur, cur + got));
+  }
+  if (got == 0) {
     for (int i = 0; i < n; ++i) f(i);
     return;
   }
+  const int nt = got + 1;
   std::atomic<int> next{0};
   std::exception_ptr err;
   std::mutex m;
@@ -182,9 +196,13 @@ void parallelFor(int n, F&& f) {
     }
   };
   std::vector<std::thread> pool;
-  for (int k = 1; k < nt; ++k) pool.emplace_back(work);
+  try {
+    for (int k = 1; k < nt; ++k) pool.emplace_back(work);
+  } catch (...) {  // no thread could be started: the caller does the rest
+  }
   work();
   for (std::thread& th : pool) th.join();
+  gHelpers -= got;
   if (err) std::rethrow_exception(err);
 }
 
