@@ -24,11 +24,14 @@ using namespace pps;
 
 namespace {
 
+// Card id of a rank and suit character (either case), -1 for a bad rank,
+// -2 for a bad suit (the rank is checked first, as the reference does).
 int cardOf(char r, char s) {
   const int rank = rankFromChar((char)std::toupper((unsigned char)r));
+  if (rank < 0) return -1;
   const char* suits = "cdhs";
-  const char* sp = std::strchr(suits, std::tolower((unsigned char)s));
-  if (rank < 0 || !sp || !s) return -1;
+  const char* sp = s ? std::strchr(suits, std::tolower((unsigned char)s)) : nullptr;
+  if (!sp) return -2;
   return (int)(sp - suits) * 13 + rank;
 }
 
@@ -65,8 +68,9 @@ int main(int argc, char** argv) {
     spot.nBoard = (int)board.size() / 2;
     for (int i = 0; i < spot.nBoard; ++i) {
       const int c = cardOf(board[2 * i], board[2 * i + 1]);
-      if (c < 0) {
-        std::fprintf(stderr, "bad card '%s'\n", board.substr(2 * i, 2).c_str());
+      if (c < 0) {  // the reference's messages (tools/gpu_pfflop.cu:44, 52)
+        if (c == -1) std::fprintf(stderr, "bad card rank '%c'\n", board[2 * i]);
+        else std::fprintf(stderr, "bad card suit '%c'\n", board[2 * i + 1]);
         return 2;
       }
       spot.board[i] = (Card)c;
@@ -81,7 +85,14 @@ int main(int argc, char** argv) {
     for (const std::string& tok : split(argv[7])) {
       if (tok == "a" || tok == "A" || tok == "allin") cfg.betAllIn = true;
       else if (tok == "e" || tok == "E" || tok == "geo") cfg.betGeometric = true;
-      else cfg.betFracs.push_back(std::stod(tok));
+      else {
+        try {
+          cfg.betFracs.push_back(std::stod(tok));
+        } catch (const std::exception&) {  // the reference's message and status
+          std::fprintf(stderr, "bad bet sizes '%s' (use fractions and/or 'a')\n", argv[7]);
+          return 2;
+        }
+      }
     }
     for (const std::string& tok : split(argv[8])) cfg.raiseMults.push_back(std::stod(tok));
     int iters = std::stoi(argv[9]);

@@ -157,3 +157,21 @@ def test_layout_is_pinned_and_deterministic(golden_dir):
         args = (sp.board, sp.oop, sp.ip, sp.pot, sp.stack, abi_cfgs(sp))
         got = [pn.layout_digest(*args) for _ in range(2)]
         assert got[0] == got[1] == int(hexd, 16), name
+
+
+def test_cli_argument_errors():
+    """gpu_pfflop rejects bad arguments before any device use, with the
+    reference CLI's messages and exit status 2 (tools/gpu_pfflop.cu:44-52,
+    104-137)."""
+    import subprocess
+    exe = os.path.join(os.path.dirname(pn.__file__), "gpu_pfflop")
+    ok = ["TT+", "AA", "100", "100", "0.5", "2", "10"]
+    cases = [([], "usage: gpu_pfflop postflop"),
+             (["postflop", "Qs9h"] + ok, "board must be 3, 4 or 5 cards"),
+             (["postflop", "QsXh2d"] + ok, "bad card rank 'X'"),
+             (["postflop", "Qs9z2d"] + ok, "bad card suit 'z'"),
+             (["postflop", "Qs9h2d", "TT+", "AA", "100", "100", "0.5,zz", "2", "10"],
+              "bad bet sizes '0.5,zz' (use fractions and/or 'a')")]
+    for args, msg in cases:
+        r = subprocess.run([exe] + args, capture_output=True, text=True, timeout=60)
+        assert r.returncode == 2 and r.stdout == "" and r.stderr.startswith(msg), (args, r.stderr)
