@@ -97,6 +97,16 @@ def test_bad_inputs_rejected_on_host():
         pn.Solver(board="Qs9h2d7c", oop="TT+", ip="99+", pot=100, stack=100, bets="")
     with pytest.raises(RuntimeError):
         pn.Solver(board="QsQs2d7c", oop="TT+", ip="99+", pot=100, stack=100)
+    # the reference binding's messages (python/pps_native.cpp:66, 74, 104, 152)
+    for kw, msg in ((dict(board="QsXh2d"), "bad card rank 'X'"),
+                    (dict(board="Qs9z2d"), "bad card suit 'z'"),
+                    (dict(board="Qs9h"), 'board must be 3, 4 or 5 cards (e.g. "Qs9h2d")'),
+                    (dict(bets="0.5,zz"), "bad bet size token 'zz'")):
+        args = dict(board="Qs9h2d", oop="TT+", ip="99+", pot=100, stack=100)
+        args.update(kw)
+        with pytest.raises(RuntimeError) as e:
+            pn.Solver(**args)
+        assert str(e.value) == msg
 
 
 def test_batch_footprint_host_only():
