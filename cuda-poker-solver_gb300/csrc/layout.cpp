@@ -332,9 +332,10 @@ HostLayout buildLayout(const Tree& t) {
   L.reachQuads[0] = reachQ[0];
   L.reachQuads[1] = reachQ[1];
 
-  // ---- warp task lists ----
+  // ---- warp task lists (per traverser) and terminal groups ----
+  // Three independent jobs, each writing only its own lists.
   const int D = t.maxDepth + 1;
-  for (int tr = 0; tr < 2; ++tr) {
+  auto taskLists = [&](int tr) {
     L.fwdTasks[tr].assign(D, {});
     L.bwdTasks[tr].assign(D, {});
     std::vector<std::vector<int>> sd(D), fd(D), ch(D), dc(D);
@@ -367,28 +368,34 @@ HostLayout buildLayout(const Tree& t) {
       L.innerTasks[tr].push_back(ch[d]);
       L.innerTasks[tr].back().insert(L.innerTasks[tr].back().end(), dc[d].begin(), dc[d].end());
     }
-  }
+  };
   // Terminal groups: per depth, the showdown (then fold) nodes of one board
   // state in fours, in node order (the same groups serve both traversers).
-  L.sdGroupTasks.assign(D, {});
-  L.fdGroupTasks.assign(D, {});
-  for (int kind : {(int)kShowdown, (int)kFold}) {
-    std::vector<std::vector<std::vector<int>>> byState(D, std::vector<std::vector<int>>(S));
-    for (int u = 0; u < N; ++u)
-      if (t.nodes[u].kind == kind) byState[t.nodes[u].depth][t.nodes[u].state].push_back(u);
-    for (int d = 0; d < D; ++d)
-      for (int s = 0; s < S; ++s) {
-        const auto& v = byState[d][s];
-        for (size_t i = 0; i < v.size(); i += 4) {
-          TermGroup g{{-1, -1, -1, -1}};
-          for (size_t k = 0; k < 4 && i + k < v.size(); ++k) g.node[k] = v[i + k];
-          const int task = makeTask(kind == kShowdown ? kTaskShowdown : kTaskFold, 0,
-                                    (int)L.groups.size());
-          (kind == kShowdown ? L.sdGroupTasks : L.fdGroupTasks)[d].push_back(task);
-          L.groups.push_back(g);
+  auto termGroups = [&] {
+    L.sdGroupTasks.assign(D, {});
+    L.fdGroupTasks.assign(D, {});
+    for (int kind : {(int)kShowdown, (int)kFold}) {
+      std::vector<std::vector<std::vector<int>>> byState(D, std::vector<std::vector<int>>(S));
+      for (int u = 0; u < N; ++u)
+        if (t.nodes[u].kind == kind) byState[t.nodes[u].depth][t.nodes[u].state].push_back(u);
+      for (int d = 0; d < D; ++d)
+        for (int s = 0; s < S; ++s) {
+          const auto& v = byState[d][s];
+          for (size_t i = 0; i < v.size(); i += 4) {
+            TermGroup g{{-1, -1, -1, -1}};
+            for (size_t k = 0; k < 4 && i + k < v.size(); ++k) g.node[k] = v[i + k];
+            const int task = makeTask(kind == kShowdown ? kTaskShowdown : kTaskFold, 0,
+                                      (int)L.groups.size());
+            (kind == kShowdown ? L.sdGroupTasks : L.fdGroupTasks)[d].push_back(task);
+            L.groups.push_back(g);
+          }
         }
-      }
-  }
+    }
+  };
+  parallelFor(3, [&](int job) {
+    if (job < 2) taskLists(job);
+    else termGroups();
+  });
   // Decide records and chance word lists of the default iteration.
   for (int tr = 0; tr < 2; ++tr) {
     L.bwdRecs[tr].assign(D, {});
