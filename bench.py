@@ -149,6 +149,84 @@ def cpu_baseline(spot, seconds=12.0):
                       % n}
 
 
+def accuracy(threads=None):
+    """Each result's error against an FP64 run of the same iterations (the
+    CPU oracle in double precision, as the checker): the product's root EV
+    and exploitability (its FP64 walks) and root strategy (range-weighted
+    frequencies of the root actions) after the spot's iterations, and its
+    regret and strategy rows after one iteration (later rows are
+    ill-conditioned: where exact regrets are zero, f32 rounding picks the
+    strategy, so row errors of O(0.1) appear in any f32 arithmetic). Beside
+    each, the same errors of a plain f32 restatement of the reference's
+    arithmetic (the oracle in single precision). Sizes the oracle finishes
+    in seconds: the river spot at its full 1,000 iterations, the 6,333-node
+    per-street turn at 200 and the 48,255-node benchmark turn at 30."""
+    import numpy as np
+    import pps
+    from pps import workloads as wl
+    from oracle.cpu_oracle import oracle_for
+
+    def root_freqs(rows, na, w):
+        n = len(w)
+        r = np.asarray(rows[:na * n], dtype=np.float64).reshape(na, n)
+        tot = r.sum(axis=0)
+        sig = np.where(tot > 0, r / np.where(tot > 0, tot, 1), 1.0 / na)
+        return (sig * w[None, :]).sum(axis=1) / w.sum()
+
+    def normwise(a, b):
+        b = np.asarray(b, dtype=np.float64)
+        return float(np.max(np.abs(np.asarray(a, dtype=np.float64) - b))) / max(
+            float(np.max(np.abs(b))), 1e-30)
+
+    def make(spot):
+        streets = None
+        if spot.street_cfgs:
+            streets = [{"bets": c.bet_text(), "raises": c.raise_text() or [],
+                        "max_raises": c.max_raises} for c in spot.street_cfgs]
+        return pps.Solver(board=spot.board_text(), oop=spot.oop, ip=spot.ip, pot=spot.pot,
+                          stack=spot.stack, bets=spot.cfg.bet_text(),
+                          raises=spot.cfg.raise_text() or [], max_raises=spot.cfg.max_raises,
+                          streets=streets)
+
+    out = {"reference": "CPU oracle in FP64, same tree, schedule and iteration count",
+           "fields": "ev_err: |EV_oop - FP64| chips (FP64 walks); expl_ratio: exploitability / "
+                     "FP64's; strategy_linf: root frequencies; rows_1_iteration: max |row - "
+                     "FP64| / max |FP64| over regret and strategy rows after one iteration; "
+                     "f32_restatement: the same errors of a plain f32 restatement of the "
+                     "reference iteration"}
+    for name, iters in (("river_c1", 1000), ("turn_c2", 200), ("turn_c3", 30)):
+        spot = wl.NAMED[name]()
+        s = make(spot)
+        s.solve(1)
+        o64 = oracle_for(spot, threads, precision=64)
+        o32 = oracle_for(spot, threads, precision=32)
+        o64.iterate(1)
+        o32.iterate(1)
+        rows1 = [max(normwise(x.rows(k) if x is not s else s.read_rows(k), o64.rows(k))
+                     for k in (0, 1)) for x in (s, o32)]
+        s.solve(iters)
+        st = s.stats()
+        o64.iterate(iters - 1)
+        o32.iterate(iters - 1)
+        e64, e32 = o64.stats(spot.pot), o32.stats(spot.pot)
+        na = len(s.decide_nodes()[0]["actions"])
+        w0 = np.asarray(s.player_weights(0), dtype=np.float64)
+        f64 = root_freqs(o64.rows(1), na, w0)
+
+        def errs(ev, expl, freqs, r1):
+            return {"ev_err": abs(ev - e64["ev_oop"]),
+                    "expl_ratio": expl / max(e64["exploitability"], 1e-12),
+                    "strategy_linf": float(np.max(np.abs(np.asarray(freqs) - f64))),
+                    "rows_1_iteration": r1}
+        out[name] = {"iterations": iters, "nodes": s.num_nodes,
+                     "fp64_ev_oop": e64["ev_oop"], "fp64_exploitability": e64["exploitability"],
+                     "gpu": errs(st["ev_oop"], st["exploitability"], s.root_strategy(), rows1[0]),
+                     "f32_restatement": errs(e32["ev_oop"], e32["exploitability"],
+                                             root_freqs(o32.rows(1), na, w0), rows1[1])}
+        del s, o64, o32
+    return out
+
+
 def max_over_ranks(x, dist, device="cpu"):
     """The job's time is the slowest rank's (identity without a process
     group)."""
@@ -178,7 +256,7 @@ def batched_bench(spots, loop_sample, check_every=64):
     """Batched: every spot solved to 0.5%-pot exploitability in one batch
     (all submitted at once, host compile threads, one device forest), next
     to the plain loop (pps.Solver per spot, solve with the same target,
-    stats, destroy) timed on a bounded sample of the same spots."""
+    stats, destroy) over the same spots (all of them by default)."""
     import pps
     import numpy as np
     from pps import pps_native as pn
@@ -203,6 +281,13 @@ def batched_bench(spots, loop_sample, check_every=64):
     loop_s = time.perf_counter() - t1
     batched = len(spots) / el
     loop = len(loop_sample) / loop_s
+    rivers = lambda ss: sum(1 for sp in ss if len(sp.board) == 5)
+    same = len(loop_sample) == len(spots)
+    sample = ("the same %d spots (%d river, %d turn)" % (len(spots), rivers(spots),
+                                                         len(spots) - rivers(spots))
+              if same else "first %d of the %d spots (%d river, %d turn)"
+              % (len(loop_sample), len(spots), rivers(loop_sample),
+                 len(loop_sample) - rivers(loop_sample)))
     return {"spots": len(spots), "finished": ok, "seconds": el, "solves_per_s": batched,
             "converged": int(sum(r["converged"] for r in res)),
             "failed": int(sum(r["status"] != 0 for r in res)),
@@ -212,8 +297,8 @@ def batched_bench(spots, loop_sample, check_every=64):
                       "16-%d iterations" % check_every,
             "max_expl_frac_pot": float(max(r["exploitability"] / sp.pot
                                            for r, sp in zip(res, spots))),
-            "one_at_a_time": {"solves_per_s": loop, "sample": "first %d of the %d spots"
-                              % (len(loop_sample), len(spots)),
+            "mix": "%d river, %d turn" % (rivers(spots), len(spots) - rivers(spots)),
+            "one_at_a_time": {"solves_per_s": loop, "seconds": loop_s, "sample": sample,
                               "path": "pps.Solver + solve(target, checks every 128) + stats"},
             "speedup_vs_one_at_a_time": batched / loop,
             "device_bytes_peak": info["peak_used_bytes"],
@@ -246,10 +331,16 @@ def served_bench(spots, lam, count, seed=7):
     lat = np.array([r["latency_ms"] for r in done]) if done else np.array([float("nan")])
     first = min(r["submit_ms"] for r in done) if done else 0.0
     last = max(r["finish_ms"] for r in done) if done else 1.0
+    rate = len(done) / max((last - first) / 1000.0, 1e-9)
+    its = [r["iterations"] for r in done] or [0]
     return {"lambda_per_s": lam, "requests": count, "completed": len(done),
-            "solves_per_s": len(done) / max((last - first) / 1000.0, 1e-9),
+            "solves_per_s": rate,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "peak_active": info["peak_active"], "offered_seconds": float(arrivals[-1])}
+            "peak_active": info["peak_active"], "offered_seconds": float(arrivals[-1]),
+            "iterations_mean": float(np.mean(its)),
+            "converged": int(sum(r["converged"] for r in done)),
+            "device_bytes_peak": info["peak_used_bytes"],
+            "saturated": bool(rate < 0.9 * lam)}
 
 
 def reference_kernels(steps, warmup):
@@ -339,10 +430,13 @@ def main():
                     help="iterations of the end-to-end solve (the workload's 1000)")
     ap.add_argument("--batch-spots", type=int, default=256,
                     help="spots of the batched solve (0 skips batched and served)")
-    ap.add_argument("--loop-sample", type=int, default=64,
-                    help="spots of the one-at-a-time loop the batched solve is set against")
-    ap.add_argument("--served-requests", type=int, default=400,
+    ap.add_argument("--loop-sample", type=int, default=0,
+                    help="spots of the one-at-a-time loop the batched solve is set against "
+                         "(0: the same spots as the batch)")
+    ap.add_argument("--served-requests", type=int, default=100,
                     help="requests per arrival rate of the served run (0 skips it)")
+    ap.add_argument("--served-rates", default="50,200,800",
+                    help="Poisson arrival rates (requests/s) of the served run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -423,7 +517,8 @@ def main():
         mine = shard(spots, rank, world)
         if dist:
             dist.barrier()
-        batched = batched_bench(mine, mine[:max(1, min(args.loop_sample, len(mine)))])
+        loop = mine if args.loop_sample <= 0 else mine[:max(1, min(args.loop_sample, len(mine)))]
+        batched = batched_bench(mine, loop)
         if dist:
             slowest = max_over_ranks(batched["seconds"], dist, "cuda")
             batched.update({"spots": len(spots), "ranks": world, "seconds": slowest,
@@ -471,16 +566,18 @@ def main():
         del sf
     if batched is not None:
         line["batched"] = batched
-        if world == 1 and args.served_requests > 0:
-            stream = wl.batched(1024, seed=505)
-            line["served"] = {"distribution": "batched-distribution spots (seed 505, 1024 "
-                                              "cycled); "
-                                              "target 0.5%% pot; bounded sample of %d "
-                                              "requests per rate" % args.served_requests,
-                              "rates": [served_bench(stream, lam, args.served_requests)
-                                        for lam in (50, 200, 800)]}
+    if world == 1 and args.batch_spots > 0 and args.served_requests > 0:
+        stream = wl.c3_stream(args.served_requests)
+        rates = [served_bench(stream, float(lam), args.served_requests)
+                 for lam in args.served_rates.split(",")]
+        line["served"] = {"distribution": "turn_c3 distribution: %d distinct 48,255-node turn "
+                                          "spots (seeded boards and mixture ranges, pot 100, "
+                                          "stack 400); target 0.5%% pot" % len(stream),
+                          "requests_per_rate": args.served_requests,
+                          "rates": rates}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(spot)
+        line["accuracy"] = accuracy()
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -97,8 +97,11 @@ int64_t BatchServer::submit(const gpu::PostflopSpot& spot, const gpu::StreetBetC
 }
 
 void BatchServer::setBudget(int64_t bytes) {
-  std::lock_guard<std::mutex> lock(m_);
-  budget_ = bytes;
+  {
+    std::lock_guard<std::mutex> lock(m_);
+    budget_ = bytes;
+  }
+  cvCompile_.notify_all();  // the compile-ahead limit follows the budget
 }
 
 void BatchServer::compileLoop() {
@@ -109,7 +112,10 @@ void BatchServer::compileLoop() {
     bool perStreet;
     {
       std::unique_lock<std::mutex> lock(m_);
-      cvCompile_.wait(lock, [&] { return closing_ || compileHead_ < compileQueue_.size(); });
+      cvCompile_.wait(lock, [&] {
+        return closing_ || (compileHead_ < compileQueue_.size() &&
+                            (ready_.empty() || budget_ <= 0 || readyBytes_ <= 2 * budget_));
+      });
       if (closing_) return;
       ticket = compileQueue_[compileHead_++];
       if (compileHead_ == compileQueue_.size()) {
@@ -152,6 +158,7 @@ void BatchServer::compileLoop() {
     r.result.deviceBytes = cs->bytes;
     r.state = kWaiting;
     ++stats_.waiting;
+    readyBytes_ += (int64_t)cs->bytes;
     ready_[ticket] = std::move(cs);
     cvReady_.notify_all();
   }
@@ -186,6 +193,7 @@ bool BatchServer::epoch() {
       ticket = it->first;
       cs = std::move(it->second);
       ready_.erase(it);
+      readyBytes_ -= (int64_t)cs->bytes;
       budget = budget_;
     }
     int slot = -1;
@@ -204,10 +212,12 @@ bool BatchServer::epoch() {
     }
     std::unique_lock<std::mutex> lock(m_);
     if (code == PPS_GB_OK && slot < 0) {
+      readyBytes_ += (int64_t)cs->bytes;
       ready_[ticket] = std::move(cs);  // waits for memory to free up
       break;
     }
     --stats_.waiting;
+    cvCompile_.notify_all();  // the waiting queue shrank
     if (code != PPS_GB_OK) {
       BatchResult res = reqs_.at(ticket).result;
       res.status = code;
@@ -248,6 +258,10 @@ bool BatchServer::epoch() {
   }
   n = std::max(n, kCheckStep);
   F.iterate(n);
+  // Wait for the replays here, so that the check time below covers the
+  // walks alone (the replays are timed on the device).
+  const double iterMs = F.lastIterateMs();
+  const double tIterated = nowMs();
   std::vector<int> due;
   for (int slot : slots)
     if (F.iterations(slot) >= nextCheck_.at(slot)) due.push_back(slot);
@@ -279,7 +293,6 @@ bool BatchServer::epoch() {
     nextCheck_[slot] = t + step;
   }
   const double tChecked = nowMs();
-  const double iterMs = F.lastIterateMs();
   {
     std::lock_guard<std::mutex> lock(m_);
     ++stats_.epochs;
@@ -287,7 +300,7 @@ bool BatchServer::epoch() {
     stats_.checks += (int64_t)due.size();
     stats_.captures = F.captures();
     stats_.iterateMs += iterMs;
-    stats_.checkMs += tChecked - tAdmitted;
+    stats_.checkMs += tChecked - tIterated;
   }
   if (done.empty()) return true;
 

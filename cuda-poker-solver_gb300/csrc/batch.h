@@ -124,6 +124,12 @@ class BatchServer {
   std::vector<int64_t> compileQueue_;  // FIFO of tickets to compile
   size_t compileHead_ = 0;
   std::map<int64_t, std::unique_ptr<CompiledSpot>> ready_;
+  // Device bytes of the compiled spots waiting for admission. Compile
+  // threads pause while it exceeds twice the HBM budget: spots beyond that
+  // cannot be admitted soon, and each holds its host tables meanwhile
+  // (~50 MB for a 48,255-node turn), so a long queue of requests would
+  // otherwise grow host memory without bound.
+  int64_t readyBytes_ = 0;
   std::map<int, int64_t> slotTicket_;
   std::map<int, int> nextCheck_;  // slot -> iteration count of its next check
   int64_t nextTicket_ = 1;

@@ -245,6 +245,7 @@ int pps_gb_get_info(pps_gb_solver* h, pps_gb_info* out) {
       out->h2d_bytes = s.engine()->h2dBytes();
       out->d2h_bytes = s.engine()->d2hBytes();
       out->engine = s.engine()->engineKind();
+      out->compensated = s.engine()->compensated() ? 1 : 0;
     }
   });
 }
@@ -452,6 +453,13 @@ int pps_gb_set_engine(pps_gb_solver* h, int engine) {
   });
 }
 
+int pps_gb_set_compensated(pps_gb_solver* h, int on) {
+  return guarded([&] {
+    SolverCore& s = core(h);
+    if (s.engine()) s.engine()->setCompensated(on != 0);
+  });
+}
+
 int pps_gb_time_iterations(pps_gb_solver* h, int n, double* ms) {
   return guarded([&] {
     if (!ms || n < 0) throw Error{PPS_GB_E_ARG, "bad arguments"};
@@ -480,10 +488,9 @@ int pps_gb_solve_noalloc(const pps_gb_spot* spot, const pps_gb_bet_config* cfg,
                          int first_iteration, int iterations, void* stream, int64_t* n_rows) {
   return guarded([&] {
     if (!spot || !cfg) throw Error{PPS_GB_E_ARG, "null argument"};
-    const int64_t n = pps::gb::noallocSolve(toSpot(*spot), toConfig(*cfg), d_regret, d_strat,
-                                            row_capacity, first_iteration, iterations,
-                                            static_cast<cudaStream_t>(stream));
-    if (n_rows) *n_rows = n;
+    pps::gb::noallocSolve(toSpot(*spot), toConfig(*cfg), d_regret, d_strat, row_capacity,
+                          first_iteration, iterations, static_cast<cudaStream_t>(stream),
+                          n_rows);
   });
 }
 

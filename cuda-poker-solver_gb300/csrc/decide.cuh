@@ -51,6 +51,22 @@ __device__ __forceinline__ DecRec loadRec(const uint32_t* __restrict__ recs, uin
   return d;
 }
 
+// One entry of the cumulative-strategy update: compensated (stratComp)
+// where the tree carries low words, else the plain f32 form.
+__device__ __forceinline__ void stratUpdate(float& sg, float& lo, float avg, float sigma,
+                                            const float* strLo) {
+  if (strLo) stratComp(sg, lo, avg, sigma);
+  else sg = sg * avg + sigma;
+}
+// Asks for the low words of a record's strategy rows ahead of the update
+// (an L2 hint, no data): they are read only there, by plain loads.
+__device__ __forceinline__ void prefetchStratLo(const DevTree& t, const DecRec& r, int q, int nq) {
+  if (!t.stratLo) return;
+  const float* lo = t.stratLo + (size_t)r.regQ * 4;
+  for (int a = 0; a < r.na; ++a)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(lo + ((size_t)a * nq + q) * 4));
+}
+
 // Backward decide record (CFR mode, f32 rows), one warp: lane = quad.
 __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<float>& rows,
                                              const DecRec& r, int lane) {
@@ -85,6 +101,7 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
     asm volatile("prefetch.global.L1 [%0];" ::"l"(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q));
     asm volatile("prefetch.global.L2 [%0];" ::"l"(str + ((size_t)a * nq + q) * 4));
   }
+  prefetchStratLo(t, r, q, nq);
   // Streaming form: a row is reloaded (a cache hit) instead of held in
   // registers, which keeps the kernel at 40 registers and 48 warps per SM;
   // the launches are bound by memory latency, not by instruction count.
@@ -100,18 +117,21 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
     for (int l = 0; l < 4; ++l) val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, 0) : 0.f) * c[l];
   }
   stq(out + 4 * q, val);
+  float* strLo = t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr;
   for (int a = 0; a < na; ++a) {
-    float rg[4], sg[4], c[4];
+    float rg[4], sg[4], c[4], lo[4] = {0.f, 0.f, 0.f, 0.f};
     const size_t o = ((size_t)a * nq + q) * 4;
     ldq(reg + o, rg);
     ldq(str + o, sg);
+    if (strLo) ldq(strLo + o, lo);
     ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, c);
     for (int l = 0; l < 4; ++l) {
       const float s = live[l] ? sigmaOf(rg[l], acc[l], uniform, 0) : 0.f;
-      sg[l] = sg[l] * avg + s;
+      stratUpdate(sg[l], lo[l], avg, s, strLo);
       rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
     }
     stq(str + o, sg);
+    if (strLo) stq(strLo + o, lo);
     stq(reg + o, rg);
   }
 }
@@ -193,6 +213,7 @@ __device__ __forceinline__ void decideRecordOwnRows(const DevTree& t, const DecR
     cpAsync16(&R[a * kThreads + tid], reg + o);
     cpAsync16(&S[a * kThreads + tid], str + o);
   }
+  prefetchStratLo(t, r, q, nq);
 }
 
 // Backward decide record, staged (same arithmetic and order as
@@ -249,18 +270,21 @@ __device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRo
     for (int l = 0; l < 4; ++l) val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, 0) : 0.f) * c[l];
   }
   stq(out + 4 * q, val);
+  float* strLo = t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr;
   for (int a = 0; a < na; ++a) {
-    float rg[4], sg[4], c[4];
+    float rg[4], sg[4], c[4], lo[4] = {0.f, 0.f, 0.f, 0.f};
     const size_t o = ((size_t)a * nq + q) * 4;
     ld4s(&R[a * kThreads + tid], rg);
     ld4s(&S[a * kThreads + tid], sg);
     ld4s(&C[a * kThreads + tid], c);
+    if (strLo) ldq(strLo + o, lo);
     for (int l = 0; l < 4; ++l) {
       const float s = live[l] ? sigmaOf(rg[l], acc[l], uniform, 0) : 0.f;
-      sg[l] = sg[l] * avg + s;
+      stratUpdate(sg[l], lo[l], avg, s, strLo);
       rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
     }
     stq(str + o, sg);
+    if (strLo) stq(strLo + o, lo);
     stq(reg + o, rg);
   }
 }
@@ -338,6 +362,9 @@ __device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const De
 // output: their copies go out after the wait.
 // ---------------------------------------------------------------------------
 constexpr int kBarSpins = 1 << 16;
+// Rounds of kBarSpins polls that a warp whose wait ran out spends draining
+// its own copies before it leaves the record.
+constexpr int kDrainRounds = 4;
 
 __device__ __forceinline__ void pdlTrigger() { asm volatile("griddepcontrol.launch_dependents;"); }
 __device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
@@ -413,14 +440,24 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
         bulkLoad(&S[a * kRecQuads], str + o, segBytes, bar);
       }
   }
+  if (r.own && q0 + lane < nq) prefetchStratLo(t, r, q0 + lane, nq);
   pdlWait();
   if (lane == 0)
     for (int a = 0; a < na; ++a)
       bulkLoad(&C[a * kRecQuads], rows.cfv + ((size_t)r.kid[a] + q0) * 4, segBytes, bar);
-  const bool ok = barWait(bar, phase);
+  const uint32_t parity = phase;
+  const bool ok = barWait(bar, parity);
   phase ^= 1u;
   if (!ok) {
-    if (lane == 0 && t.err) atomicOr(t.err, 1);
+    // Give-up path: the copies are this warp's own and still count on the
+    // barrier. Wait for them once more (bounded again) so that the CTA does
+    // not leave with asynchronous writes into its shared memory in flight;
+    // error bit 1: the wait ran out, bit 2: the drain ran out as well (the
+    // copies may then outlive the CTA; the host discards the launch's
+    // results either way).
+    bool drained = false;
+    for (int k = 0; k < kDrainRounds && !drained; ++k) drained = barWait(bar, parity);
+    if (lane == 0 && t.err) atomicOr(t.err, drained ? 1 : 3);
     return;
   }
   const int q = q0 + lane;
@@ -456,18 +493,21 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
     for (int l = 0; l < 4; ++l) val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, 0) : 0.f) * c[l];
   }
   stq(out + 4 * q, val);
+  float* strLo = t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr;
   for (int a = 0; a < na; ++a) {
-    float rg[4], sg[4], c[4];
+    float rg[4], sg[4], c[4], lo[4] = {0.f, 0.f, 0.f, 0.f};
     const size_t o = ((size_t)a * nq + q) * 4;
     ld4s(&R[a * kRecQuads + lane], rg);
     ld4s(&S[a * kRecQuads + lane], sg);
     ld4s(&C[a * kRecQuads + lane], c);
+    if (strLo) ldq(strLo + o, lo);
     for (int l = 0; l < 4; ++l) {
       const float s = live[l] ? sigmaOf(rg[l], acc[l], uniform, 0) : 0.f;
-      sg[l] = sg[l] * avg + s;
+      stratUpdate(sg[l], lo[l], avg, s, strLo);
       rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
     }
     stq(str + o, sg);
+    if (strLo) stq(strLo + o, lo);
     stq(reg + o, rg);
   }
 }

@@ -71,6 +71,7 @@ struct Engine::Dev {
   int4* groups = nullptr;
   uint32_t* recs = nullptr;
   uint32_t* recTasks = nullptr;
+  float* stratLo = nullptr;  // low words of the strategy rows (compensated sums)
   std::vector<Launch> plan[3];  // per engine kind: one iteration (kind 0 flattened)
   StagedPlan staged;           // kind 0 as captured
   StagedEvents sev;
@@ -238,7 +239,10 @@ double Engine::taskBytes(int task, int tr, bool fwd) const {
       return 4.0 * e * (1.0 + kids / std::max(n, 1));
     }
     default:
-      return nd.player == tr ? 4.0 * share(t.n(u, tr)) * (5.0 * nd.na + 1)
+      // Traverser's node: regret and strategy rows read and written, child
+      // values read, own value written (plus the strategy's low words read
+      // and written with compensated sums).
+      return nd.player == tr ? 4.0 * share(t.n(u, tr)) * ((comp_ ? 7.0 : 5.0) * nd.na + 1)
                              : 4.0 * share(t.n(u, tr)) * (nd.na + 1.0);
   }
 }
@@ -357,10 +361,31 @@ void Engine::buildPlans() {
   }
 }
 
+void Engine::setCompensated(bool on) {
+  Dev& d = *d_;
+  if (on == comp_) return;
+  GB_CK(cudaStreamSynchronize(d.stream));
+  if (on) {
+    if (!d.stratLo) d.stratLo = d.own(alloc<float>(L_.regQuads * 4, deviceBytes_));
+    GB_CK(cudaMemsetAsync(d.stratLo, 0, L_.regQuads * 16, d.stream));
+    GB_CK(cudaStreamSynchronize(d.stream));
+  }
+  d.tree.stratLo = on ? d.stratLo : nullptr;
+  comp_ = on;
+  buildPlans();  // the byte model counts the low words
+  if (d.exec) {  // the captured kernels hold the old tree arguments
+    cudaGraphExecDestroy(d.exec);
+    cudaGraphDestroy(d.graph);
+    d.exec = nullptr;
+    d.graph = nullptr;
+  }
+}
+
 void Engine::zeroRows() {
   Dev& d = *d_;
   GB_CK(cudaMemsetAsync(d.tree.regret, 0, L_.regQuads * 16, d.stream));
   GB_CK(cudaMemsetAsync(d.tree.strat, 0, L_.regQuads * 16, d.stream));
+  if (d.tree.stratLo) GB_CK(cudaMemsetAsync(d.tree.stratLo, 0, L_.regQuads * 16, d.stream));
   GB_CK(cudaMemsetAsync(d.counter, 0, sizeof(int), d.stream));
   GB_CK(cudaStreamSynchronize(d.stream));
 }
@@ -754,6 +779,9 @@ void Engine::setDenseRows(int which, const std::vector<float>& dense) {
     GB_CK(cudaMemcpy(which == 0 ? d_->tree.regret : d_->tree.strat, padded.data(),
                      padded.size() * sizeof(float), cudaMemcpyHostToDevice));
   h2d_ += (int64_t)(padded.size() * sizeof(float));
+  // New strategy sums carry no low words.
+  if (which == 1 && d_->tree.stratLo && L_.regQuads)
+    GB_CK(cudaMemset(d_->tree.stratLo, 0, L_.regQuads * 16));
 }
 
 namespace {
@@ -799,6 +827,8 @@ void Engine::unpackRows(int which, const std::vector<uint16_t>& codes,
     GB_CK(cudaMemsetAsync(rows, 0, (size_t)L_.regQuads * 4 * sizeof(float), d_->stream));
   gb::unpackRows(rows, actionRowTable(t_, L_), which == 0, codes, scales, d_->stream);
   h2d_ += (int64_t)(codes.size() * sizeof(uint16_t) + scales.size() * sizeof(float));
+  if (which == 1 && d_->tree.stratLo && L_.regQuads)
+    GB_CK(cudaMemsetAsync(d_->tree.stratLo, 0, L_.regQuads * 16, d_->stream));
 }
 
 std::vector<float> Engine::nodeRows(int which, int node) const {

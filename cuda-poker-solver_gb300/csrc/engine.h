@@ -80,6 +80,12 @@ class Engine {
   // setEngineKind, and where the fused plan does not apply.
   void autotune();
   int engineKind() const { return engineKind_; }
+  // Compensated (two-float) cumulative-strategy sums: the strategy rows get
+  // a row of low words (allocated on first use, zeroed when turned on; the
+  // current sums become their high words) and the update carries its
+  // rounding errors there. Off by default; recaptures on change.
+  void setCompensated(bool on);
+  bool compensated() const { return comp_; }
   int launchesPerIteration() const { return launchesPerIter_; }
   size_t deviceBytes() const { return deviceBytes_; }
   // The stream every launch of this engine is issued on.
@@ -94,6 +100,7 @@ class Engine {
   int engineKind_ = 0;
   std::vector<int> subEnd_;  // per node: one past the last id of its subtree (walkFrom)
   bool tuned_ = false;
+  bool comp_ = false;
   int launchesPerIter_ = 0;
   size_t deviceBytes_ = 0;
   mutable int64_t h2d_ = 0, d2h_ = 0;

@@ -43,6 +43,9 @@ struct DevTree {
   const ShowdownInfo* poolSd;
   float* regret;
   float* strat;
+  float* stratLo;        // compensated strategy sums: the low words of the
+                         // strategy rows (same layout), or nullptr for the
+                         // plain f32 sums
   const float* coef;     // 3 floats per iteration: pos, neg, avg
   const int* counter;    // current iteration index, per spot (node meta
                          // bits 16-31; a lone spot is spot 0)
@@ -114,6 +117,24 @@ __device__ __forceinline__ T sigmaOfScaled(T x, T acc, T scale, T uniform, int s
   } else {
     return sigmaOf(x, acc, uniform, sigSrc);
   }
+}
+
+// Cumulative-strategy update s <- s * avg + sigma (the reference's
+// cuda/gpu_cfr.cu:512-523). Plain: one f32 fma. Compensated: s is carried
+// as an unevaluated sum hi + lo of two floats; the rounding error of the
+// product (from an fma) and of the sum (Knuth's two-sum) go into lo, and
+// the pair is renormalized (Dekker's fast two-sum) so that hi stays the
+// sum rounded to f32 - every reader of the strategy rows reads hi alone.
+// The _rn intrinsics keep the compiler from contracting the steps.
+__device__ __forceinline__ void stratComp(float& hi, float& lo, float avg, float sigma) {
+  const float p = __fmul_rn(hi, avg);
+  const float ep = __fmaf_rn(hi, avg, -p);
+  const float t = __fadd_rn(p, sigma);
+  const float bb = __fsub_rn(t, p);
+  const float es = __fadd_rn(__fsub_rn(p, __fsub_rn(t, bb)), __fsub_rn(sigma, bb));
+  const float l = __fmaf_rn(lo, avg, __fadd_rn(ep, es));
+  hi = __fadd_rn(t, l);
+  lo = __fsub_rn(l, __fsub_rn(hi, t));
 }
 
 template <typename T>
@@ -638,17 +659,23 @@ __device__ void decideChunk(const DevTree& t, const DevRows<T>& rows, int u, int
         }
     stq(out + 4 * q, val);
     if (mode != kModeCFR) return;
+    float* strLo = t.stratLo ? t.stratLo + (size_t)nd.regQ * 4 : nullptr;
 #pragma unroll
     for (int a = 0; a < kRegNa; ++a)
       if (a < na) {
-        float rg[4], sg[4];
+        float rg[4], sg[4], lo[4];
         const size_t o = ((size_t)a * nq + q) * 4;
         ldq(reg + o, rg);
         ldq(str + o, sg);
-        for (int l = 0; l < 4; ++l) {
-          sg[l] = sg[l] * avg + (float)x[a][l];
-          rg[l] = rg[l] * (rg[l] >= 0.0f ? pos : neg) + (float)(cv[a][l] - val[l]);
+        if (strLo) {
+          ldq(strLo + o, lo);
+          for (int l = 0; l < 4; ++l) stratComp(sg[l], lo[l], avg, (float)x[a][l]);
+          stq(strLo + o, lo);
+        } else {
+          for (int l = 0; l < 4; ++l) sg[l] = sg[l] * avg + (float)x[a][l];
         }
+        for (int l = 0; l < 4; ++l)
+          rg[l] = rg[l] * (rg[l] >= 0.0f ? pos : neg) + (float)(cv[a][l] - val[l]);
         stq(str + o, sg);
         stq(reg + o, rg);
       }
@@ -670,19 +697,23 @@ __device__ void decideChunk(const DevTree& t, const DevRows<T>& rows, int u, int
   }
   stq(out + 4 * q, val);
   if (mode != kModeCFR) return;
+  float* strLo = t.stratLo ? t.stratLo + (size_t)nd.regQ * 4 : nullptr;
   for (int a = 0; a < na; ++a) {
-    float rg[4], sg[4];
+    float rg[4], sg[4], lo[4] = {0.f, 0.f, 0.f, 0.f};
     T c[4];
     const size_t o = ((size_t)a * nq + q) * 4;
     ldq(reg + o, rg);
     ldq(str + o, sg);
+    if (strLo) ldq(strLo + o, lo);
     ldq(rows.cfv + (size_t)t.rows[kids[a]].cfvQ * 4 + 4 * q, c);
     for (int l = 0; l < 4; ++l) {
       const T s = live[l] ? sigmaOf((T)rg[l], acc[l], uniform, 0) : T(0);
-      sg[l] = sg[l] * avg + (float)s;
+      if (strLo) stratComp(sg[l], lo[l], avg, (float)s);
+      else sg[l] = sg[l] * avg + (float)s;
       rg[l] = rg[l] * (rg[l] >= 0.0f ? pos : neg) + (float)(c[l] - val[l]);
     }
     stq(str + o, sg);
+    if (strLo) stq(strLo + o, lo);
     stq(reg + o, rg);
   }
 }

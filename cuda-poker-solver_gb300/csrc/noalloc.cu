@@ -12,10 +12,14 @@
 // Host code never dereferences or passes gNoAllocScratch itself: on the
 // host that name is a stand-in, not a device address. Its device address is
 // looked up once per device with cudaGetSymbolAddress (with that device
-// current) and kept; the first call on a device does this set-up, so it
-// should come before any stream capture. All calls share the array and leave
-// their contents in it; every buffer a call reads is written by that call
-// first (or cleared), and calls that overlap on a GPU race on it.
+// current) and kept, keyed on the device's current context: after a
+// cudaDeviceReset the next call finds a new context and looks the address
+// up again. The first call on a device (and the first after a reset) does
+// this set-up, so it should come before any stream capture. All calls share
+// the array and leave their contents in it; every buffer a call reads is
+// written by that call first (or cleared), and calls that overlap on a GPU
+// race on it.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -50,20 +54,52 @@ namespace {
 
 constexpr int kMaxDevices = 128;
 std::mutex gSetupMutex;
-unsigned char* gScratchOnDevice[kMaxDevices] = {};
+struct ScratchAddr {
+  CUcontext ctx = nullptr;      // the context the address belongs to
+  unsigned char* ptr = nullptr; // gNoAllocScratch's device address there
+};
+ScratchAddr gScratchOnDevice[kMaxDevices];
 
-// Device address of gNoAllocScratch on the current device (set up once).
+// The driver's cuCtxGetCurrent, looked up through the runtime (the library
+// does not link the driver library directly).
+decltype(&::cuCtxGetCurrent) ctxGetCurrent() {
+  static const decltype(&::cuCtxGetCurrent) fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<decltype(&::cuCtxGetCurrent)>(p);
+  }();
+  return fn;
+}
+
+CUcontext currentContext() {
+  const auto get = ctxGetCurrent();
+  if (!get) throw Error{PPS_GB_E_CUDA, "driver entry point missing: cuCtxGetCurrent"};
+  CUcontext ctx = nullptr;
+  if (get(&ctx) != CUDA_SUCCESS) throw Error{PPS_GB_E_CUDA, "cuCtxGetCurrent failed"};
+  return ctx;
+}
+
+// Device address of gNoAllocScratch on the current device, looked up once
+// per device and context (cudaGetSymbolAddress also makes the device's
+// primary context current on the first call).
 unsigned char* scratchBase() {
   int dev = 0;
   NA_CK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) throw Error{PPS_GB_E_CUDA, "device index out of range"};
+  const CUcontext ctx = currentContext();
   std::lock_guard<std::mutex> lock(gSetupMutex);
-  if (!gScratchOnDevice[dev]) {
+  ScratchAddr& a = gScratchOnDevice[dev];
+  if (!a.ptr || !ctx || a.ctx != ctx) {
     void* p = nullptr;
     NA_CK(cudaGetSymbolAddress(&p, gNoAllocScratch));
-    gScratchOnDevice[dev] = static_cast<unsigned char*>(p);
+    a.ptr = static_cast<unsigned char*>(p);
+    a.ctx = currentContext();
   }
-  return gScratchOnDevice[dev];
+  return a.ptr;
 }
 
 // Per decide node: where its rows sit in the caller's dense layout and in
@@ -105,16 +141,25 @@ struct Arena {
 
 int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, float* dRegret,
                      float* dStrat, int64_t rowCapacity, int firstIteration, int iterations,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, int64_t* needRows) {
   if (firstIteration < 0 || iterations < 0 ||
       (int64_t)firstIteration + iterations > (int64_t)INT_MAX)
     throw Error{PPS_GB_E_ARG, "bad iteration range"};
+  // An error left pending by the caller's own earlier CUDA work is reported
+  // as such (and left pending), not as a failure of this solve.
+  {
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+      throw Error{PPS_GB_E_CUDA, std::string("a CUDA error was pending before this call: ") +
+                                     cudaGetErrorString(pending)};
+  }
   gpu::StreetBetConfigs cfgs;
   cfgs.street[0] = cfgs.street[1] = cfgs.street[2] = cfg;
   const Tree t = compileTree(spot, cfgs, false);
   if (t.empty) throw Error{PPS_GB_E_STATE, "solver compiled to empty ranges"};
+  if (needRows) *needRows = t.rowTotal;  // also on the errors below: a size query
   if (t.rowTotal > (int64_t)INT_MAX) throw Error{PPS_GB_E_BUDGET, "row table too large"};
-  if (!dRegret || !dStrat) throw Error{PPS_GB_E_ARG, "null row buffer"};
+  if (t.rowTotal > 0 && (!dRegret || !dStrat)) throw Error{PPS_GB_E_ARG, "null row buffer"};
   if (rowCapacity < t.rowTotal)
     throw Error{PPS_GB_E_ARG, "row buffers hold " + std::to_string(rowCapacity) +
                                   " floats; the spot needs " + std::to_string(t.rowTotal)};
@@ -147,13 +192,19 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
     rowMap.push_back({dense, L.nodes[u].regQ, nd.na, n});
     dense += nd.na * n;
   }
-  std::vector<float> coef((size_t)(firstIteration + iterations) * 3 + 3, 0.0f);
+  // The schedule window of this call only: the device counter starts at 0
+  // and entry k holds the coefficients of absolute iteration
+  // firstIteration + k (the DCFR coefficients depend on the absolute index
+  // alone), so a continuation far into a solve costs no more than its own
+  // iterations.
+  std::vector<float> coef((size_t)iterations * 3 + 3, 0.0f);
   Schedule sched;
-  for (int k = 0; k < firstIteration + iterations; ++k) {
+  for (int k = 0; k < iterations; ++k) {
     double c[3];
-    sched.coefs(k, firstIteration + iterations, c);
+    sched.coefs(firstIteration + k, firstIteration + iterations, c);
     for (int j = 0; j < 3; ++j) coef[(size_t)k * 3 + j] = (float)c[j];
   }
+  const int counterStart = 0;
   std::vector<float> rootReach[2];
   for (int tr = 0; tr < 2; ++tr) {
     const Side& opp = t.side[1 - tr];
@@ -175,9 +226,12 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
                oReach0 = A.take(L.reachQuads[0] * 16), oReach1 = A.take(L.reachQuads[1] * 16),
                oCoef = A.take(bytesOf(coef)), oCounter = A.take(sizeof(int));
   if (A.used > (size_t)PPS_GB_NOALLOC_SCRATCH_BYTES)
-    throw Error{PPS_GB_E_BUDGET, "spot needs " + std::to_string(A.used) +
-                                     " bytes of scratch; the static scratch holds " +
-                                     std::to_string((size_t)PPS_GB_NOALLOC_SCRATCH_BYTES)};
+    throw Error{PPS_GB_E_BUDGET,
+                "spot and iteration window need " + std::to_string(A.used) +
+                    " bytes of scratch (of which the schedule of " + std::to_string(iterations) +
+                    " iterations takes " + std::to_string(bytesOf(coef)) +
+                    "); the static scratch holds " +
+                    std::to_string((size_t)PPS_GB_NOALLOC_SCRATCH_BYTES)};
 
   unsigned char* base = scratchBase();
   auto put = [&](size_t off, const auto& v) {
@@ -199,7 +253,7 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
   put(oCoef, coef);
   put(oReach0, rootReach[0]);
   put(oReach1, rootReach[1]);
-  NA_CK(cudaMemcpyAsync(base + oCounter, &firstIteration, sizeof(int), cudaMemcpyHostToDevice,
+  NA_CK(cudaMemcpyAsync(base + oCounter, &counterStart, sizeof(int), cudaMemcpyHostToDevice,
                         stream));
   // Padded rows start from zero (padding lanes must stay zero), then take
   // the caller's values.
@@ -208,10 +262,14 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
   float* reg = reinterpret_cast<float*>(base + oReg);
   float* str = reinterpret_cast<float*>(base + oStr);
   const RowMap* map = reinterpret_cast<const RowMap*>(base + oMap);
+  // A spot without decide nodes (a zero behind-stack makes the root a
+  // showdown or chance node) has no rows to move.
   const int nMap = (int)rowMap.size();
   const unsigned gMap = (unsigned)std::min(nMap, 1 << 20);
-  repackK<<<gMap, 128, 0, stream>>>(map, nMap, dRegret, reg, 1);
-  repackK<<<gMap, 128, 0, stream>>>(map, nMap, dStrat, str, 1);
+  if (nMap > 0) {
+    repackK<<<gMap, 128, 0, stream>>>(map, nMap, dRegret, reg, 1);
+    repackK<<<gMap, 128, 0, stream>>>(map, nMap, dStrat, str, 1);
+  }
 
   DevTree tree{};
   tree.nodes = reinterpret_cast<const NodeDev*>(base + oNodes);
@@ -259,8 +317,10 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
     advanceCounterK<<<1, 32, 0, stream>>>(counter, 1);
     NA_CK(cudaGetLastError());
   }
-  repackK<<<gMap, 128, 0, stream>>>(map, nMap, reg, dRegret, 0);
-  repackK<<<gMap, 128, 0, stream>>>(map, nMap, str, dStrat, 0);
+  if (nMap > 0) {
+    repackK<<<gMap, 128, 0, stream>>>(map, nMap, reg, dRegret, 0);
+    repackK<<<gMap, 128, 0, stream>>>(map, nMap, str, dStrat, 0);
+  }
   NA_CK(cudaGetLastError());
   NA_CK(cudaStreamSynchronize(stream));
   return t.rowTotal;

@@ -48,7 +48,8 @@ class Info(C.Structure):
                 ("total_iterations", C.c_int64), ("n_base", C.c_int32 * 2),
                 ("row_total", C.c_int64), ("empty", C.c_int32),
                 ("launches_per_iteration", C.c_int32), ("device_bytes", C.c_int64),
-                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("engine", C.c_int32)]
+                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("engine", C.c_int32),
+                ("compensated", C.c_int32)]
 
 
 class KernelStat(C.Structure):
@@ -129,6 +130,7 @@ _SIGS = {
     "pps_gb_write_rows": (C.c_int, [H, C.c_int, P(C.c_float), C.c_int64]),
     "pps_gb_walk": (C.c_int, [H, C.c_int, C.c_int, P(C.c_double), P(C.c_double)]),
     "pps_gb_set_engine": (C.c_int, [H, C.c_int]),
+    "pps_gb_set_compensated": (C.c_int, [H, C.c_int]),
     "pps_gb_time_iterations": (C.c_int, [H, C.c_int, P(C.c_double)]),
     "pps_gb_profile": (C.c_int, [H, C.c_int, C.c_int, P(KernelStat), C.c_int, P(C.c_int)]),
     "pps_gb_solve_noalloc": (C.c_int, [P(Spot), P(BetConfig), C.c_void_p, C.c_void_p, C.c_int64,

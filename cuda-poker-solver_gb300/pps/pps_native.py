@@ -415,6 +415,10 @@ class Solver:
     def set_engine(self, kind: int) -> None:
         check(lib.pps_gb_set_engine(self._h, int(kind)))
 
+    def set_compensated(self, on: bool = True) -> None:
+        """Two-float cumulative-strategy sums (pps_gb_set_compensated)."""
+        check(lib.pps_gb_set_compensated(self._h, 1 if on else 0))
+
     def time_iterations(self, n: int) -> float:
         """Milliseconds of n more iterations (graph replays, CUDA events on
         the solver's stream)."""

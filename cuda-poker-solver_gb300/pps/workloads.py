@@ -228,6 +228,14 @@ def batched(count: int = 256, seed: int = 404) -> List[Spot]:
     return out
 
 
+def c3_stream(count: int = 1024, seed: int = 606) -> List[Spot]:
+    """The served distribution: spots drawn like turn_c3 (48,255-node turn
+    trees), each with its own seeded 4-card board and mixture ranges (60%
+    of combos at U(0.5, 1), the rest U(0, 0.2)); pot 100, stack 400, bets
+    {25, 50, 100, 150}% plus all-in on both streets, raises 2x, max 4."""
+    return [turn_c3(seed=seed * 1000003 + k) for k in range(count)]
+
+
 def turn_short() -> Spot:
     """Short stack: all-in on the turn, the river is a dead-street runout
     (the regression spot of tools/quality/gpu_postflop_parity.sh:139)."""

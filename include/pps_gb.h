@@ -98,6 +98,7 @@ typedef struct {
   int64_t h2d_bytes; /* host->device bytes copied since creation */
   int64_t d2h_bytes; /* device->host bytes copied since creation */
   int32_t engine;    /* 0 terminal groups (default), 1 per-node terminal kernels */
+  int32_t compensated; /* 1: two-float cumulative-strategy sums (pps_gb_set_compensated) */
 } pps_gb_info;
 
 /* Per kernel class of one profile pass (pps_gb_profile). */
@@ -232,6 +233,15 @@ int pps_gb_walk(pps_gb_solver* h, int traverser, int mode, double* root_cfv,
  * faster; setting an engine turns that off. */
 int pps_gb_set_engine(pps_gb_solver* h, int engine);
 
+/* Extension: compensated (two-float) cumulative-strategy sums, the update
+ * strat = strat * avg + sigma of cuda/gpu_cfr.cu:512-523 carried as an
+ * unevaluated sum of two floats (a row of low words beside the strategy
+ * rows, device memory allocated on first use). The strategy rows keep the
+ * sum rounded to f32, so every reader - walks, queries, files - is
+ * unchanged; turning the option on keeps the current sums (low words 0).
+ * Off by default (the reference's plain f32 sums). */
+int pps_gb_set_compensated(pps_gb_solver* h, int on);
+
 /* Benchmark helper: enqueues n further DCFR iterations (graph replays that
  * continue the current DCFR schedule) bracketed by CUDA events recorded on
  * the solver's own stream, waits, and returns the elapsed milliseconds.
@@ -264,14 +274,24 @@ int pps_gb_profile(pps_gb_solver* h, int n, int flags, pps_gb_kernel_stat* out,
  * (tree tables, reach and value rows, schedule) lives in ONE static device
  * array of PPS_GB_NOALLOC_SCRATCH_BYTES (64 MiB), held by every GPU that
  * loads the library until the process exits; spots that need more are
- * rejected with PPS_GB_E_BUDGET and a message giving both sizes. The call
- * allocates no device memory (no cudaMalloc, cudaFree or allocating library
- * routine), issues its work on `stream` (NULL: the legacy default stream)
- * and waits for it. The first call on a device looks up the array's device
- * address with cudaGetSymbolAddress; make that first call before any stream
- * capture. All calls share the array and leave their contents in it: calls
- * that overlap on a GPU (other threads or streams) race - serialize them.
- * *n_rows receives the row count the spot needs. */
+ * rejected with PPS_GB_E_BUDGET and a message giving both sizes (the
+ * schedule table counts too: it holds this call's `iterations` entries, so
+ * a very long call may need splitting). The call allocates no device memory
+ * (no cudaMalloc, cudaFree or allocating library routine), issues its work
+ * on `stream` (NULL: the legacy default stream) and waits for it. The first
+ * call on a device looks up the array's device address with
+ * cudaGetSymbolAddress and keeps it for the device's current context (after
+ * a cudaDeviceReset the next call looks it up again); make that first call
+ * before any stream capture. All calls share the array and leave their
+ * contents in it: calls that overlap on a GPU (other threads or streams)
+ * race - serialize them. A spot without decide nodes (zero behind-stack)
+ * has no rows: the buffers may then be NULL. A CUDA error left pending by
+ * the caller's earlier work is reported as such (PPS_GB_E_CUDA) and left
+ * pending.
+ * *n_rows (may be NULL) receives the row count the spot needs as soon as
+ * the spot is compiled - also when the call then fails because
+ * row_capacity is too small or the scratch too small - so a call with
+ * row_capacity 0 is a size query. */
 int pps_gb_solve_noalloc(const pps_gb_spot* spot, const pps_gb_bet_config* cfg,
                          float* d_regret, float* d_strat, int64_t row_capacity,
                          int first_iteration, int iterations, void* stream,

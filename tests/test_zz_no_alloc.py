@@ -83,3 +83,53 @@ def test_noalloc_rejects_spots_beyond_the_scratch():
     assert rc == _abi.E_BUDGET
     msg = _abi.lib.pps_gb_last_error().decode()
     assert "scratch" in msg and str(64 << 20) in msg
+
+
+@pytest.mark.parametrize("name", ["river_c1", "turn_api"])
+def test_noalloc_spot_without_decide_nodes(name):
+    """A zero behind-stack makes the root a showdown (river) or chance node
+    (turn): the spot has no decide nodes and no rows. The call succeeds with
+    NULL row buffers and reports 0 rows, as the regular solver does."""
+    pytest.importorskip("torch")
+    import dataclasses
+    spot = dataclasses.replace(wl.NAMED[name](), stack=0)
+    ref = solver(spot)
+    ref.solve(3)
+    assert ref.info().row_total == 0
+    n_rows = C.c_int64(-1)
+    rc = _abi.lib.pps_gb_solve_noalloc(
+        C.byref(_abi_spot(spot)), C.byref(abi_cfgs(spot)[0]), None, None, 0, 0, 3, None,
+        C.byref(n_rows))
+    assert rc == 0, _abi.lib.pps_gb_last_error().decode()
+    assert n_rows.value == 0
+
+
+def test_noalloc_size_query_and_late_window():
+    """row_capacity 0 is a size query: the call fails with PPS_GB_E_ARG and
+    still reports the rows the spot needs. A continuation far into a solve
+    (absolute iteration 6,000,000) holds only its own schedule window in the
+    scratch, so it runs; its coefficients are those of the late iterations
+    (positive regrets kept almost whole, the average weighted ~1)."""
+    torch = pytest.importorskip("torch")
+    spot = wl.river_c1()
+    n_rows = C.c_int64(-1)
+    rc = _abi.lib.pps_gb_solve_noalloc(
+        C.byref(_abi_spot(spot)), C.byref(abi_cfgs(spot)[0]), None, None, 0, 0, 1, None,
+        C.byref(n_rows))
+    assert rc == _abi.E_ARG
+    n = solver(spot).info().row_total
+    assert n_rows.value == n
+
+    regret = torch.zeros(n, dtype=torch.float32, device="cuda")
+    strat = torch.zeros(n, dtype=torch.float32, device="cuda")
+    rc, rows = _noalloc(spot, regret, strat, 0, 20, torch)
+    assert rc == 0 and rows == n
+    before = strat.clone()
+    rc, _ = _noalloc(spot, regret, strat, 6_000_000, 2, torch)
+    assert rc == 0, _abi.lib.pps_gb_last_error().decode()
+    s = strat.cpu().numpy()
+    assert np.all(np.isfinite(s)) and np.all(s >= 0)
+    # Average weight ((t-k)/(t-k+1))^3 ~ 1 this late: the strategy sums grow
+    # by about one strategy (1 per combo summed over actions) per iteration.
+    grow = float(s.sum() - before.cpu().numpy().sum())
+    assert grow > 0
