@@ -1,6 +1,7 @@
 #!/bin/sh
-# Builds the reference's own code, compiled in place from /root/reference,
-# into oracle/_ref/ (git-ignored). TEST INFRASTRUCTURE ONLY: these programs
+# Builds the reference's own code, compiled in place from the reference
+# checkout (PPS_REFERENCE; default: a `reference` directory beside this
+# repository), into oracle/_ref/ (git-ignored). TEST INFRASTRUCTURE ONLY: these programs
 # generate and pin the golden fixtures under tests/golden/; no product code
 # links or runs them.
 #
@@ -13,11 +14,11 @@
 #                            oracle/ref/ref_gpu.cpp as a second checker and
 #                            timed beside the CPU port
 #
-# Only files under /root/reference are compiled; the reference's own build
-# system (CMake/Makefile) is not used.
+# Only the reference checkout's own files are compiled; its build system
+# (CMake/Makefile) is not used.
 set -e
-REF="${PPS_REFERENCE:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${PPS_REFERENCE:-$HERE/../../../reference}"
 OUT="$HERE/../_ref"
 if [ ! -d "$REF/cuda" ]; then
   echo "reference sources not found at $REF" >&2

@@ -11,6 +11,15 @@
 //
 //   ref_capture <out.bin> <board> <oop> <ip> <pot> <stack> <bets> <raises>
 //               <maxRaises>
+//   ref_capture --save <out.pps> <iterations> <board> <oop> <ip> <pot> <stack>
+//               <bets> <raises> <maxRaises>
+//       the reference's own save() (cuda/gpu_cfr.cu:2743-2785) of the spot
+//       with rows set to a fixed pattern (savePattern) and the iteration
+//       count given: a "PPS1" version-1 solution file written by the
+//       reference, for the file-format golden test
+//   ref_capture --load <in.pps> <out.bin>
+//       the reference's load constructor (cuda/gpu_cfr.cu:2787-2853) on a
+//       solution file, dumping the rows and scalars it read back
 //
 // <oop>/<ip>: a range string (reference syntax, src/range.h:34-41) or
 // "@path" to 1326 little-endian float64 combo weights.
@@ -146,6 +155,60 @@ std::vector<double> parseList(const std::string& s) {
 
 }  // namespace
 
+// Deterministic row contents for the file-format golden: regrets of both
+// signs, strategy sums >= 0 (the test reproduces them from the index).
+float savePattern(int which, uint32_t i) {
+  if (which == 0) return (float)((int)((i * 2654435761u) % 20001u) - 10000) / 64.0f;
+  return (float)((i * 40503u) % 1000u) / 8.0f;
+}
+
+int saveMode(int argc, char** argv) {
+  // --save <out.pps> <iterations> <board> <oop> <ip> <pot> <stack> <bets> <raises> <maxRaises>
+  if (argc != 12) return 2;
+  gpu::PostflopSpot spot;
+  const std::string board = argv[4];
+  spot.nBoard = (int)board.size() / 2;
+  for (int i = 0; i < spot.nBoard; ++i) spot.board[i] = cardFromText(board, i);
+  spot.oop = rangeFromSpec(argv[5]);
+  spot.ip = rangeFromSpec(argv[6]);
+  spot.pot = std::stoll(argv[7]);
+  spot.stack = std::stoll(argv[8]);
+  pf::BetConfig cfg;
+  cfg.betFracs.clear();
+  parseBets(argv[9], cfg);
+  cfg.raiseMults = parseList(argv[10]);
+  cfg.maxRaises = std::atoi(argv[11]);
+  gpu::GpuPostflopSolver solver(spot, cfg);
+  auto* I = solver.impl_;
+  for (size_t i = 0; i < I->regTotal; ++i) {
+    I->dRegret[i] = savePattern(0, (uint32_t)i);
+    I->dStrat[i] = savePattern(1, (uint32_t)i);
+  }
+  solver.totalIters_ = std::atoll(argv[3]);
+  I->lastAlgo = "dcfr";
+  solver.save(argv[2]);
+  std::fprintf(stderr, "ref_capture --save: nodes=%d regTotal=%zu -> %s\n", I->numNodes,
+               I->regTotal, argv[2]);
+  return 0;
+}
+
+int loadMode(int argc, char** argv) {
+  // --load <in.pps> <out.bin>
+  if (argc != 4) return 2;
+  gpu::GpuPostflopSolver solver{std::string(argv[2])};
+  auto* I = solver.impl_;
+  Dump d(argv[3]);
+  d.scalar("numNodes", I->numNodes);
+  d.scalar("regTotal", (int64_t)I->regTotal);
+  d.scalar("totalIterations", (int64_t)solver.totalIters_);
+  d.raw("regret", 'f', sizeof(float), I->dRegret, I->regTotal);
+  d.raw("strat", 'f', sizeof(float), I->dStrat, I->regTotal);
+  int counter = 0;
+  std::memcpy(&counter, I->dCounter, sizeof(int));
+  d.scalar("counter", counter);
+  return 0;
+}
+
 // `ref_capture --treebuf`: the reference kernels' argument block, TreeBuf
 // (cuda/gpu_cfr.cu:132-201), as "name offset" lines plus "sizeof N".
 int printTreeBuf() {
@@ -166,6 +229,8 @@ int printTreeBuf() {
 
 int main(int argc, char** argv) {
   if (argc == 2 && std::strcmp(argv[1], "--treebuf") == 0) return printTreeBuf();
+  if (argc >= 2 && std::strcmp(argv[1], "--save") == 0) return saveMode(argc, argv);
+  if (argc >= 2 && std::strcmp(argv[1], "--load") == 0) return loadMode(argc, argv);
   if (argc != 10) {
     std::fprintf(stderr,
                  "usage: ref_capture <out.bin> <board> <oop> <ip> <pot> "

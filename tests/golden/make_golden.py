@@ -18,6 +18,10 @@ Fixtures:
   ref_treebuf.json    byte offset of every TreeBuf member (the argument
                       block of the reference kernels, cuda/gpu_cfr.cu:
                       132-201) and its size, as compiled from the source
+  ref_solution_v1.pps a "PPS1" version-1 solution file written by the
+                      reference's own save() (cuda/gpu_cfr.cu:2743-2785) for
+                      a small river spot, rows set to a fixed pattern, with
+                      ref_solution_v1.json (the spot, sizes, sha256)
 """
 from __future__ import annotations
 
@@ -34,6 +38,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 REF_BIN = os.path.join(REPO, "oracle", "_ref")
+# The reference checkout: PPS_REFERENCE, else `reference` beside this repository.
+REF_SRC = os.environ.get("PPS_REFERENCE") or os.path.join(os.path.dirname(REPO), "reference")
 sys.path.insert(0, os.path.join(REPO, "cuda-poker-solver_gb300"))
 from pps import workloads as wl  # noqa: E402
 
@@ -114,8 +120,7 @@ def treebuf_layout():
 
 def api_routes():
     import re
-    src = open(os.path.join(os.environ.get("PPS_REFERENCE", "/root/reference"),
-                            "python", "pps_api.py")).read()
+    src = open(os.path.join(REF_SRC, "python", "pps_api.py")).read()
     routes = sorted({(m.upper(), p) for m, p, rest in
                      re.findall(r'@app\.(get|post|delete|put)\("([^"]+)"([^)]*)\)', src)
                      if "include_in_schema=False" not in rest})
@@ -123,9 +128,36 @@ def api_routes():
               indent=0)
 
 
+# The solution-file golden: a small river spot saved by the reference's own
+# save() with rows set to ref_capture's fixed pattern.
+SOLUTION_SPOT = {"board": "Qs9h2d7c5d", "oop": "TT+,AKo", "ip": "AQ+,KQs", "pot": 200,
+                 "stack": 500, "bets": "0.75,a", "raises": "2.5,3", "max_raises": 0,
+                 "iterations": 300}
+
+
+def solution_file():
+    sp = SOLUTION_SPOT
+    path = os.path.join(HERE, "ref_solution_v1.pps")
+    subprocess.run([os.path.join(REF_BIN, "ref_capture"), "--save", path, str(sp["iterations"]),
+                    sp["board"], sp["oop"], sp["ip"], str(sp["pot"]), str(sp["stack"]),
+                    sp["bets"], sp["raises"], str(sp["max_raises"])], check=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "load.bin")
+        subprocess.run([os.path.join(REF_BIN, "ref_capture"), "--load", path, out], check=True)
+        d = read_dump(out)
+    meta = dict(sp)
+    meta.update({"num_nodes": int(d["numNodes"][0]), "reg_total": int(d["regTotal"][0]),
+                 "sha256": hashlib.sha256(open(path, "rb").read()).hexdigest()})
+    json.dump(meta, open(os.path.join(HERE, "ref_solution_v1.json"), "w"), indent=1)
+    print("solution file", meta["num_nodes"], "nodes,", meta["reg_total"], "rows")
+
+
 def main():
     if sys.argv[1:] == ["--api-routes"]:
         api_routes()
+        return
+    if sys.argv[1:] == ["--solution-file"]:
+        solution_file()
         return
     if not os.path.exists(os.path.join(REF_BIN, "ref_capture")):
         raise SystemExit("build the reference tools first: sh oracle/ref/build_ref.sh")
