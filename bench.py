@@ -343,12 +343,43 @@ def served_bench(spots, lam, count, seed=7):
             "saturated": bool(rate < 0.9 * lam)}
 
 
+def _workloads():
+    """pps/workloads.py (the synthetic spot definitions; standard library
+    only) loaded by its path, so that the reference arm never imports the
+    product package or maps its library."""
+    import importlib.util
+    name = "spot_workloads"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, os.path.join(PKG, "pps", "workloads.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _reference_weights(r):
+    """1326 combo weights of a spot side: a list as given, or a range string
+    as the reference's own parser read it (tests/golden/ranges.json, written
+    by the reference's parseRange)."""
+    import numpy as np
+    if not isinstance(r, str):
+        return np.asarray(r, dtype=np.float64)
+    table = json.load(open(os.path.join(REPO, "tests", "golden", "ranges.json")))
+    if table.get(r) is None:
+        raise KeyError("no reference parse of range %r" % r)
+    return np.asarray(table[r], dtype=np.float64)
+
+
 def reference_kernels(steps, warmup):
     """The reference's own GPU kernels (cuda/gpu_cfr.cu compiled from its
     source for sm_103a, oracle/ref/ref_gpu.cpp's host runner: the
     reference's layout, graph and launch sequence) timed on this GPU with
-    CUDA events over graph replays, per spot."""
+    CUDA events over graph replays, per spot. Their input is the
+    reference's layout as the oracle restates it (bit-exact against the
+    reference's init()); no product code runs in this arm."""
     from oracle import ref_gpu
+    from oracle import cpu_oracle as co
     if not ref_gpu.fatbin_present():
         return {"unavailable": "oracle/_ref/gpu_cfr_kernels.fatbin not built (the reference "
                                "sources are needed to build it)"}
@@ -358,14 +389,16 @@ def reference_kernels(steps, warmup):
             return {"unavailable": "no GPU"}
     except ImportError:
         return {"unavailable": "no torch"}
-    from pps import pps_native as pn
-    from pps import workloads as wl
+    wl = _workloads()
     out = {"unit": "iters/s", "kind": "reference kernels on this GPU",
-           "method": "CUDA events over graph replays after warm-up"}
+           "method": "CUDA events over graph replays after warm-up",
+           "input": "the reference's layout restated by the oracle (bit-exact against the "
+                    "reference's init()); no product code in this arm"}
     for name in ("turn_c3", "turn_w52", "flop_164k"):
         spot = wl.NAMED[name]()
-        cfg = pn.bet_config(spot.cfg.bet_text(), spot.cfg.raise_text(), spot.cfg.max_raises)
-        exp = pn.compile_export(spot.board, spot.oop, spot.ip, spot.pot, spot.stack, [cfg])
+        exp = co.reference_layout(spot.board, _reference_weights(spot.oop),
+                                  _reference_weights(spot.ip), spot.pot, spot.stack,
+                                  co.cfg_from(spot.cfg))
         r = ref_gpu.RefKernels(exp, spot.pot)
         n = max(1, min(steps, 300))
         ms = r.ms_per_iteration(max(3, warmup), n)
@@ -382,7 +415,7 @@ def run_reference(args, rank):
     reference's own GPU kernels on the same GPU."""
     if rank != 0:
         return
-    from pps import workloads as wl
+    wl = _workloads()
     from oracle.cpu_oracle import oracle_for
     spot = wl.turn_c3()
     threads = os.cpu_count() or 1

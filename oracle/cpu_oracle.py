@@ -11,6 +11,7 @@ import os
 import subprocess
 
 import numpy as np
+from typing import Dict
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
@@ -32,6 +33,10 @@ def build() -> str:
 
 
 _lib = None
+
+
+EXPORT_CB = C.CFUNCTYPE(None, C.c_void_p, C.c_char_p, C.c_char, C.c_void_p, C.c_int64)
+_DT = {b"i": np.int32, b"q": np.int64, b"B": np.uint8, b"f": np.float32, b"d": np.float64}
 
 
 def lib():
@@ -61,6 +66,7 @@ def lib():
         L.orc_actions.argtypes = [C.c_int64, C.c_int64, C.POINTER(OrcCfg), C.c_int64, C.c_int64,
                                   C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
                                   C.POINTER(C.c_int64)]
+        L.orc_export.argtypes = [C.c_void_p, EXPORT_CB, C.c_void_p]
         _lib = L
     return _lib
 
@@ -143,6 +149,25 @@ class Oracle:
     def set_rows(self, which, rows):
         a = np.ascontiguousarray(rows, dtype=np.float32)
         lib().orc_set_rows(self.h, int(which), a.ctypes.data_as(C.POINTER(C.c_float)))
+
+
+def reference_layout(board, w0, w1, pot, stack, cfg) -> Dict[str, np.ndarray]:
+    """The reference's device layout of a spot (the arrays its init()
+    uploads, cuda/gpu_cfr.cu:1363-1827), restated by the oracle from its own
+    tree: what the reference's kernels run on (oracle/ref_gpu.py). One bet
+    config for every street, as in the reference. w0 / w1: 1326 weights."""
+    o = Oracle(board, w0, w1, pot, stack, [cfg], 32, 1)
+    out: Dict[str, np.ndarray] = {}
+
+    def sink(_user, name, dt, data, n):
+        t = _DT[dt]
+        a = np.ctypeslib.as_array(C.cast(data, C.POINTER(C.c_uint8)), (int(n) * np.dtype(t).itemsize,)) \
+            if n else np.zeros(0, dtype=np.uint8)
+        out[name.decode()] = a.view(t).copy()
+
+    cb = EXPORT_CB(sink)
+    lib().orc_export(o.h, cb, None)
+    return out
 
 
 def oracle_for(spot, threads=None, precision=32, parse_range=None):

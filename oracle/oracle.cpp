@@ -221,6 +221,7 @@ struct ONode {
   std::vector<int> dealt; // chance: card per branch
   int64_t rowOff = -1;    // decide: offset in the dense row table
   int na = 0;
+  int actBase = 0;        // decide: first action in Spot::acts
 };
 
 struct Spot {
@@ -229,6 +230,7 @@ struct Spot {
   int64_t pot = 0, stack = 0;
   Cfg cfg[3];
   std::vector<ONode> nodes;
+  std::vector<Act> acts;  // every decide node's actions, in node order
   int64_t rowTotal = 0;
   int nBoard0 = 0;
 
@@ -295,6 +297,8 @@ struct Spot {
     nodes[id].kind = kDecide;
     nodes[id].player = actor;
     nodes[id].na = (int)acts.size();
+    nodes[id].actBase = (int)this->acts.size();
+    this->acts.insert(this->acts.end(), acts.begin(), acts.end());
     for (const Act& a : acts) {
       int64_t n0 = sc0, n1 = sc1;
       bool after = afterAllin, ends = false;
@@ -633,6 +637,378 @@ double pairMass(const Spot& sp) {
   return Z;
 }
 
+// ---------------------------------------------------------------------------
+// The reference's device layout, restated from this file's tree: the
+// arrays GpuPostflopSolver's init() uploads (cuda/gpu_cfr.cu:1363-1827),
+// under the names of its TreeBuf / Impl members, so that the reference's
+// own kernels can run a spot with no product code in the path. The tests
+// pin every array against the reference's init() run on a host CUDA stub.
+// ---------------------------------------------------------------------------
+
+using Sink = void (*)(void* user, const char* name, char dtype, const void* data, int64_t n);
+
+struct RefExport {
+  const Spot& sp;
+  Sink sink;
+  void* user;
+  std::vector<int> comboOff[2], comboId, runOffOff, runOff, ctapBase, ctap, expOffOff,
+      expIdxBase, expOff, expIdx;
+
+  void ints(const char* name, const std::vector<int>& v) { sink(user, name, 'i', v.data(), (int64_t)v.size()); }
+  void longs(const char* name, const std::vector<int64_t>& v) {
+    sink(user, name, 'q', v.data(), (int64_t)v.size());
+  }
+  void scalar(const char* name, int64_t v) { sink(user, name, 'q', &v, 1); }
+
+  // Node-local slot in the parent's list of each child-list entry.
+  static std::vector<int> parentSlots(const std::vector<int>& parent, const std::vector<int>& child) {
+    std::vector<int> out;
+    size_t i = 0;
+    for (int b : child) {
+      while (parent[i] != b) ++i;
+      out.push_back((int)i);
+    }
+    return out;
+  }
+
+  // Combo lists and chance maps in the order the reference's recursion
+  // appends them (cuda/gpu_cfr.cu:1197-1245): a chance node reserves its
+  // runOff section, appends each branch's child lists right before
+  // building that child, and writes its ctap / expOff / expIdx sections
+  // after all children.
+  void lists(int u, int off0, int off1) {
+    const ONode& n = sp.nodes[u];
+    comboOff[0][u] = off0;
+    comboOff[1][u] = off1;
+    if (n.kind != kChance) {
+      for (int k : n.kids) lists(k, off0, off1);
+      return;
+    }
+    const int nb = (int)n.kids.size();
+    runOffOff[u] = (int)runOff.size();
+    runOff.resize(runOff.size() + 2 * (nb + 1), 0);
+    for (int k : n.kids) {
+      const ONode& c = sp.nodes[k];
+      const int c0 = (int)comboId.size();
+      comboId.insert(comboId.end(), c.list[0]->begin(), c.list[0]->end());
+      const int c1 = (int)comboId.size();
+      comboId.insert(comboId.end(), c.list[1]->begin(), c.list[1]->end());
+      lists(k, c0, c1);
+    }
+    ctapBase[u] = (int)ctap.size();
+    for (int p = 0; p < 2; ++p) {
+      const int base = runOffOff[u] + p * (nb + 1);
+      int total = 0;
+      for (int br = 0; br < nb; ++br) {
+        runOff[base + br] = total;
+        for (int j : parentSlots(*n.list[p], *sp.nodes[n.kids[br]].list[p])) {
+          ctap.push_back(j);
+          ++total;
+        }
+      }
+      runOff[base + nb] = total;
+    }
+    expOffOff[u] = (int)expOff.size();
+    expIdxBase[u] = (int)expIdx.size();
+    for (int p = 0; p < 2; ++p) {
+      std::vector<std::vector<int>> perSlot(n.list[p]->size());
+      for (int br = 0; br < nb; ++br) {
+        const auto par = parentSlots(*n.list[p], *sp.nodes[n.kids[br]].list[p]);
+        for (int j = 0; j < (int)par.size(); ++j) perSlot[par[j]].push_back(br * 4096 + j);
+      }
+      int cnt = 0;
+      for (const auto& v : perSlot) {
+        expOff.push_back(cnt);
+        expIdx.insert(expIdx.end(), v.begin(), v.end());
+        cnt += (int)v.size();
+      }
+      expOff.push_back(cnt);
+    }
+  }
+
+  void run() {
+    const int N = (int)sp.nodes.size();
+    std::vector<int> parent(N, -1), depth(N, 0);
+    for (int u = 0; u < N; ++u)
+      for (int k : sp.nodes[u].kids) {
+        parent[k] = u;
+        depth[k] = depth[u] + 1;
+      }
+    int maxDepth = 0, maxNa = 0;
+    for (int u = 0; u < N; ++u) {
+      maxDepth = std::max(maxDepth, depth[u]);
+      maxNa = std::max(maxNa, sp.nodes[u].na);
+    }
+    const int n0 = (int)sp.side[0].size(), n1 = (int)sp.side[1].size();
+    scalar("numNodes", N);
+    scalar("maxDepth", maxDepth);
+    scalar("n0Base", n0);
+    scalar("n1Base", n1);
+    scalar("maxNa", maxNa);
+    scalar("regTotal", sp.rowTotal);
+
+    for (int p = 0; p < 2; ++p) comboOff[p].assign(N, 0);
+    runOffOff.assign(N, 0);
+    ctapBase.assign(N, 0);
+    expOffOff.assign(N, 0);
+    expIdxBase.assign(N, 0);
+    for (int p = 0; p < 2; ++p)
+      for (int i = 0; i < (int)sp.side[p].size(); ++i) comboId.push_back(i);
+    lists(0, 0, n0);
+
+    std::vector<int> kind(N), player(N), foldBy(N), na(N), childBase(N), childFlat, boardId(N, 0),
+        nC0(N), nC1(N), regOff(N, 0), cfvOff(N), reachOff0(N), reachOff1(N), nBranch(N),
+        chanceQ(N);
+    std::vector<int64_t> sc0(N), sc1(N), potBase(N), pc0(N), pc1(N);
+    std::vector<uint8_t> nodeBoard((size_t)N * 5, 0);
+    std::vector<std::vector<int>> boards;  // showdown boards, first seen
+    std::vector<int> boardNode;
+    int64_t reachTotal = 0, reachTotal0 = 0, reachTotal1 = 0, regTotal = 0;
+    for (int u = 0; u < N; ++u) {
+      const ONode& n = sp.nodes[u];
+      kind[u] = n.kind;
+      player[u] = n.kind == kDecide ? n.player : 0;
+      foldBy[u] = n.kind == kFoldN ? n.foldBy : 0;
+      na[u] = n.kind == kDecide ? n.na : 0;
+      childBase[u] = (int)childFlat.size();
+      childFlat.insert(childFlat.end(), n.kids.begin(), n.kids.end());
+      nC0[u] = (int)n.list[0]->size();
+      nC1[u] = (int)n.list[1]->size();
+      sc0[u] = n.sc0;
+      sc1[u] = n.sc1;
+      potBase[u] = n.potBase;
+      pc0[u] = n.pc0;
+      pc1[u] = n.pc1;
+      nBranch[u] = n.kind == kChance ? (int)n.kids.size() : 0;
+      chanceQ[u] = 52 - n.nBoard - 4;
+      for (int i = 0; i < n.nBoard; ++i) nodeBoard[(size_t)u * 5 + i] = (uint8_t)n.board[i];
+      if (n.kind == kShow) {
+        const std::vector<int> key(n.board, n.board + 5);
+        int id = -1;
+        for (size_t b = 0; b < boards.size(); ++b)
+          if (boards[b] == key) id = (int)b;
+        if (id < 0) {
+          id = (int)boards.size();
+          boards.push_back(key);
+          boardNode.push_back(u);
+        }
+        boardId[u] = id;
+      }
+      const int row = std::max(nC0[u], nC1[u]);
+      cfvOff[u] = (int)reachTotal;
+      reachTotal += row;
+      if (n.kind == kDecide) {
+        regOff[u] = (int)regTotal;
+        regTotal += (int64_t)n.na * (n.player == 0 ? nC0[u] : nC1[u]);
+      }
+      // Rows under a decide node of the layout's traverser alias the
+      // parent's row (cuda/gpu_cfr.cu:1491-1514).
+      const int par = parent[u];
+      const bool parDecide = par >= 0 && sp.nodes[par].kind == kDecide;
+      if (parDecide && sp.nodes[par].player == 0) reachOff0[u] = reachOff0[par];
+      else { reachOff0[u] = (int)reachTotal0; reachTotal0 += row; }
+      if (parDecide && sp.nodes[par].player == 1) reachOff1[u] = reachOff1[par];
+      else { reachOff1[u] = (int)reachTotal1; reachTotal1 += row; }
+    }
+    scalar("reachTotal", reachTotal);
+    scalar("reachTotal0", reachTotal0);
+    scalar("reachTotal1", reachTotal1);
+    scalar("empty", 0);
+    ints("kind", kind);
+    ints("player", player);
+    ints("foldBy", foldBy);
+    ints("na", na);
+    ints("childBase", childBase);
+    ints("childFlat", childFlat);
+    ints("boardId", boardId);
+    ints("nC0", nC0);
+    ints("nC1", nC1);
+    ints("comboOff0", comboOff[0]);
+    ints("comboOff1", comboOff[1]);
+    ints("comboId", comboId);
+    ints("reachOff0", reachOff0);
+    ints("reachOff1", reachOff1);
+    ints("cfvOff", cfvOff);
+    ints("regOff", regOff);
+    longs("sc0", sc0);
+    longs("sc1", sc1);
+    longs("potBase", potBase);
+    longs("pc0", pc0);
+    longs("pc1", pc1);
+    ints("nBranch", nBranch);
+    ints("chanceQ", chanceQ);
+    ints("runOffOff", runOffOff);
+    ints("runOff", runOff);
+    ints("ctapBase", ctapBase);
+    ints("ctap", ctap);
+    ints("expOffOff", expOffOff);
+    ints("expIdxBase", expIdxBase);
+    ints("expOff", expOff);
+    ints("expIdx", expIdx);
+    for (int p = 0; p < 2; ++p) {
+      std::vector<float> wf;
+      std::vector<uint8_t> cards;
+      for (const Combo& c : sp.side[p]) {
+        wf.push_back((float)c.w);
+        cards.push_back((uint8_t)c.a);
+        cards.push_back((uint8_t)c.b);
+      }
+      sink(user, p == 0 ? "w0" : "w1", 'f', wf.data(), (int64_t)wf.size());
+      sink(user, p == 0 ? "cards0" : "cards1", 'B', cards.data(), (int64_t)cards.size());
+      ints(p == 0 ? "sameOther0" : "sameOther1", sp.same[p]);
+    }
+
+    // Strength tables per (showdown board, traverser) over the full base
+    // lists (cuda/gpu_cfr.cu:1594-1703): opponent combos stable-sorted by
+    // strength, less / tie ends per traverser combo, the sorted positions
+    // holding each card, and sorted position -> the board's node-local slot.
+    const int nTables = (int)boards.size() * 2;
+    std::vector<int> oppSortedOff(nTables + 1, 0), oppSorted, lessOff(nTables + 1, 0), lessEnd,
+        tieEnd, cardPosOff(nTables * 53 + 1, 0), cardPosIdx, revSortedOff(nTables + 1, 0),
+        revSorted;
+    for (int bid = 0; bid < (int)boards.size(); ++bid) {
+      const ONode& bn = sp.nodes[boardNode[bid]];
+      std::vector<uint64_t> key[2];
+      for (int p = 0; p < 2; ++p)
+        for (const Combo& c : sp.side[p]) {
+          const int seven[7] = {c.a, c.b, bn.board[0], bn.board[1], bn.board[2], bn.board[3],
+                                bn.board[4]};
+          key[p].push_back(strength7(seven));
+        }
+      for (int tr = 0; tr < 2; ++tr) {
+        const int ti = bid * 2 + tr, opp = 1 - tr;
+        const int no = (int)sp.side[opp].size();
+        std::vector<int> ord(no);
+        for (int i = 0; i < no; ++i) ord[i] = i;
+        std::stable_sort(ord.begin(), ord.end(),
+                         [&](int x, int y) { return key[opp][x] < key[opp][y]; });
+        oppSortedOff[ti] = (int)oppSorted.size();
+        oppSorted.insert(oppSorted.end(), ord.begin(), ord.end());
+        std::vector<int> local(no, -1);
+        const std::vector<int>& lo = *bn.list[opp];
+        for (size_t j = 0; j < lo.size(); ++j) local[lo[j]] = (int)j;
+        revSortedOff[ti] = (int)revSorted.size();
+        for (int k = 0; k < no; ++k) revSorted.push_back(local[ord[k]]);
+        lessOff[ti] = (int)lessEnd.size();
+        for (size_t i = 0; i < sp.side[tr].size(); ++i) {
+          const uint64_t v = key[tr][i];
+          int lo2 = 0, hi2 = no;
+          while (lo2 < hi2) {  // first position not weaker
+            const int m = (lo2 + hi2) / 2;
+            if (key[opp][ord[m]] < v) lo2 = m + 1; else hi2 = m;
+          }
+          int lo3 = lo2, hi3 = no;
+          while (lo3 < hi3) {  // first position stronger
+            const int m = (lo3 + hi3) / 2;
+            if (key[opp][ord[m]] <= v) lo3 = m + 1; else hi3 = m;
+          }
+          lessEnd.push_back(lo2);
+          tieEnd.push_back(lo3);
+        }
+        const int cpo = ti * 53;
+        cardPosOff[cpo] = (int)cardPosIdx.size();
+        for (int c = 0; c < 52; ++c) {
+          cardPosOff[cpo + c + 1] = cardPosOff[cpo + c];
+          for (int pos = 0; pos < no; ++pos) {
+            const Combo& cb = sp.side[opp][ord[pos]];
+            if (cb.a == c || cb.b == c) {
+              cardPosIdx.push_back(pos);
+              ++cardPosOff[cpo + c + 1];
+            }
+          }
+        }
+      }
+    }
+    ints("brOppSortedOff", oppSortedOff);
+    ints("brOppSorted", oppSorted);
+    ints("brLessOff", lessOff);
+    ints("brLessEnd", lessEnd);
+    ints("brTieEnd", tieEnd);
+    ints("brCardPosOff", cardPosOff);
+    ints("brCardPosIdx", cardPosIdx);
+    ints("brRevSortedOff", revSortedOff);
+    ints("brRevSorted", revSorted);
+
+    // Fold nodes: per traverser combo, the node-local slot of the identical
+    // combo in the opponent's list (cuda/gpu_cfr.cu:1754-1786).
+    std::vector<int> foldSonOff(N, 0), foldSon;
+    for (int u = 0; u < N; ++u) {
+      const ONode& n = sp.nodes[u];
+      if (n.kind != kFoldN) continue;
+      foldSonOff[u] = (int)foldSon.size();
+      for (int p = 0; p < 2; ++p) {
+        std::vector<int> local(sp.side[1 - p].size(), -1);
+        const std::vector<int>& lo = *n.list[1 - p];
+        for (size_t j = 0; j < lo.size(); ++j) local[lo[j]] = (int)j;
+        for (int b : *n.list[p]) {
+          const int so = sp.same[p][b];
+          foldSon.push_back(so >= 0 ? local[so] : -1);
+        }
+      }
+    }
+    ints("foldSonOff", foldSonOff);
+    ints("foldSon", foldSon);
+    std::vector<double> wd[2];
+    for (int p = 0; p < 2; ++p)
+      for (const Combo& c : sp.side[p]) wd[p].push_back(c.w);
+    sink(user, "w0d", 'd', wd[0].data(), (int64_t)wd[0].size());
+    sink(user, "w1d", 'd', wd[1].data(), (int64_t)wd[1].size());
+    sink(user, "nodeBoard", 'B', nodeBoard.data(), (int64_t)nodeBoard.size());
+
+    // Per-depth node lists and chance-branch prefixes (cuda/gpu_cfr.cu:1377-1421).
+    const int D = maxDepth + 1;
+    std::vector<int> decideCount(D, 0), chanceCount(D, 0), bwdCount(D, 0), chanceBrTotal(D, 0),
+        decideList, chanceList, bwdList, chanceBrOff;
+    std::vector<std::vector<int>> dl(D), cl(D), bl(D);
+    for (int u = 0; u < N; ++u) {
+      bl[depth[u]].push_back(u);
+      if (sp.nodes[u].kind == kDecide) dl[depth[u]].push_back(u);
+      if (sp.nodes[u].kind == kChance) cl[depth[u]].push_back(u);
+    }
+    for (int d = 0; d < D; ++d) {
+      decideCount[d] = (int)dl[d].size();
+      chanceCount[d] = (int)cl[d].size();
+      bwdCount[d] = (int)bl[d].size();
+      decideList.insert(decideList.end(), dl[d].begin(), dl[d].end());
+      chanceList.insert(chanceList.end(), cl[d].begin(), cl[d].end());
+      bwdList.insert(bwdList.end(), bl[d].begin(), bl[d].end());
+      int acc = 0;
+      chanceBrOff.push_back(0);
+      for (int u : cl[d]) {
+        acc += (int)sp.nodes[u].kids.size();
+        chanceBrOff.push_back(acc);
+      }
+      chanceBrTotal[d] = acc;
+    }
+    ints("decideCount", decideCount);
+    ints("chanceCount", chanceCount);
+    ints("bwdCount", bwdCount);
+    ints("chanceBrTotal", chanceBrTotal);
+    ints("decideList", decideList);
+    ints("chanceList", chanceList);
+    ints("bwdList", bwdList);
+    ints("chanceBrOff", chanceBrOff);
+
+    std::vector<int> meta;
+    for (int u = 0; u < N; ++u) {
+      const ONode& n = sp.nodes[u];
+      if (n.kind != kDecide) continue;
+      const int row[8] = {regOff[u], n.na, n.player, n.player == 0 ? nC0[u] : nC1[u],
+                          depth[u], n.nBoard, u, n.actBase};
+      meta.insert(meta.end(), row, row + 8);
+    }
+    ints("decideMeta", meta);
+    std::vector<uint8_t> actKind;
+    std::vector<int64_t> actAmount;
+    for (const Act& a : sp.acts) {
+      actKind.push_back((uint8_t)a.kind);
+      actAmount.push_back(a.amt);
+    }
+    sink(user, "actKind", 'B', actKind.data(), (int64_t)actKind.size());
+    longs("actAmount", actAmount);
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -721,6 +1097,12 @@ void* orc_create(const uint8_t* board, int nBoard, const double* w0, const doubl
 }
 
 void orc_destroy(void* p) { delete (Handle*)p; }
+
+// The reference's device layout of the spot (RefExport), array by array.
+void orc_export(void* p, Sink sink, void* user) {
+  RefExport e{((Handle*)p)->spot(), sink, user};
+  e.run();
+}
 int orc_num_nodes(void* p) { return (int)((Handle*)p)->spot().nodes.size(); }
 int64_t orc_row_total(void* p) { return ((Handle*)p)->spot().rowTotal; }
 

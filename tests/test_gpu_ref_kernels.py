@@ -6,11 +6,11 @@ the reference's rows and solutions on the same inputs."""
 import numpy as np
 import pytest
 
-from pps import pps_native as pn
 from pps import workloads as wl
+from oracle import cpu_oracle as co
 from oracle import ref_gpu
 
-from helpers import abi_cfgs, oracle, solver
+from helpers import oracle, solver, weights
 
 pytestmark = [
     pytest.mark.gpu,
@@ -21,8 +21,11 @@ pytestmark = [
 
 
 def reference(spot):
-    exp = pn.compile_export(spot.board, spot.oop, spot.ip, spot.pot, spot.stack,
-                            abi_cfgs(spot))
+    """The reference's kernels on the reference's layout of the spot, as the
+    oracle restates it (bit-exact against the reference's init(), pinned in
+    tests/test_oracle_golden.py): no product code builds their input."""
+    exp = co.reference_layout(spot.board, weights(spot.oop), weights(spot.ip), spot.pot,
+                              spot.stack, co.cfg_from(spot.cfg))
     return ref_gpu.RefKernels(exp, spot.pot)
 
 

@@ -67,3 +67,33 @@ def test_oracle_river_converges():
     rows[rows.size // 3: 2 * rows.size // 3] += 5.0
     o.set_rows(1, rows)
     assert o.stats(spot.pot)["exploitability"] > 10 * st["exploitability"]
+
+
+def _layout(spot):
+    from helpers import weights
+    return co.reference_layout(spot.board, weights(spot.oop), weights(spot.ip), spot.pot,
+                               spot.stack, co.cfg_from(spot.cfg))
+
+
+@pytest.mark.parametrize("name", ["river_c1", "turn_api", "turn_tiny", "turn_short",
+                                  "flop_short", "river_geo"])
+def test_reference_layout_bit_exact_small(golden_dir, name):
+    """The oracle's restatement of the reference's device layout (the input
+    of the reference's kernels) equals the reference's own init() arrays,
+    every one bit for bit."""
+    ref = dict(np.load(os.path.join(golden_dir, "ref_%s.npz" % name)))
+    mine = _layout(wl.NAMED[name]())
+    assert sorted(ref) == sorted(mine)
+    for k, v in ref.items():
+        assert mine[k].dtype == v.dtype and np.array_equal(mine[k], v), k
+
+
+@pytest.mark.parametrize("name", ["turn_w52", "turn_c3", "turn_c2_uniform", "flop_small"])
+def test_reference_layout_bit_exact_large(golden_dir, name):
+    import hashlib
+    hashes = json.load(open(os.path.join(golden_dir, "ref_hashes.json")))[name]
+    mine = _layout(wl.NAMED[name]())
+    assert sorted(hashes) == sorted(mine)
+    for k, (digest, size) in hashes.items():
+        a = np.ascontiguousarray(mine[k])
+        assert a.size == size and hashlib.sha256(a.tobytes()).hexdigest() == digest, k
