@@ -570,6 +570,16 @@ def main():
             "gpu_launches": int(info.launches_per_iteration) * args.steps,
             "engine": "terminal groups + decide records" if info.engine == 0 else
                       "per-node terminals"}
+    # The timed value uses the reference's plain f32 cumulative-strategy
+    # sums; the compensated (two-float) form is timed beside it.
+    sc = make()
+    sc.set_compensated(True)
+    sc.time_iterations(args.warmup)
+    n_comp = max(min(args.steps, 1000), 100)
+    line["strategy_sums"] = {"timed": "plain f32 (the reference's update)",
+                             "compensated": {"value": n_comp / (sc.time_iterations(n_comp) / 1000.0),
+                                             "unit": "iters/s", "iterations": n_comp}}
+    del sc
     # The reference's own published spot (tools/quality/bench_turn.sh:40-41,
     # 51,903 nodes; ~747-807 it/s on an RTX 4070, docs/STATUS.md:69).
     w52 = wl.turn_w52()
