@@ -462,7 +462,7 @@ __device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, in
     const ShowdownInfo f = fs[j];
     const int le = f.x & 0xffff, te = f.x >> 16;
     const int len1 = f.y & 0xff, len2 = (f.y >> 8) & 0xff;
-    const int a1 = f.w & 0xffff, a2 = f.w >> 16;
+    const int a1 = f.w & 0xfff, a2 = (f.w >> 16) & 0xfff;
     const T x1le = ws.X[a1 + ((f.y >> 16) & 0xff)], x1te = ws.X[a1 + (f.y >> 24)];
     const T x2le = ws.X[a2 + (f.z & 0xff)], x2te = ws.X[a2 + ((f.z >> 8) & 0xff)];
     const int same = (int)(f.z >> 16) - 1;

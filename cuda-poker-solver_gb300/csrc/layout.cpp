@@ -116,7 +116,11 @@ void buildStateParts(const Tree& t, int s, StateParts& P) {
       return keyBase[opp][ol[a]] < keyBase[opp][ol[b]];
     });
     std::vector<uint64_t> sortedKey(no);
-    for (int k = 0; k < no; ++k) sortedKey[k] = keyBase[opp][ol[ord[k]]];
+    std::vector<int> posOfSlot(no);  // opponent slot -> sorted position
+    for (int k = 0; k < no; ++k) {
+      sortedKey[k] = keyBase[opp][ol[ord[k]]];
+      posOfSlot[ord[k]] = k;
+    }
     std::vector<int>& segStart = P.segStart[tr];
     std::vector<int>& segSlot = P.segSlot[tr];
     segStart.assign(53, 0);
@@ -147,13 +151,24 @@ void buildStateParts(const Tree& t, int s, StateParts& P) {
       const int so = t.side[tr].sameOther[b];
       const int same = so >= 0 ? slotOf(ol, so) : -1;
       const int len1 = (int)posOfCard[c1].size(), len2 = (int)posOfCard[c2].size();
+      // The identical combo's entry in card c1's segment (it holds c1), plus
+      // one; 0: none.
+      int ks1 = 0;
+      if (same >= 0) {
+        const auto& v = posOfCard[c1];
+        ks1 = (int)(std::lower_bound(v.begin(), v.end(), posOfSlot[same]) - v.begin()) + 1;
+      }
+      const int a1 = segStart[c1] + c1, a2 = segStart[c2] + c2;
+      if (a1 >= 4096 || a2 >= 4096 || ks1 >= 64)
+        throw Error{PPS_GB_E_FORMAT, "showdown table entry out of range"};
       ShowdownInfo info;
       info.x = (uint32_t)le | ((uint32_t)te << 16);
       info.y = (uint32_t)len1 | ((uint32_t)len2 << 8) | ((uint32_t)below(c1, le) << 16) |
                ((uint32_t)below(c1, te) << 24);
       info.z = (uint32_t)below(c2, le) | ((uint32_t)below(c2, te) << 8) |
                ((uint32_t)(same + 1) << 16);
-      info.w = (uint32_t)(segStart[c1] + c1) | ((uint32_t)(segStart[c2] + c2) << 16);
+      info.w = (uint32_t)a1 | ((uint32_t)(ks1 & 15) << 12) | ((uint32_t)a2 << 16) |
+               ((uint32_t)(ks1 >> 4) << 28);
       P.info[tr].push_back(info);
     }
   }

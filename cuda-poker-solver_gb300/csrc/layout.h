@@ -77,10 +77,12 @@ struct alignas(16) StateDev {
 // Showdown entry of one traverser combo (cards c1, c2): x = le | te << 16
 // (opponents strictly weaker / weaker-or-equal, in sorted positions);
 // y = len1 | len2 << 8 | k1le << 16 | k1te << 24; z = k2le | k2te << 8 |
-// (same+1) << 16; w = a1 | a2 << 16. lenX is the length of card cX's
-// segment, kXle / kXte count its entries below le / te, aX = seg[cX] + cX
-// is where its prefix run starts in the kernels' segment scan, and `same`
-// is the opponent slot of the identical combo (-1: none).
+// (same+1) << 16; w = a1 | (s1 & 15) << 12 | a2 << 16 | (s1 >> 4) << 28.
+// lenX is the length of card cX's segment, kXle / kXte count its entries
+// below le / te, aX = seg[cX] + cX (< 4096) is where its prefix run starts
+// in the kernels' segment scan, `same` is the opponent slot of the
+// identical combo (-1: none) and s1 its entry in card c1's segment plus one
+// (0: none).
 struct alignas(16) ShowdownInfo {
   uint32_t x, y, z, w;
 };

@@ -27,11 +27,28 @@ namespace gb {
 constexpr int kTermThreads = 256;
 
 // ---- float4 lane arithmetic ----
+// Each float4 operation is two packed f32x2 instructions (sm_100+), the
+// lanes rounded exactly as four scalar operations would be; a - b is
+// fma(b, -1, a), which rounds once, as a subtraction does.
+__device__ __forceinline__ float2 lanesXY(float4 a) { return make_float2(a.x, a.y); }
+__device__ __forceinline__ float2 lanesZW(float4 a) { return make_float2(a.z, a.w); }
+__device__ __forceinline__ float4 lanes4(float2 xy, float2 zw) {
+  return make_float4(xy.x, xy.y, zw.x, zw.y);
+}
 __device__ __forceinline__ float4 operator+(float4 a, float4 b) {
-  return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+  return lanes4(__fadd2_rn(lanesXY(a), lanesXY(b)), __fadd2_rn(lanesZW(a), lanesZW(b)));
 }
 __device__ __forceinline__ float4 operator-(float4 a, float4 b) {
-  return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+  const float2 m1 = make_float2(-1.f, -1.f);
+  return lanes4(__ffma2_rn(lanesXY(b), m1, lanesXY(a)), __ffma2_rn(lanesZW(b), m1, lanesZW(a)));
+}
+// a * b + c per lane (one rounding).
+__device__ __forceinline__ float4 fma4(float4 a, float4 b, float4 c) {
+  return lanes4(__ffma2_rn(lanesXY(a), lanesXY(b), lanesXY(c)),
+                __ffma2_rn(lanesZW(a), lanesZW(b), lanesZW(c)));
+}
+__device__ __forceinline__ float4 mul4(float4 a, float4 b) {
+  return lanes4(__fmul2_rn(lanesXY(a), lanesXY(b)), __fmul2_rn(lanesZW(a), lanesZW(b)));
 }
 __device__ __forceinline__ float4& operator+=(float4& a, float4 b) { return a = a + b; }
 __device__ __forceinline__ float4 max0(float4 a) {
@@ -240,10 +257,6 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   const float4 TH = BH4[bn], TL = BL4[bn], Pno = P4[pad8(no)];
   float* out[4];
   outRows4(out, t, rows, u);
-  const float* rr[4];
-#pragma unroll
-  for (int g = 0; g < 4; ++g)
-    rr[g] = u[g] >= 0 ? rows.reach[tr] + (size_t)t.rows[u[g]].reachQ[tr] * 4 : nullptr;
   const int nt4 = quadsOf(nt) * 4;
 #pragma unroll 2
   for (int i = threadIdx.x; i < nt4; i += blockDim.x) {
@@ -254,15 +267,16 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
     const ShowdownInfo f = info[i];
     const int le = f.x & 0xffff, te = f.x >> 16;
     const int len1 = f.y & 0xff, len2 = (f.y >> 8) & 0xff;
-    const int a1 = f.w & 0xffff, a2 = f.w >> 16;
+    const int a1 = f.w & 0xfff, a2 = (f.w >> 16) & 0xfff;
+    const int s1 = ((f.w >> 12) & 15) | ((f.w >> 28) << 4);
     const float4 x1le = X4[pad8(a1 + ((f.y >> 16) & 0xff))], x1te = X4[pad8(a1 + (f.y >> 24))];
     const float4 x2le = X4[pad8(a2 + (f.z & 0xff))], x2te = X4[pad8(a2 + ((f.z >> 8) & 0xff))];
     const float4 x1end = X4[pad8(a1 + len1)], x2end = X4[pad8(a2 + len2)];
-    const int same = (int)(f.z >> 16) - 1;
+    // The identical combo's reach: its step in card c1's segment prefix
+    // (exact up to the rounding of that prefix, a few units in the last
+    // place of a sum of at most 51 entries).
     float4 sameR = zero4();
-    if (same >= 0)  // the identical combo's reach, from the (cached) rows
-      sameR = make_float4(rr[0] ? rr[0][same] : 0.f, rr[1] ? rr[1][same] : 0.f,
-                          rr[2] ? rr[2][same] : 0.f, rr[3] ? rr[3][same] : 0.f);
+    if (s1 > 0) sameR = X4[pad8(a1 + s1)] - X4[pad8(a1 + s1 - 1)];
     const int bl = le >> kSpanShift, bt = te >> kSpanShift;
     const float4 bhl = BH4[bl], bll = BL4[bl], bht = BH4[bt], blt = BL4[bt];
     const float4 ple = P4[pad8(le)], pte = P4[pad8(te)];
@@ -272,10 +286,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
     const float4 lm = max0(below - x1le - x2le);
     const float4 tm = max0(band - (x1te - x1le) - (x2te - x2le) + sameR);
     const float4 gm = max0(above - (x1end - x1te) - (x2end - x2te));
-    const float4 c = make_float4(lm.x * win4.x + tm.x * tie4.x + gm.x * lose4.x,
-                                 lm.y * win4.y + tm.y * tie4.y + gm.y * lose4.y,
-                                 lm.z * win4.z + tm.z * tie4.z + gm.z * lose4.z,
-                                 lm.w * win4.w + tm.w * tie4.w + gm.w * lose4.w);
+    const float4 c = fma4(gm, lose4, fma4(tm, tie4, mul4(lm, win4)));
     storeOut4(out, i, c);
   }
 }
@@ -347,7 +358,7 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
     float4 w = tot - cs4[cp & 0xff] - cs4[cp >> 8];
     if (sm >= 0) w += rs4[pad8(sm)];
     w = max0(w);
-    storeOut4(out, i, make_float4(w.x * v[0], w.y * v[1], w.z * v[2], w.w * v[3]));
+    storeOut4(out, i, mul4(w, make_float4(v[0], v[1], v[2], v[3])));
   }
 }
 
