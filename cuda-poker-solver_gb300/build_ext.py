@@ -26,7 +26,7 @@ INCLUDES = ["-I", os.path.join(REPO, "include", "pps"), "-I", os.path.join(REPO,
             "-I", CSRC]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["cards.cpp", "bet_tree.cpp", "compiler.cpp", "layout.cpp", "solver.cpp",
-               "capi.cpp", "gpu_cfr.cpp", "engine.cu", "rowcodec.cu", "noalloc.cu", "forest.cu", "batch.cpp"]
+               "capi.cpp", "gpu_cfr.cpp", "tune.cpp", "engine.cu", "rowcodec.cu", "noalloc.cu", "forest.cu", "batch.cpp"]
 
 
 def _nvcc():

@@ -453,6 +453,35 @@ int pps_gb_set_engine(pps_gb_solver* h, int engine) {
   });
 }
 
+int pps_gb_set_launch_shape(pps_gb_solver* h, const pps_gb_launch_shape* shape) {
+  return guarded([&] {
+    SolverCore& s = core(h);
+    if (!shape) throw Error{PPS_GB_E_ARG, "null argument"};
+    pps::gb::LaunchShape ls;
+    ls.plan = shape->plan;
+    ls.fwdCap = shape->fwd_cap;
+    ls.bwdCap = shape->bwd_cap;
+    ls.sdCap = shape->sd_cap;
+    ls.fdCap = shape->fd_cap;
+    if (s.engine()) s.engine()->setShape(ls);
+  });
+}
+
+int pps_gb_get_launch_shape(pps_gb_solver* h, pps_gb_launch_shape* out) {
+  return guarded([&] {
+    SolverCore& s = core(h);
+    if (!out) throw Error{PPS_GB_E_ARG, "null argument"};
+    std::memset(out, 0, sizeof(*out));
+    if (!s.engine()) return;
+    const pps::gb::LaunchShape ls = s.engine()->shape();
+    out->plan = ls.plan;
+    out->fwd_cap = ls.fwdCap;
+    out->bwd_cap = ls.bwdCap;
+    out->sd_cap = ls.sdCap;
+    out->fd_cap = ls.fdCap;
+  });
+}
+
 int pps_gb_set_compensated(pps_gb_solver* h, int on) {
   return guarded([&] {
     SolverCore& s = core(h);

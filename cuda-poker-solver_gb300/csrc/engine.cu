@@ -21,6 +21,7 @@
 #include "plan.cuh"
 #include "rowcodec.h"
 #include "terminal.cuh"
+#include "tune.h"
 #include "pps_gb.h"
 
 namespace pps {
@@ -76,6 +77,7 @@ struct Engine::Dev {
   StagedPlan staged;           // kind 0 as captured
   StagedEvents sev;
   bool walkReady = false;
+  LaunchShape shape;  // grids of the captured iteration (tune.h)
   int maxN = 0;
   size_t smemF = 0, smemD = 0;
 
@@ -101,7 +103,7 @@ V* upload(Engine::Dev& d, const std::vector<V>& v, size_t& bytes, int64_t& h2d) 
 
 PlanArgs planArgs(const Engine::Dev& d) {
   return PlanArgs{d.tree,   d.rowsF, d.tasks, d.counter, 1, d.maxN, d.smemF, d.groups,
-                  sdGroupSmem(d.maxN), fdGroupSmem(d.maxN), d.recs, d.recTasks};
+                  sdGroupSmem(d.maxN), fdGroupSmem(d.maxN), d.recs, d.recTasks, d.shape};
 }
 
 // Issues one planned launch (CFR mode, f32 rows) on stream s.
@@ -460,29 +462,95 @@ void Engine::setEngineKind(int kind) {
   const int k = kind == 1 || kind == 2 ? kind : 0;
   if (k == engineKind_ && d_->exec) return;
   engineKind_ = k;
+  d_->shape.plan = k == 2 ? 2 : 0;
   capture();
 }
 
+void Engine::setShape(const LaunchShape& s) {
+  if (s.plan != 0 && s.plan != 2) throw Error{PPS_GB_E_ARG, "launch shape: plan must be 0 or 2"};
+  if (s.plan == 2 && d_->plan[2].empty())
+    throw Error{PPS_GB_E_ARG, "engine 2 (fused levels) needs lists of at most " +
+                                  std::to_string(kFusedMaxN) + " combos"};
+  for (int c : {s.fwdCap, s.bwdCap, s.sdCap, s.fdCap})
+    if (c < 0 || c > 64) throw Error{PPS_GB_E_ARG, "launch shape: caps must be 0..64"};
+  tuned_ = true;
+  d_->shape = s;
+  engineKind_ = s.plan;
+  capture();
+}
+
+LaunchShape Engine::shape() const { return d_->shape; }
+
+// Times `shape` on this tree: capture, one warm-up replay, then `n` timed
+// replays from iteration 0 of the schedule (the counter is reset first, so
+// no replay reads past the table).
+double Engine::timeShape(const LaunchShape& s, int n) {
+  d_->shape = s;
+  engineKind_ = s.plan;
+  capture();
+  setCounter(0);
+  iterate(1);
+  return timeIterations(n) / n;
+}
+
+// Picks the launch shape of this tree: the cached one of its size class,
+// else the fastest candidate by timing, one knob at a time (plan, then the
+// showdown, fold, forward and backward grids), each candidate taking over
+// only when it is at least 1% faster. The choice is cached for the class;
+// the rows and the counter are zeroed afterwards (shapes compute identical
+// rows).
 void Engine::autotune() {
   if (tuned_) return;
   tuned_ = true;
-  if (d_->plan[2].empty()) return;
-  double best = 0.0;
-  int bestKind = 0;
-  for (int k : {0, 2}) {
-    engineKind_ = k;
+  const TuneKey key = tuneKeyOf(d_->maxN, (int64_t)L_.regQuads * 16);
+  LaunchShape cached;
+  if (lookupShape(key, &cached) && (cached.plan == 0 || !d_->plan[2].empty())) {
+    d_->shape = cached;
+    engineKind_ = cached.plan;
     capture();
-    iterate(2);  // warm-up
-    const double ms = timeIterations(6);
-    if (k == 0 || ms < best) {
-      best = ms;
-      bestKind = k;
+    return;
+  }
+  const int n = 4;
+  LaunchShape best = d_->shape;
+  best.plan = 0;
+  double bestMs = timeShape(best, n);
+  auto consider = [&](LaunchShape c) {
+    if (c == best) return;
+    const double ms = timeShape(c, n);
+    if (ms < 0.99 * bestMs) {
+      best = c;
+      bestMs = ms;
     }
+  };
+  if (!d_->plan[2].empty()) {
+    LaunchShape c = best;
+    c.plan = 2;
+    consider(c);
   }
-  if (bestKind != engineKind_) {
-    engineKind_ = bestKind;
+  if (best.plan == 0) {
+    for (int cap : {1, 2}) {
+      LaunchShape c = best;
+      c.sdCap = cap;
+      consider(c);
+    }
+    LaunchShape c = best;
+    c.fdCap = 3;
+    consider(c);
+  }
+  for (int cap : {16}) {
+    LaunchShape c = best;
+    c.fwdCap = cap;
+    consider(c);
+    c = best;
+    c.bwdCap = cap;
+    consider(c);
+  }
+  if (!(d_->shape == best)) {
+    d_->shape = best;
+    engineKind_ = best.plan;
     capture();
   }
+  storeShape(key, best, bestMs);
   zeroRows();
 }
 

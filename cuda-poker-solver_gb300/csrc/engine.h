@@ -10,6 +10,7 @@
 
 #include "compiler.h"
 #include "layout.h"
+#include "tune.h"
 
 namespace pps {
 namespace gb {
@@ -79,6 +80,10 @@ class Engine {
   // counter (both plans compute identical rows). A no-op once tuned, after
   // setEngineKind, and where the fused plan does not apply.
   void autotune();
+  // Sets the launch shape (plan and level / group grids, tune.h) and turns
+  // the autotuner off; recaptures.
+  void setShape(const LaunchShape& s);
+  LaunchShape shape() const;
   int engineKind() const { return engineKind_; }
   // Compensated (two-float) cumulative-strategy sums: the strategy rows get
   // a row of low words (allocated on first use, zeroed when turned on; the
@@ -105,6 +110,7 @@ class Engine {
   size_t deviceBytes_ = 0;
   mutable int64_t h2d_ = 0, d2h_ = 0;
   void capture();
+  double timeShape(const LaunchShape& s, int n);
   void buildPlans();
   double taskBytes(int task, int tr, bool fwd) const;
   void ensureWalkBuffers();

@@ -13,6 +13,7 @@
 
 #include "kernels.cuh"
 #include "plan.cuh"
+#include "tune.h"
 #include "pps_gb.h"
 
 namespace pps {
@@ -799,10 +800,19 @@ void Forest::iterate(int n) {
     const int maxN = d.maxN(all);
     const size_t smemSd = sdGroupSmem(maxN), smemFd = fdGroupSmem(maxN);
     raiseGroupSmem(maxN);
+    // The launch shape the autotuner cached for this size class (tune.h);
+    // the forest always runs the staged plan.
+    LaunchShape shape;
+    {
+      int64_t rowBytes = 0;
+      for (const auto& kv : d.live) rowBytes += (int64_t)kv.second.spot->layout.regQuads * 16;
+      if (lookupShape(tuneKeyOf(maxN, rowBytes), &shape)) shape.plan = 0;
+      else shape = LaunchShape{};
+    }
     const PlanArgs args{d.tree(), d.rows<float>(aReachF0, aReachF1, aCfvF), d.tasks, d.counter,
                         (int)d.counterCap, maxN, bwdScratchBytes<float>(maxN),
                         static_cast<const int4*>(d.arr[aGroups]), smemSd, smemFd,
-                        static_cast<const uint32_t*>(d.arr[aRecs]), d.recTasks};
+                        static_cast<const uint32_t*>(d.arr[aRecs]), d.recTasks, shape};
     GB_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
     issueStaged(d.staged, d.br, d.sev,
                 [&](const Launch& l, cudaStream_t s) { issueLaunch(args, l, s); });

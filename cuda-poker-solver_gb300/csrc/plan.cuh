@@ -15,6 +15,7 @@
 #include "decide.cuh"
 #include "pps_gb.h"
 #include "terminal.cuh"
+#include "tune.h"
 
 namespace pps {
 namespace gb {
@@ -70,6 +71,7 @@ struct PlanArgs {
   size_t smemSd, smemFd;  // sdGroupSmem / fdGroupSmem(maxN)
   const uint32_t* recs;      // decide record pool
   const uint32_t* recTasks;  // record offsets (the record and chance lists index these)
+  LaunchShape shape{};       // grids of the level and group launches (tune.h)
 };
 
 inline unsigned gridOf(int count) { return (unsigned)std::min(count, 1 << 20); }
@@ -93,15 +95,18 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
                                                  kModeCFR);
       break;
     case kSdGroup:
-      launchSdGroups(g, a.smemSd, s, a.tree, a.rows, a.groups, tk, l.list.count, l.tr, a.maxN);
+      launchSdGroups(cappedGrid(g, a.shape.sdCap), a.smemSd, s, a.tree, a.rows, a.groups, tk,
+                     l.list.count, l.tr, a.maxN);
       break;
     case kFdGroup:
-      launchFdGroups(g, a.smemFd, s, a.tree, a.rows, a.groups, tk, l.list.count, l.tr, a.maxN);
+      launchFdGroups(cappedGrid(g, a.shape.fdCap), a.smemFd, s, a.tree, a.rows, a.groups, tk,
+                     l.list.count, l.tr, a.maxN);
       break;
     case kBwdFused: {
       cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(gridOf(recordCtas(l.list.count) + l.list2.count + l.list3.count +
-                                l.list4.count));
+      cfg.gridDim = dim3(cappedGrid(gridOf(recordCtas(l.list.count) + l.list2.count +
+                                           l.list3.count + l.list4.count),
+                                    a.shape.bwdCap));
       cfg.blockDim = dim3(kThreads);
       cfg.dynamicSmemBytes = fusedLevelSmem(a.maxN);
       cfg.stream = s;
@@ -123,7 +128,8 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       // previous kernel in the stream drains (the kernels wait for it
       // before touching rows).
       cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(gridOf(recordCtas(l.list.count) + l.list2.count));
+      cfg.gridDim = dim3(cappedGrid(gridOf(recordCtas(l.list.count) + l.list2.count),
+                                    l.kind == kFwdMix ? a.shape.fwdCap : a.shape.bwdCap));
       cfg.blockDim = dim3(kThreads);
       cfg.dynamicSmemBytes = l.kind == kFwdMix ? fwdStageBytes() : bwdStageBytes();
       cfg.stream = s;

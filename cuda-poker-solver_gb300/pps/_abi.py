@@ -52,6 +52,11 @@ class Info(C.Structure):
                 ("compensated", C.c_int32)]
 
 
+class LaunchShape(C.Structure):
+    _fields_ = [("plan", C.c_int32), ("fwd_cap", C.c_int32), ("bwd_cap", C.c_int32),
+                ("sd_cap", C.c_int32), ("fd_cap", C.c_int32)]
+
+
 class KernelStat(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("ms", C.c_double),
                 ("algo_bytes", C.c_double)]
@@ -131,6 +136,8 @@ _SIGS = {
     "pps_gb_walk": (C.c_int, [H, C.c_int, C.c_int, P(C.c_double), P(C.c_double)]),
     "pps_gb_set_engine": (C.c_int, [H, C.c_int]),
     "pps_gb_set_compensated": (C.c_int, [H, C.c_int]),
+    "pps_gb_set_launch_shape": (C.c_int, [H, P(LaunchShape)]),
+    "pps_gb_get_launch_shape": (C.c_int, [H, P(LaunchShape)]),
     "pps_gb_time_iterations": (C.c_int, [H, C.c_int, P(C.c_double)]),
     "pps_gb_profile": (C.c_int, [H, C.c_int, C.c_int, P(KernelStat), C.c_int, P(C.c_int)]),
     "pps_gb_solve_noalloc": (C.c_int, [P(Spot), P(BetConfig), C.c_void_p, C.c_void_p, C.c_int64,

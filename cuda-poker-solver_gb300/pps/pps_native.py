@@ -415,6 +415,22 @@ class Solver:
     def set_engine(self, kind: int) -> None:
         check(lib.pps_gb_set_engine(self._h, int(kind)))
 
+    _SHAPE_KEYS = ("plan", "fwd_cap", "bwd_cap", "sd_cap", "fd_cap")
+
+    def set_launch_shape(self, **shape: int) -> None:
+        """Launch shape of the iteration graph (pps_gb_set_launch_shape):
+        plan 0 / 2 and grid caps in SM multiples (0: one CTA per task);
+        unnamed keys keep their current values. Turns the autotuner off."""
+        cur = self.launch_shape()
+        cur.update(shape)
+        ls = _abi.LaunchShape(*[int(cur[k]) for k in self._SHAPE_KEYS])
+        check(lib.pps_gb_set_launch_shape(self._h, C.byref(ls)))
+
+    def launch_shape(self) -> Dict[str, int]:
+        ls = _abi.LaunchShape()
+        check(lib.pps_gb_get_launch_shape(self._h, C.byref(ls)))
+        return {k: int(getattr(ls, k)) for k in self._SHAPE_KEYS}
+
     def set_compensated(self, on: bool = True) -> None:
         """Two-float cumulative-strategy sums (pps_gb_set_compensated)."""
         check(lib.pps_gb_set_compensated(self._h, 1 if on else 0))

@@ -233,6 +233,24 @@ int pps_gb_walk(pps_gb_solver* h, int traverser, int mode, double* root_cfv,
  * faster; setting an engine turns that off. */
 int pps_gb_set_engine(pps_gb_solver* h, int engine);
 
+/* Extension: the launch shape of the iteration graph, which the first solve
+ * of 32 or more iterations picks by timing candidates on the tree (or takes
+ * from the autotuner's cache for the tree's size class: file
+ * PPS_GB_TUNE_FILE, "off" for none, else $XDG_CACHE_HOME or $HOME/.cache
+ * pps_gb/launch_shapes). plan: 0 staged, 2 fused backward levels (lists of
+ * at most 1023 combos). Each cap gives a launch kind's grid: 0, one CTA per
+ * task; k (1..64), a persistent grid of k x SM-count CTAs striding over the
+ * level's (spot, node-range) tasks. Shapes change timing only: the rows are
+ * identical under every shape. Setting a shape turns the autotuner off. No
+ * reference counterpart (its launch geometry is fixed: block 128, one block
+ * per node, cuda/gpu_cfr.cu:806-816). */
+typedef struct {
+  int32_t plan;
+  int32_t fwd_cap, bwd_cap, sd_cap, fd_cap;
+} pps_gb_launch_shape;
+int pps_gb_set_launch_shape(pps_gb_solver* h, const pps_gb_launch_shape* shape);
+int pps_gb_get_launch_shape(pps_gb_solver* h, pps_gb_launch_shape* out);
+
 /* Extension: compensated (two-float) cumulative-strategy sums, the update
  * strat = strat * avg + sigma of cuda/gpu_cfr.cu:512-523 carried as an
  * unevaluated sum of two floats (a row of low words beside the strategy
