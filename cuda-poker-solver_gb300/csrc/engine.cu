@@ -170,16 +170,20 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
     d.fdG.push_back(addList(L_.fdGroupTasks[dd]));
   }
   std::vector<uint32_t> recTasks;
-  for (int tr = 0; tr < 2; ++tr)
-    for (int dd = 0; dd < D; ++dd) {
-      const std::vector<uint32_t>* src[4] = {&L_.bwdRecs[tr][dd], &L_.fwdRecs[tr][dd],
-                                             &L_.bwdChanceRecs[tr][dd], &L_.fwdChanceRecs[tr][dd]};
-      std::vector<ListRef>* dst[4] = {&d.bRec[tr], &d.fRec[tr], &d.bCh[tr], &d.fCh[tr]};
-      for (int k = 0; k < 4; ++k) {
-        dst[k]->push_back(ListRef{(int)recTasks.size(), (int)src[k]->size()});
-        recTasks.insert(recTasks.end(), src[k]->begin(), src[k]->end());
-      }
+  auto addRecs = [&](const std::vector<uint32_t>& v, std::vector<ListRef>& dst) {
+    dst.push_back(ListRef{(int)recTasks.size(), (int)v.size()});
+    recTasks.insert(recTasks.end(), v.begin(), v.end());
+  };
+  for (int tr = 0; tr < 2; ++tr) {
+    for (int dd = 0; dd < D; ++dd) {  // backward: per depth
+      addRecs(L_.bwdRecs[tr][dd], d.bRec[tr]);
+      addRecs(L_.bwdChanceRecs[tr][dd], d.bCh[tr]);
     }
+    for (size_t lv = 0; lv < L_.fwdRecs[tr].size(); ++lv) {  // forward: per level
+      addRecs(L_.fwdRecs[tr][lv], d.fRec[tr]);
+      addRecs(L_.fwdChanceRecs[tr][lv], d.fCh[tr]);
+    }
+  }
   d.recs = upload(d, L_.recPool, B, h2d_);
   d.recTasks = upload(d, recTasks, B, h2d_);
   d.tasks = upload(d, all, B, h2d_);
@@ -281,20 +285,24 @@ void Engine::buildPlans() {
   const int D = (int)d.fwd[0].size();
   for (int tr = 0; tr < 2; ++tr) {
     HalfStep& h = d.staged.half[tr];
-    h.fwd.assign(D, {});
+    const int F = (int)d.fRec[tr].size();
+    h.fwd.assign(F, {});
     h.bwd.assign(D, {});
     h.sd.assign(D, Launch{kSdGroup, tr, ListRef{}, 0.0});
     h.fd.assign(D, Launch{kFdGroup, tr, ListRef{}, 0.0});
-    for (int dd = 0; dd < D; ++dd) {
-      if (d.fRec[tr][dd].count || d.fCh[tr][dd].count) {
-        Launch l{kFwdMix, tr, d.fRec[tr][dd],
-                 listBytes(kindOnly(L_.fwdTasks[tr][dd], kTaskDecide), tr, true) +
-                     listBytes(L_.fwdChance[tr][dd], tr, true)};
-        l.list2 = d.fCh[tr][dd];
-        l.bytes2 = listBytes(L_.fwdChance[tr][dd], tr, true);
+    h.termAfter = L_.termAfter[tr];
+    for (int lv = 0; lv < F; ++lv) {
+      if (d.fRec[tr][lv].count || d.fCh[tr][lv].count) {
+        Launch l{kFwdMix, tr, d.fRec[tr][lv],
+                 listBytes(L_.fwdDecide[tr][lv], tr, true) +
+                     listBytes(L_.fwdChance[tr][lv], tr, true)};
+        l.list2 = d.fCh[tr][lv];
+        l.bytes2 = listBytes(L_.fwdChance[tr][lv], tr, true);
         l.early = tr == 0;  // the first half-step of the iteration
-        h.fwd[dd].push_back(l);
+        h.fwd[lv].push_back(l);
       }
+    }
+    for (int dd = 0; dd < D; ++dd) {
       if (d.sdG[dd].count)
         h.sd[dd] = {kSdGroup, tr, d.sdG[dd], groupBytes(L_.sdGroupTasks[dd], tr)};
       if (d.fdG[dd].count)
@@ -340,8 +348,8 @@ void Engine::buildPlans() {
   if (d.maxN <= kFusedMaxN) {
     for (int tr = 0; tr < 2; ++tr) {
       const HalfStep& h = d.staged.half[tr];
-      for (int dd = 0; dd < D; ++dd)
-        for (Launch l : h.fwd[dd]) {
+      for (const auto& set : h.fwd)
+        for (Launch l : set) {
           l.late = true;
           F.push_back(l);
         }

@@ -265,6 +265,9 @@ struct SlotRec {
   std::vector<std::vector<int>> sdG, fdG;
   std::vector<std::vector<uint32_t>> bCh[2], fCh[2];  // chance record offsets, relocated
   std::vector<std::vector<uint32_t>> bRec[2], fRec[2];  // record offsets, relocated
+  // fRec / fCh are per forward level (layout.h); termAfter[tr][d]: the
+  // forward level after which depth d's terminal reach rows are written.
+  std::vector<int> termAfter[2];
 };
 
 struct Forest::Dev {
@@ -642,6 +645,7 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
     rec.fRec[tr] = std::move(L.fwdRecs[tr]);
     rec.bCh[tr] = std::move(L.bwdChanceRecs[tr]);
     rec.fCh[tr] = std::move(L.fwdChanceRecs[tr]);
+    rec.termAfter[tr] = L.termAfter[tr];
     for (auto* lists : {&rec.bRec[tr], &rec.fRec[tr], &rec.bCh[tr], &rec.fCh[tr]})
       for (auto& v : *lists)
         for (uint32_t& o : v) o += recShift;
@@ -703,6 +707,7 @@ struct Lists {
   std::vector<int> all;
   std::vector<uint32_t> recs;  // record offsets
   std::vector<ListRef> fwd[2], bwd[2], fCh[2], bCh[2], fRec[2], bRec[2], sdG, fdG;
+  std::vector<int> termAfter[2];  // per depth: the latest of the spots' levels
 };
 
 Lists gather(const std::map<int, SlotRec>& live, const std::vector<int>& slots, bool iteration) {
@@ -731,18 +736,33 @@ Lists gather(const std::map<int, SlotRec>& live, const std::vector<int>& slots, 
   auto atR = [](const std::vector<std::vector<uint32_t>>& lists, int dd) {
     return dd < (int)lists.size() ? &lists[dd] : nullptr;
   };
-  for (int tr = 0; tr < 2; ++tr)
+  for (int tr = 0; tr < 2; ++tr) {
+    if (iteration) {
+      // Forward levels: a spot's level l tasks depend only on its own
+      // levels below l, so the spots' levels merge by index.
+      int F = 0;
+      for (int s : slots) F = std::max(F, (int)live.at(s).fRec[tr].size());
+      for (int lv = 0; lv < F; ++lv) {
+        out.fCh[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.fCh[tr], lv); }));
+        out.fRec[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.fRec[tr], lv); }));
+      }
+      out.termAfter[tr].assign(D, -1);
+      for (int s : slots) {
+        const std::vector<int>& ta = live.at(s).termAfter[tr];
+        for (int dd = 0; dd < D && dd < (int)ta.size(); ++dd)
+          out.termAfter[tr][dd] = std::max(out.termAfter[tr][dd], ta[dd]);
+      }
+    }
     for (int dd = 0; dd < D; ++dd) {
       if (iteration) {
-        out.fCh[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.fCh[tr], dd); }));
         out.bCh[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.bCh[tr], dd); }));
-        out.fRec[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.fRec[tr], dd); }));
         out.bRec[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.bRec[tr], dd); }));
       } else {
         out.fwd[tr].push_back(cat([&](const SlotRec& r) { return at(r.fwd[tr], dd); }));
         out.bwd[tr].push_back(cat([&](const SlotRec& r) { return at(r.bwd[tr], dd); }));
       }
     }
+  }
   if (iteration)
     for (int dd = 0; dd < D; ++dd) {
       out.sdG.push_back(cat([&](const SlotRec& r) { return at(r.sdG, dd); }));
@@ -772,19 +792,22 @@ void Forest::iterate(int n) {
       GB_CK(cudaMemcpyAsync(d.recTasks, ls.recs.data(), ls.recs.size() * sizeof(uint32_t),
                             cudaMemcpyHostToDevice, d.stream));
     for (int tr = 0; tr < 2; ++tr) {
-      const int D = (int)ls.fRec[tr].size();
+      const int D = (int)ls.bRec[tr].size();
       HalfStep& h = d.staged.half[tr];
-      h.fwd.assign(D, {});
+      const int F = (int)ls.fRec[tr].size();
+      h.fwd.assign(F, {});
       h.bwd.assign(D, {});
       h.sd.assign(D, Launch{kSdGroup, tr, ListRef{}, 0.0});
       h.fd.assign(D, Launch{kFdGroup, tr, ListRef{}, 0.0});
-      for (int dd = 0; dd < D; ++dd) {
-        if (ls.fRec[tr][dd].count || ls.fCh[tr][dd].count) {
-          Launch l{kFwdMix, tr, ls.fRec[tr][dd], 0.0};
-          l.list2 = ls.fCh[tr][dd];
+      h.termAfter = ls.termAfter[tr];
+      for (int lv = 0; lv < F; ++lv)
+        if (ls.fRec[tr][lv].count || ls.fCh[tr][lv].count) {
+          Launch l{kFwdMix, tr, ls.fRec[tr][lv], 0.0};
+          l.list2 = ls.fCh[tr][lv];
           l.early = tr == 0;  // the first half-step of the iteration
-          h.fwd[dd].push_back(l);
+          h.fwd[lv].push_back(l);
         }
+      for (int dd = 0; dd < D; ++dd) {
         if (ls.sdG[dd].count) h.sd[dd] = {kSdGroup, tr, ls.sdG[dd], 0.0};
         if (ls.fdG[dd].count) h.fd[dd] = {kFdGroup, tr, ls.fdG[dd], 0.0};
         if (ls.bRec[tr][dd].count || ls.bCh[tr][dd].count) {

@@ -411,17 +411,49 @@ HostLayout buildLayout(const Tree& t) {
     if (job < 2) taskLists(job);
     else termGroups();
   });
+  // Forward levels (see layout.h): level of a forward-working node = one
+  // more than its nearest forward-working ancestor's (0 without one); the
+  // nodes are in DFS pre-order, so parents come first.
+  std::vector<int> fwdLevel[2];
+  int F[2] = {0, 0};
+  for (int tr = 0; tr < 2; ++tr) {
+    std::vector<int>& lev = fwdLevel[tr];
+    std::vector<int> writer(N, -1);  // level of the task that wrote u's reach row
+    lev.assign(N, -1);
+    for (int u = 0; u < N; ++u) {
+      const Node& nd = t.nodes[u];
+      const int par = nd.parent;
+      if (par >= 0) {
+        const Node& pn = t.nodes[par];
+        const bool parWorks = pn.kind == kChance || (pn.kind == kDecide && pn.player != tr);
+        writer[u] = parWorks ? lev[par] : writer[par];
+      }
+      const bool works = nd.kind == kChance || (nd.kind == kDecide && nd.player != tr);
+      if (works) {
+        lev[u] = writer[u] + 1;
+        F[tr] = std::max(F[tr], lev[u] + 1);
+      }
+    }
+    L.termAfter[tr].assign(D, -1);
+    for (int u = 0; u < N; ++u)
+      if (t.nodes[u].kind == kShowdown || t.nodes[u].kind == kFold)
+        L.termAfter[tr][t.nodes[u].depth] =
+            std::max(L.termAfter[tr][t.nodes[u].depth], writer[u]);
+  }
   // Decide records and chance word lists of the default iteration.
   for (int tr = 0; tr < 2; ++tr) {
     L.bwdRecs[tr].assign(D, {});
-    L.fwdRecs[tr].assign(D, {});
+    L.fwdRecs[tr].assign(F[tr], {});
     L.bwdChance[tr].assign(D, {});
-    L.fwdChance[tr].assign(D, {});
+    L.fwdChance[tr].assign(F[tr], {});
+    L.fwdDecide[tr].assign(F[tr], {});
     for (int d = 0; d < D; ++d) {
       for (int w : L.bwdTasks[tr][d])
         if ((w & 3) == kTaskChance) L.bwdChance[tr][d].push_back(w);
-      for (int w : L.fwdTasks[tr][d])
-        if ((w & 3) == kTaskChance) L.fwdChance[tr][d].push_back(w);
+      for (int w : L.fwdTasks[tr][d]) {
+        const int lv = fwdLevel[tr][(int)((unsigned)w >> 8)];
+        ((w & 3) == kTaskChance ? L.fwdChance : L.fwdDecide)[tr][lv].push_back(w);
+      }
     }
   }
   // Decide records: [own regret row, value or reach row, n | na << 16 |
@@ -446,10 +478,7 @@ HostLayout buildLayout(const Tree& t) {
     }
   }
   for (int tr = 0; tr < 2; ++tr)
-    for (int d = 0; d < D; ++d) {
-      L.bwdRecs[tr][d].reserve(nBwd[tr][d]);
-      L.fwdRecs[tr][d].reserve(nFwd[tr][d]);
-    }
+    for (int d = 0; d < D; ++d) L.bwdRecs[tr][d].reserve(nBwd[tr][d]);
   size_t w = L.recPool.size();
   L.recPool.resize(words, 0u);
   std::vector<uint32_t> kids;
@@ -479,7 +508,7 @@ HostLayout buildLayout(const Tree& t) {
         kids[a] = L.rows[t.children[nd.childBase + a]].reachQ[tr];
       const int nOpp = t.n(u, 1 - tr);
       for (int c = 0, cf = chunksOf(nOpp); c < cf; ++c)
-        L.fwdRecs[tr][nd.depth].push_back(
+        L.fwdRecs[tr][fwdLevel[tr][u]].push_back(
             addRecord(L.nodes[u].regQ, L.rows[u].reachQ[tr], nOpp, nd.na, 0, c));
     }
   }
@@ -493,12 +522,12 @@ HostLayout buildLayout(const Tree& t) {
   //     value row, parent -> child slot map (i16 pool)], once per node.
   for (int tr = 0; tr < 2; ++tr) {
     const int opp = 1 - tr;
-    L.fwdChanceRecs[tr].assign(D, {});
     L.bwdChanceRecs[tr].assign(D, {});
     L.chanceTables[tr].clear();
     std::map<int, uint32_t> table;  // node -> its branch table
-    for (int d = 0; d < D; ++d) {
-      for (int w : L.fwdChance[tr][d]) {
+    L.fwdChanceRecs[tr].assign(F[tr], {});
+    for (int lv = 0; lv < F[tr]; ++lv)
+      for (int w : L.fwdChance[tr][lv]) {
         const int u = (int)((unsigned)w >> 8), br = (w >> 2) & 63;
         const int ch = t.children[t.nodes[u].childBase + br];
         const StateDev& cs = L.states[t.nodes[ch].state];
@@ -507,8 +536,9 @@ HostLayout buildLayout(const Tree& t) {
         L.recPool.push_back(L.rows[ch].reachQ[tr]);
         L.recPool.push_back((uint32_t)cs.upOff[opp]);
         L.recPool.push_back((uint32_t)cs.n[opp] | ((uint32_t)L.rows[u].chanceQ << 16));
-        L.fwdChanceRecs[tr][d].push_back(off);
+        L.fwdChanceRecs[tr][lv].push_back(off);
       }
+    for (int d = 0; d < D; ++d) {
       for (int w : L.bwdChance[tr][d]) {
         const int u = (int)((unsigned)w >> 8), chunk = (w >> 2) & 63;
         const Node& nd = t.nodes[u];
@@ -601,6 +631,8 @@ uint64_t layoutDigest(const HostLayout& L) {
     }
     f.vecs(L.bwdChance[tr]);
     f.vecs(L.fwdChance[tr]);
+    f.vecs(L.fwdDecide[tr]);
+    f.vec(L.termAfter[tr]);
   }
   f.bytes(&L.maxN, sizeof L.maxN);
   f.bytes(&L.maxCardSeg, sizeof L.maxCardSeg);

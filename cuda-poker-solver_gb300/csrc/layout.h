@@ -118,9 +118,17 @@ struct HostLayout {
   std::vector<TermGroup> groups;
   std::vector<std::vector<int>> sdGroupTasks, fdGroupTasks;
   std::vector<std::vector<int>> innerTasks[2];
-  // Decide records (decide.cuh) of the default iteration: the pool, and per
-  // traverser and depth the backward and forward record offsets (16-byte
-  // units); the chance tasks of those levels as task words.
+  // Decide records (decide.cuh) of the default iteration: the pool, per
+  // traverser and depth the backward record offsets (16-byte units), and
+  // per traverser and FORWARD LEVEL the forward ones. A forward task (an
+  // opponent decide node's chunk, a chance branch) reads the reach row that
+  // its node's nearest forward-working ancestor wrote (the traverser's own
+  // decide nodes pass rows through unchanged), so its level is one more
+  // than that ancestor's: a chain of opponent and chance nodes, about half
+  // the depth. fwdDecide / fwdChance hold the same tasks as task words
+  // (byte model); termAfter[tr][d] is the forward level after which every
+  // reach row that depth d's terminal nodes read is written (-1: at the
+  // start of the half-step).
   std::vector<uint32_t> recPool;
   std::vector<std::vector<uint32_t>> bwdRecs[2], fwdRecs[2];
   // Chance records in the same pool (decide.cuh): forward one per branch,
@@ -128,7 +136,8 @@ struct HostLayout {
   std::vector<std::vector<uint32_t>> fwdChanceRecs[2], bwdChanceRecs[2];
   // Branch tables: offset (16-byte units) and branch count.
   std::vector<std::pair<uint32_t, int>> chanceTables[2];
-  std::vector<std::vector<int>> bwdChance[2], fwdChance[2];
+  std::vector<std::vector<int>> bwdChance[2], fwdChance[2], fwdDecide[2];
+  std::vector<int> termAfter[2];
   int maxN = 0;        // largest list size (either side)
   int maxCardSeg = 0;  // longest card segment of any list
 };

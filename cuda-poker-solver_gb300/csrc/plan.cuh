@@ -211,8 +211,12 @@ void issuePlan(const std::vector<Launch>& P, const Branches& b, IssueOne&& one) 
 // own streams, beside the rest of the forward pass; a backward level waits
 // only for the terminals one depth below it.
 struct HalfStep {
-  std::vector<std::vector<Launch>> fwd, bwd;  // per depth
-  std::vector<Launch> sd, fd;                 // per depth (count 0: none)
+  std::vector<std::vector<Launch>> fwd;  // per forward level (layout.h)
+  std::vector<std::vector<Launch>> bwd;  // per depth
+  std::vector<Launch> sd, fd;            // per depth (count 0: none)
+  // Per depth: the forward level after which its terminal groups may
+  // start (-1: at the start of the half-step).
+  std::vector<int> termAfter;
 };
 struct StagedPlan {
   HalfStep half[2];
@@ -284,16 +288,16 @@ void issueStaged(const StagedPlan& P, const Branches& b, StagedEvents& ev, Issue
     GB_CK(cudaStreamWaitEvent(b.main, ev.ljoin, 0));
   };
   for (const HalfStep& h : P.half) {
-    const int D = (int)h.fwd.size();
-    ev.ensure(D);
+    const int D = (int)h.bwd.size(), F = (int)h.fwd.size();
+    ev.ensure(std::max(D, F));
     GB_CK(cudaEventRecord(ev.start, b.main));
     std::vector<char> sdOpen(D, 0), fdOpen(D, 0);
-    auto startTerminals = [&](int d) {  // depth d's reach rows are written
+    auto startTerminals = [&](int d, int after) {  // depth d's reach rows are written
       for (int k = 0; k < 2; ++k) {
         const Launch& l = k == 0 ? h.sd[d] : h.fd[d];
         if (!l.list.count) continue;
         cudaStream_t s = b.side[1 + 2 * (d % kTermRot) + k];
-        GB_CK(cudaStreamWaitEvent(s, d == 0 ? ev.start : ev.fwd[d - 1], 0));
+        GB_CK(cudaStreamWaitEvent(s, after < 0 ? ev.start : ev.fwd[after], 0));
         one(l, s);
         GB_CK(cudaEventRecord(k == 0 ? ev.sd[d] : ev.fd[d], s));
         (k == 0 ? sdOpen : fdOpen)[d] = 1;
@@ -305,11 +309,19 @@ void issueStaged(const StagedPlan& P, const Branches& b, StagedEvents& ev, Issue
       if (fdOpen[d]) GB_CK(cudaStreamWaitEvent(b.main, ev.fd[d], 0));
       sdOpen[d] = fdOpen[d] = 0;
     };
-    startTerminals(0);
-    for (int d = 0; d < D; ++d) {
-      issueSet(h.fwd[d]);
-      GB_CK(cudaEventRecord(ev.fwd[d], b.main));
-      if (d + 1 < D) startTerminals(d + 1);
+    // A depth whose terminals need a level past the last one that launches
+    // (none does, but keep every depth covered) starts after the last.
+    auto afterOf = [&](int d) {
+      const int a = d < (int)h.termAfter.size() ? h.termAfter[d] : F - 1;
+      return std::min(a, F - 1);
+    };
+    for (int d = 0; d < D; ++d)
+      if (afterOf(d) < 0) startTerminals(d, -1);
+    for (int lv = 0; lv < F; ++lv) {
+      issueSet(h.fwd[lv]);
+      GB_CK(cudaEventRecord(ev.fwd[lv], b.main));
+      for (int d = 0; d < D; ++d)
+        if (afterOf(d) == lv) startTerminals(d, lv);
     }
     for (int d = D - 1; d >= 0; --d) {
       joinTerminals(d + 1);
