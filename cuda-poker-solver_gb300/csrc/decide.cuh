@@ -30,6 +30,25 @@ namespace gb {
 
 __host__ __device__ inline int recordWords(int na) { return (4 + na + 3) / 4 * 4; }
 
+// Regret matching+ with one reciprocal per combo: sigma_a = max(x_a, 0) /
+// acc (the reference's cuda/gpu_cfr.cu:245-262 and 479-500), uniform where
+// acc = 0. The quotient comes from r = RN(1 / acc), computed once per
+// combo, and one correction step (Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990): q0 = RN(x r), e = RN(x - q0 acc) exactly by an fma, q = RN(q0 +
+// e r). With r the correctly rounded reciprocal and no overflow or
+// underflow on the way (0 < x <= acc, regrets far from both limits), q is
+// the correctly rounded quotient: the same sigma as a division, bit for
+// bit, for three instructions instead of a division per action.
+__device__ __forceinline__ float rmInv(float acc) { return acc > 0.f ? __frcp_rn(acc) : 0.f; }
+__device__ __forceinline__ float rmSigma(float x, float acc, float inv, float uniform) {
+  if (!(acc > 0.f)) return uniform;
+  if (!(x > 0.f)) return 0.f;
+  const float q0 = __fmul_rn(x, inv);
+  const float e = __fmaf_rn(-q0, acc, x);
+  return __fmaf_rn(e, inv, q0);
+}
+
 struct DecRec {
   uint32_t regQ, rowQ;
   int n, na, own, chunk, spot;
@@ -110,11 +129,13 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
     ldq(reg + ((size_t)a * nq + q) * 4, x);
     for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
   }
+  float inv[4];
+  for (int l = 0; l < 4; ++l) inv[l] = rmInv(acc[l]);
   for (int a = 0; a < na; ++a) {
     float x[4], c[4];
     ldq(reg + ((size_t)a * nq + q) * 4, x);
     ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, c);
-    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, 0) : 0.f) * c[l];
+    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? rmSigma(x[l], acc[l], inv[l], uniform) : 0.f) * c[l];
   }
   stq(out + 4 * q, val);
   float* strLo = t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr;
@@ -126,7 +147,7 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
     if (strLo) ldq(strLo + o, lo);
     ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, c);
     for (int l = 0; l < 4; ++l) {
-      const float s = live[l] ? sigmaOf(rg[l], acc[l], uniform, 0) : 0.f;
+      const float s = live[l] ? rmSigma(rg[l], acc[l], inv[l], uniform) : 0.f;
       stratUpdate(sg[l], lo[l], avg, s, strLo);
       rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
     }
@@ -153,11 +174,13 @@ __device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<
     ldq(src + ((size_t)a * nq + q) * 4, x);
     for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
   }
+  float inv[4];
+  for (int l = 0; l < 4; ++l) inv[l] = rmInv(acc[l]);
   for (int a = 0; a < na; ++a) {
     float x[4], o[4];
     ldq(src + ((size_t)a * nq + q) * 4, x);
     for (int l = 0; l < 4; ++l)
-      o[l] = 4 * q + l < r.n ? rr[l] * sigmaOf(x[l], acc[l], uniform, 0) : 0.f;
+      o[l] = 4 * q + l < r.n ? rr[l] * rmSigma(x[l], acc[l], inv[l], uniform) : 0.f;
     stq(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q, o);
   }
 }
@@ -263,11 +286,13 @@ __device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRo
     ld4s(&R[a * kThreads + tid], x);
     for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
   }
+  float inv[4];
+  for (int l = 0; l < 4; ++l) inv[l] = rmInv(acc[l]);
   for (int a = 0; a < na; ++a) {
     float x[4], c[4];
     ld4s(&R[a * kThreads + tid], x);
     ld4s(&C[a * kThreads + tid], c);
-    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, 0) : 0.f) * c[l];
+    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? rmSigma(x[l], acc[l], inv[l], uniform) : 0.f) * c[l];
   }
   stq(out + 4 * q, val);
   float* strLo = t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr;
@@ -279,7 +304,7 @@ __device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRo
     ld4s(&C[a * kThreads + tid], c);
     if (strLo) ldq(strLo + o, lo);
     for (int l = 0; l < 4; ++l) {
-      const float s = live[l] ? sigmaOf(rg[l], acc[l], uniform, 0) : 0.f;
+      const float s = live[l] ? rmSigma(rg[l], acc[l], inv[l], uniform) : 0.f;
       stratUpdate(sg[l], lo[l], avg, s, strLo);
       rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
     }
@@ -332,11 +357,13 @@ __device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const De
     ld4s(&R[a * kThreads + tid], x);
     for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
   }
+  float inv[4];
+  for (int l = 0; l < 4; ++l) inv[l] = rmInv(acc[l]);
   for (int a = 0; a < na; ++a) {
     float x[4], o[4];
     ld4s(&R[a * kThreads + tid], x);
     for (int l = 0; l < 4; ++l)
-      o[l] = 4 * q + l < r.n ? rr[l] * sigmaOf(x[l], acc[l], uniform, 0) : 0.f;
+      o[l] = 4 * q + l < r.n ? rr[l] * rmSigma(x[l], acc[l], inv[l], uniform) : 0.f;
     stq(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q, o);
   }
 }
@@ -486,11 +513,13 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
     ld4s(&R[a * kRecQuads + lane], x);
     for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
   }
+  float inv[4];
+  for (int l = 0; l < 4; ++l) inv[l] = rmInv(acc[l]);
   for (int a = 0; a < na; ++a) {
     float x[4], c[4];
     ld4s(&R[a * kRecQuads + lane], x);
     ld4s(&C[a * kRecQuads + lane], c);
-    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? sigmaOf(x[l], acc[l], uniform, 0) : 0.f) * c[l];
+    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? rmSigma(x[l], acc[l], inv[l], uniform) : 0.f) * c[l];
   }
   stq(out + 4 * q, val);
   float* strLo = t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr;
@@ -502,7 +531,7 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
     ld4s(&C[a * kRecQuads + lane], c);
     if (strLo) ldq(strLo + o, lo);
     for (int l = 0; l < 4; ++l) {
-      const float s = live[l] ? sigmaOf(rg[l], acc[l], uniform, 0) : 0.f;
+      const float s = live[l] ? rmSigma(rg[l], acc[l], inv[l], uniform) : 0.f;
       stratUpdate(sg[l], lo[l], avg, s, strLo);
       rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
     }
