@@ -53,6 +53,7 @@ struct DecRec {
   uint32_t regQ, rowQ;
   int n, na, own, chunk, spot;
   const uint32_t* kid;
+  const uint32_t* pre;  // folded-in children (header bit 25), else nullptr
 };
 
 __device__ __forceinline__ DecRec loadRec(const uint32_t* __restrict__ recs, uint32_t off16) {
@@ -63,11 +64,49 @@ __device__ __forceinline__ DecRec loadRec(const uint32_t* __restrict__ recs, uin
   d.rowQ = h.y;
   d.n = (int)(h.z & 0xffff);
   d.na = (int)((h.z >> 16) & 0xff);
-  d.own = (int)(h.z >> 24);
+  d.own = (int)((h.z >> 24) & 1);
   d.chunk = (int)(h.w & 0xffff);
   d.spot = (int)(h.w >> 16);
   d.kid = r + 4;
+  d.pre = (h.z >> 25) & 1 ? r + 4 + d.na : nullptr;
   return d;
+}
+
+// Folded-in children of a traverser record (layout.cpp, buildBackwardLevels):
+// for each, the lane's quad of its value row = the sum of its children's,
+// in action order, padding lanes zero - exactly what that child's own
+// record computes (the opponent branch of decideRecord) - written before
+// the record reads its children's rows. Each lane writes only its own
+// quad; the caller orders the writes before reads by other lanes or by the
+// bulk-copy engine.
+__device__ __forceinline__ void recordFoldedChildren(const DevRows<float>& rows, const DecRec& r,
+                                                     int lane) {
+  if (!r.pre) return;
+  const int nq = quadsOf(r.n);
+  const int q = r.chunk * kRecQuads + lane;
+  const uint32_t* p = r.pre;
+  const int P = (int)p[0];
+  ++p;
+  for (int e = 0; e < P; ++e) {
+    const uint32_t row = p[0];
+    const int m = (int)p[1];
+    p += 2;
+    if (q < nq) {
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int b = 0; b < m; ++b) {
+        float c[4];
+        ldq(rows.cfv + (size_t)p[b] * 4 + 4 * q, c);
+        for (int l = 0; l < 4; ++l) v[l] += c[l];
+      }
+      for (int l = 0; l < 4; ++l)
+        if (4 * q + l >= r.n) v[l] = 0.f;
+      stq(rows.cfv + (size_t)row * 4 + 4 * q, v);
+    }
+    p += m;
+  }
+  // The rows just written are read next by copies of the async proxy (bulk
+  // and cp.async staging) and by other lanes.
+  asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 
 // One entry of the cumulative-strategy update: compensated (stratComp)
@@ -89,6 +128,7 @@ __device__ __forceinline__ void prefetchStratLo(const DevTree& t, const DecRec& 
 // Backward decide record (CFR mode, f32 rows), one warp: lane = quad.
 __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<float>& rows,
                                              const DecRec& r, int lane) {
+  recordFoldedChildren(rows, r, lane);  // this lane reads back only its own quads
   const int nq = quadsOf(r.n);
   const int q = r.chunk * kRecQuads + lane;
   if (q >= nq) return;
@@ -249,6 +289,7 @@ __device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRo
     decideRecord(t, rows, r, lane);
     return;
   }
+  recordFoldedChildren(rows, r, lane);  // each thread copies back only its own quads
   const int nq = quadsOf(r.n);
   const int q = r.chunk * kRecQuads + lane;
   if (q >= nq) return;
@@ -469,6 +510,10 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
   }
   if (r.own && q0 + lane < nq) prefetchStratLo(t, r, q0 + lane, nq);
   pdlWait();
+  if (r.pre) {  // folded-in children: every lane's quads written before lane 0's copies
+    recordFoldedChildren(rows, r, lane);
+    __syncwarp();
+  }
   if (lane == 0)
     for (int a = 0; a < na; ++a)
       bulkLoad(&C[a * kRecQuads], rows.cfv + ((size_t)r.kid[a] + q0) * 4, segBytes, bar);

@@ -69,6 +69,7 @@ struct Engine::Dev {
   std::vector<ListRef> sdG, fdG, inner[2];  // the group plan's backward lists
   std::vector<ListRef> bCh[2], fCh[2];       // its chance word lists
   std::vector<ListRef> bRec[2], fRec[2];     // its decide record lists (into recTasks)
+  std::vector<ListRef> bRecH[2], bChH[2];    // backward per level (the staged plan)
   int4* groups = nullptr;
   uint32_t* recs = nullptr;
   uint32_t* recTasks = nullptr;
@@ -182,6 +183,10 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
     for (size_t lv = 0; lv < L_.fwdRecs[tr].size(); ++lv) {  // forward: per level
       addRecs(L_.fwdRecs[tr][lv], d.fRec[tr]);
       addRecs(L_.fwdChanceRecs[tr][lv], d.fCh[tr]);
+    }
+    for (size_t lv = 0; lv < L_.bwdRecsH[tr].size(); ++lv) {  // backward: per level
+      addRecs(L_.bwdRecsH[tr][lv], d.bRecH[tr]);
+      addRecs(L_.bwdChanceRecsH[tr][lv], d.bChH[tr]);
     }
   }
   d.recs = upload(d, L_.recPool, B, h2d_);
@@ -307,14 +312,18 @@ void Engine::buildPlans() {
         h.sd[dd] = {kSdGroup, tr, d.sdG[dd], groupBytes(L_.sdGroupTasks[dd], tr)};
       if (d.fdG[dd].count)
         h.fd[dd] = {kFdGroup, tr, d.fdG[dd], groupBytes(L_.fdGroupTasks[dd], tr)};
-      if (d.bRec[tr][dd].count || d.bCh[tr][dd].count) {
-        Launch l{kBwdMix, tr, d.bRec[tr][dd],
-                 listBytes(kindOnly(L_.bwdTasks[tr][dd], kTaskDecide), tr, false) +
-                     listBytes(L_.bwdChance[tr][dd], tr, false)};
-        l.list2 = d.bCh[tr][dd];
-        l.bytes2 = listBytes(L_.bwdChance[tr][dd], tr, false);
-        h.bwd[dd].push_back(l);
-      }
+    }
+    // Backward per level (layout.h): each launch waits for the
+    // terminal depths its nodes read.
+    const int H = (int)d.bRecH[tr].size();
+    h.bwd.assign(H, {});
+    h.bwdNeed = L_.bwdNeed[tr];
+    for (int lv = 0; lv < H; ++lv) {
+      if (!d.bRecH[tr][lv].count && !d.bChH[tr][lv].count) continue;
+      Launch l{kBwdMix, tr, d.bRecH[tr][lv], listBytes(L_.bwdTasksH[tr][lv], tr, false)};
+      l.list2 = d.bChH[tr][lv];
+      l.bytes2 = listBytes(kindOnly(L_.bwdTasksH[tr][lv], kTaskChance), tr, false);
+      h.bwd[lv].push_back(l);
     }
   }
   d.plan[0] = d.staged.flat();
@@ -361,8 +370,8 @@ void Engine::buildPlans() {
         l.list3 = d.sdG[dd];
         l.list4 = d.fdG[dd];
         if (!l.list.count && !l.list2.count && !l.list3.count && !l.list4.count) continue;
-        for (const Launch& b : h.bwd[dd]) l.bytes += b.bytes;
-        l.bytes += h.sd[dd].bytes + h.fd[dd].bytes;
+        l.bytes = listBytes(kindOnly(L_.bwdTasks[tr][dd], kTaskDecide), tr, false) +
+                  listBytes(L_.bwdChance[tr][dd], tr, false) + h.sd[dd].bytes + h.fd[dd].bytes;
         F.push_back(l);
         first = false;
       }

@@ -223,6 +223,145 @@ void parallelFor(int n, F&& f) {
 
 }  // namespace
 
+namespace {
+
+// The staged plan's backward levels (layout.h). Per traverser tr:
+//   - an opponent decide node whose parent is one of tr's decide nodes is
+//     "folded into" the parent: its value row (the sum of its children's)
+//     is computed by the parent's records, chunk by chunk, right before the
+//     parent uses it, so it needs no level of its own;
+//   - every other node with backward work (tr's decide nodes, chance nodes,
+//     opponent decide nodes under a chance node) sits at a level below all
+//     the levels that read its row (see the work depth below);
+//   - an opponent decide node at the root does no work (its value is read
+//     by nothing in the iteration).
+// The records of a traverser node with folded-in children are new: [regret
+// row, value row, n | na << 16 | 1 << 24 | 1 << 25, chunk, child rows[na],
+// P, then P times (child value row, m, its m children's value rows)],
+// padded to 16 bytes; other nodes reuse their depth-list records.
+void buildBackwardLevels(const Tree& t, HostLayout& L,
+                         const std::vector<uint32_t> (&firstRec)[2],
+                         const std::vector<std::vector<uint32_t>> (&chanceRecs)[2]) {
+  const int N = (int)t.nodes.size();
+  auto child = [&](int u, int a) { return t.children[t.nodes[u].childBase + a]; };
+  auto terminal = [&](int u) {
+    return t.nodes[u].kind == kShowdown || t.nodes[u].kind == kFold;
+  };
+  auto chunks = [](int n) { return (int)((quads(n) + kRecQuads - 1) / kRecQuads); };
+  auto recWords = [](int na) { return (size_t)(4 + na + 3) / 4 * 4; };
+  for (int tr = 0; tr < 2; ++tr) {
+    auto opponent = [&](int u) {
+      return t.nodes[u].kind == kDecide && t.nodes[u].player != tr;
+    };
+    auto foldedIn = [&](int u) {
+      const int p = t.nodes[u].parent;
+      return opponent(u) && p >= 0 && t.nodes[p].kind == kDecide && t.nodes[p].player == tr;
+    };
+    auto works = [&](int u) {
+      if (terminal(u) || foldedIn(u)) return false;
+      return !(opponent(u) && t.nodes[u].parent < 0);
+    };
+    // Levels as late as possible: a node's work depth is the number of
+    // working ancestors (through folded-in children), and level = deepest
+    // work depth - its own, so each level holds the nodes of one work depth
+    // and reads the terminals of the depths just below them: the backward
+    // pass starts on the deepest nodes while shallower terminal groups are
+    // still running.
+    std::vector<int> wd(N, -1), h(N, -1);
+    std::vector<uint64_t> need(N, 0);
+    int maxWd = -1;
+    for (int u = 0; u < N; ++u) {  // parents first (DFS pre-order)
+      int up = -1;
+      for (int p = t.nodes[u].parent; p >= 0; p = t.nodes[p].parent)
+        if (works(p)) {
+          up = wd[p];
+          break;
+        }
+      if (!works(u)) continue;
+      wd[u] = up + 1;
+      maxWd = std::max(maxWd, wd[u]);
+    }
+    const int H = maxWd + 1;
+    for (int u = 0; u < N; ++u) {
+      if (!works(u)) continue;
+      h[u] = maxWd - wd[u];
+      uint64_t nd = 0;
+      auto input = [&](int k) {
+        if (terminal(k)) nd |= (uint64_t)1 << t.nodes[k].depth;
+      };
+      for (int a = 0; a < t.nodes[u].nChildren; ++a) {
+        const int k = child(u, a);
+        if (foldedIn(k))
+          for (int b = 0; b < t.nodes[k].nChildren; ++b) input(child(k, b));
+        else
+          input(k);
+      }
+      need[u] = nd;
+    }
+    if (t.maxDepth >= 64) throw Error{PPS_GB_E_ARG, "tree deeper than 64 levels"};
+    L.bwdRecsH[tr].assign(H, {});
+    L.bwdChanceRecsH[tr].assign(H, {});
+    L.bwdTasksH[tr].assign(H, {});
+    L.bwdNeed[tr].assign(H, 0);
+    L.presumRecs[tr].clear();
+    for (int u = 0; u < N; ++u) {
+      if (h[u] < 0) continue;
+      const Node& nd = t.nodes[u];
+      const int lv = h[u];
+      L.bwdNeed[tr][lv] |= need[u];
+      if (nd.kind == kChance) {
+        for (uint32_t off : chanceRecs[tr][u]) L.bwdChanceRecsH[tr][lv].push_back(off);
+        for (int c = 0; c < (int)(quads(t.n(u, tr)) * 4 + kChanceChunk - 1) / kChanceChunk; ++c)
+          L.bwdTasksH[tr][lv].push_back(makeTask(kTaskChance, c, u));
+        continue;
+      }
+      const int n = t.n(u, tr), nc = chunks(n);
+      for (int c = 0; c < (n + 4 * kChunkQuads - 1) / (4 * kChunkQuads); ++c)
+        L.bwdTasksH[tr][lv].push_back(makeTask(kTaskDecide, c, u));
+      bool folds = false;
+      for (int a = 0; a < nd.na; ++a) folds |= foldedIn(child(u, a));
+      if (!folds) {  // the depth-list records, unchanged
+        const uint32_t stride = (uint32_t)(recWords(nd.na) / 4);
+        for (int c = 0; c < nc; ++c) L.bwdRecsH[tr][lv].push_back(firstRec[tr][u] + (uint32_t)c * stride);
+        continue;
+      }
+      for (int a = 0; a < nd.na; ++a) {  // the folded-in children's work (byte model)
+        const int k = child(u, a);
+        if (foldedIn(k))
+          for (int c = 0; c < (n + 4 * kChunkQuads - 1) / (4 * kChunkQuads); ++c)
+            L.bwdTasksH[tr][lv].push_back(makeTask(kTaskDecide, c, k));
+      }
+      for (int c = 0; c < nc; ++c) {
+        while (L.recPool.size() % 4) L.recPool.push_back(0);
+        const uint32_t off = (uint32_t)(L.recPool.size() / 4);
+        L.recPool.push_back(L.nodes[u].regQ);
+        L.recPool.push_back(L.rows[u].cfvQ);
+        L.recPool.push_back((uint32_t)n | ((uint32_t)nd.na << 16) | (1u << 24) | (1u << 25));
+        L.recPool.push_back((uint32_t)c);
+        int P = 0;
+        for (int a = 0; a < nd.na; ++a) {
+          L.recPool.push_back(L.rows[child(u, a)].cfvQ);
+          P += foldedIn(child(u, a)) ? 1 : 0;
+        }
+        L.recPool.push_back((uint32_t)P);
+        for (int a = 0; a < nd.na; ++a) {
+          const int k = child(u, a);
+          if (!foldedIn(k)) continue;
+          L.recPool.push_back(L.rows[k].cfvQ);
+          L.recPool.push_back((uint32_t)t.nodes[k].nChildren);
+          for (int b = 0; b < t.nodes[k].nChildren; ++b)
+            L.recPool.push_back(L.rows[child(k, b)].cfvQ);
+        }
+        while (L.recPool.size() % 4) L.recPool.push_back(0);
+        L.bwdRecsH[tr][lv].push_back(off);
+        L.presumRecs[tr].push_back(off);
+      }
+    }
+  }
+}
+
+}  // namespace
+
 HostLayout buildLayout(const Tree& t) {
   HostLayout L;
   const int N = (int)t.nodes.size();
@@ -493,6 +632,8 @@ HostLayout buildLayout(const Tree& t) {
     w += recWords(na);
     return off;
   };
+  std::vector<uint32_t> bwdRecFirst[2] = {std::vector<uint32_t>(N, 0),
+                                          std::vector<uint32_t>(N, 0)};
   for (int u = 0; u < N; ++u) {
     const Node& nd = t.nodes[u];
     if (nd.kind != kDecide) continue;
@@ -500,6 +641,7 @@ HostLayout buildLayout(const Tree& t) {
     for (int tr = 0; tr < 2; ++tr) {
       for (int a = 0; a < nd.na; ++a) kids[a] = L.rows[t.children[nd.childBase + a]].cfvQ;
       const int nTr = t.n(u, tr);
+      bwdRecFirst[tr][u] = (uint32_t)(w / 4);
       for (int c = 0, cb = chunksOf(nTr); c < cb; ++c)
         L.bwdRecs[tr][nd.depth].push_back(
             addRecord(L.nodes[u].regQ, L.rows[u].cfvQ, nTr, nd.na, nd.player == tr, c));
@@ -520,6 +662,8 @@ HostLayout buildLayout(const Tree& t) {
   //   backward, per 128-combo chunk: [value row, n | branches << 16, chunk,
   //     branch table (16-byte units)]; the table holds per branch [child
   //     value row, parent -> child slot map (i16 pool)], once per node.
+  std::vector<std::vector<uint32_t>> chanceRecsOf[2] = {
+      std::vector<std::vector<uint32_t>>(N), std::vector<std::vector<uint32_t>>(N)};
   for (int tr = 0; tr < 2; ++tr) {
     const int opp = 1 - tr;
     L.bwdChanceRecs[tr].assign(D, {});
@@ -562,9 +706,11 @@ HostLayout buildLayout(const Tree& t) {
         L.recPool.push_back((uint32_t)chunk);
         L.recPool.push_back(it->second);
         L.bwdChanceRecs[tr][d].push_back(off);
+        chanceRecsOf[tr][u].push_back(off);
       }
     }
   }
+  buildBackwardLevels(t, L, bwdRecFirst, chanceRecsOf);
   if (N >= (1 << 24)) throw Error{PPS_GB_E_MEMORY, "tree too large for 24-bit task node ids"};
   alignU16(L.poolU16);
   return L;
@@ -633,6 +779,11 @@ uint64_t layoutDigest(const HostLayout& L) {
     f.vecs(L.fwdChance[tr]);
     f.vecs(L.fwdDecide[tr]);
     f.vec(L.termAfter[tr]);
+    f.vecs(L.bwdRecsH[tr]);
+    f.vecs(L.bwdChanceRecsH[tr]);
+    f.vecs(L.bwdTasksH[tr]);
+    f.vec(L.bwdNeed[tr]);
+    f.vec(L.presumRecs[tr]);
   }
   f.bytes(&L.maxN, sizeof L.maxN);
   f.bytes(&L.maxCardSeg, sizeof L.maxCardSeg);

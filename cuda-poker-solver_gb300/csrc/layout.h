@@ -138,6 +138,16 @@ struct HostLayout {
   std::vector<std::pair<uint32_t, int>> chanceTables[2];
   std::vector<std::vector<int>> bwdChance[2], fwdChance[2], fwdDecide[2];
   std::vector<int> termAfter[2];
+  // The staged plan's backward lists per traverser and LEVEL (see
+  // buildBackwardLevels in layout.cpp): a traverser decide node's records
+  // also compute the value rows of its opponent children, so those need no
+  // level; decide and chance record offsets, the same work as task words
+  // (byte model), per level the depths of the terminal nodes it reads (bit
+  // d), and the records with folded-in children (relocated on their own).
+  std::vector<std::vector<uint32_t>> bwdRecsH[2], bwdChanceRecsH[2];
+  std::vector<std::vector<int>> bwdTasksH[2];
+  std::vector<uint64_t> bwdNeed[2];
+  std::vector<uint32_t> presumRecs[2];
   int maxN = 0;        // largest list size (either side)
   int maxCardSeg = 0;  // longest card segment of any list
 };

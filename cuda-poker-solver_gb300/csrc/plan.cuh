@@ -212,7 +212,12 @@ void issuePlan(const std::vector<Launch>& P, const Branches& b, IssueOne&& one) 
 // only for the terminals one depth below it.
 struct HalfStep {
   std::vector<std::vector<Launch>> fwd;  // per forward level (layout.h)
-  std::vector<std::vector<Launch>> bwd;  // per depth
+  // Backward launches per level (layout.h), deepest first; bwdNeed
+  // per level: the depths (bit d) of the terminal groups its nodes read.
+  // Without bwdNeed, per depth, deepest first (each waiting for the
+  // terminals one depth below).
+  std::vector<std::vector<Launch>> bwd;
+  std::vector<uint64_t> bwdNeed;
   std::vector<Launch> sd, fd;            // per depth (count 0: none)
   // Per depth: the forward level after which its terminal groups may
   // start (-1: at the start of the half-step).
@@ -230,8 +235,11 @@ struct StagedPlan {
         if (h.sd[d].list.count) out.push_back(h.sd[d]);
         if (h.fd[d].list.count) out.push_back(h.fd[d]);
       }
-      for (size_t d = h.bwd.size(); d-- > 0;)
-        out.insert(out.end(), h.bwd[d].begin(), h.bwd[d].end());
+      if (!h.bwdNeed.empty())
+        for (const auto& set : h.bwd) out.insert(out.end(), set.begin(), set.end());
+      else
+        for (size_t d = h.bwd.size(); d-- > 0;)
+          out.insert(out.end(), h.bwd[d].begin(), h.bwd[d].end());
     }
     out.push_back(counter);
     for (Launch& l : out) l.withNext = false;
@@ -288,7 +296,7 @@ void issueStaged(const StagedPlan& P, const Branches& b, StagedEvents& ev, Issue
     GB_CK(cudaStreamWaitEvent(b.main, ev.ljoin, 0));
   };
   for (const HalfStep& h : P.half) {
-    const int D = (int)h.bwd.size(), F = (int)h.fwd.size();
+    const int D = (int)h.sd.size(), F = (int)h.fwd.size();
     ev.ensure(std::max(D, F));
     GB_CK(cudaEventRecord(ev.start, b.main));
     std::vector<char> sdOpen(D, 0), fdOpen(D, 0);
@@ -323,11 +331,19 @@ void issueStaged(const StagedPlan& P, const Branches& b, StagedEvents& ev, Issue
       for (int d = 0; d < D; ++d)
         if (afterOf(d) == lv) startTerminals(d, lv);
     }
-    for (int d = D - 1; d >= 0; --d) {
-      joinTerminals(d + 1);
-      issueSet(h.bwd[d]);
+    if (!h.bwdNeed.empty()) {
+      for (size_t lv = 0; lv < h.bwd.size(); ++lv) {
+        for (int d = 0; d < D && d < 64; ++d)
+          if ((h.bwdNeed[lv] >> d) & 1) joinTerminals(d);
+        issueSet(h.bwd[lv]);
+      }
+    } else {
+      for (int d = D - 1; d >= 0; --d) {
+        joinTerminals(d + 1);
+        issueSet(h.bwd[d]);
+      }
     }
-    joinTerminals(0);
+    for (int d = 0; d < D; ++d) joinTerminals(d);
   }
   one(P.counter, b.main);
 }
