@@ -268,6 +268,10 @@ struct SlotRec {
   // fRec / fCh are per forward level (layout.h); termAfter[tr][d]: the
   // forward level after which depth d's terminal reach rows are written.
   std::vector<int> termAfter[2];
+  // Backward per level (layout.h): records, chance records, and the
+  // terminal depths each level reads.
+  std::vector<std::vector<uint32_t>> bRecH[2], bChH[2];
+  std::vector<uint64_t> bNeed[2];
 };
 
 struct Forest::Dev {
@@ -582,6 +586,26 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
           for (int a = 0; a < na; ++a) r[4 + a] += rowOff;
         }
     }
+  // Records with folded-in children (the backward levels' own records):
+  // the header rows, the child rows and every folded-in row list.
+  for (int tr = 0; tr < 2; ++tr)
+    for (uint32_t o : L.presumRecs[tr]) {
+      uint32_t* r = &L.recPool[(size_t)o * 4];
+      const int na = (int)((r[2] >> 16) & 0xff);
+      const uint32_t cfv = (uint32_t)off[rCfv];
+      r[0] += (uint32_t)off[rReg];
+      r[1] += cfv;
+      r[3] = (r[3] & 0xffffu) | ((uint32_t)slot << 16);
+      for (int a = 0; a < na; ++a) r[4 + a] += cfv;
+      uint32_t* p = r + 4 + na;
+      const int P = (int)*p++;
+      for (int e = 0; e < P; ++e) {
+        p[0] += cfv;
+        const int m = (int)p[1];
+        for (int b = 0; b < m; ++b) p[2 + b] += cfv;
+        p += 2 + m;
+      }
+    }
   // Chance records and their branch tables: rows, maps, table offsets.
   const uint32_t recShift16 = (uint32_t)(off[rRec] / 4);
   for (int tr = 0; tr < 2; ++tr) {
@@ -646,7 +670,11 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
     rec.bCh[tr] = std::move(L.bwdChanceRecs[tr]);
     rec.fCh[tr] = std::move(L.fwdChanceRecs[tr]);
     rec.termAfter[tr] = L.termAfter[tr];
-    for (auto* lists : {&rec.bRec[tr], &rec.fRec[tr], &rec.bCh[tr], &rec.fCh[tr]})
+    rec.bRecH[tr] = std::move(L.bwdRecsH[tr]);
+    rec.bChH[tr] = std::move(L.bwdChanceRecsH[tr]);
+    rec.bNeed[tr] = L.bwdNeed[tr];
+    for (auto* lists : {&rec.bRec[tr], &rec.fRec[tr], &rec.bCh[tr], &rec.fCh[tr], &rec.bRecH[tr],
+                        &rec.bChH[tr]})
       for (auto& v : *lists)
         for (uint32_t& o : v) o += recShift;
   }
@@ -708,6 +736,8 @@ struct Lists {
   std::vector<uint32_t> recs;  // record offsets
   std::vector<ListRef> fwd[2], bwd[2], fCh[2], bCh[2], fRec[2], bRec[2], sdG, fdG;
   std::vector<int> termAfter[2];  // per depth: the latest of the spots' levels
+  std::vector<ListRef> bRecH[2], bChH[2];  // backward per level
+  std::vector<uint64_t> bNeed[2];          // per level: the union of the spots' masks
 };
 
 Lists gather(const std::map<int, SlotRec>& live, const std::vector<int>& slots, bool iteration) {
@@ -751,6 +781,19 @@ Lists gather(const std::map<int, SlotRec>& live, const std::vector<int>& slots, 
         const std::vector<int>& ta = live.at(s).termAfter[tr];
         for (int dd = 0; dd < D && dd < (int)ta.size(); ++dd)
           out.termAfter[tr][dd] = std::max(out.termAfter[tr][dd], ta[dd]);
+      }
+      // Backward levels merge by index too: each spot's level l reads only
+      // its own levels below l.
+      int H = 0;
+      for (int s : slots) H = std::max(H, (int)live.at(s).bRecH[tr].size());
+      out.bNeed[tr].assign(H, 0);
+      for (int lv = 0; lv < H; ++lv) {
+        out.bRecH[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.bRecH[tr], lv); }));
+        out.bChH[tr].push_back(catRec([&](const SlotRec& r) { return atR(r.bChH[tr], lv); }));
+        for (int s : slots) {
+          const std::vector<uint64_t>& nd = live.at(s).bNeed[tr];
+          if (lv < (int)nd.size()) out.bNeed[tr][lv] |= nd[lv];
+        }
       }
     }
     for (int dd = 0; dd < D; ++dd) {
@@ -810,12 +853,16 @@ void Forest::iterate(int n) {
       for (int dd = 0; dd < D; ++dd) {
         if (ls.sdG[dd].count) h.sd[dd] = {kSdGroup, tr, ls.sdG[dd], 0.0};
         if (ls.fdG[dd].count) h.fd[dd] = {kFdGroup, tr, ls.fdG[dd], 0.0};
-        if (ls.bRec[tr][dd].count || ls.bCh[tr][dd].count) {
-          Launch l{kBwdMix, tr, ls.bRec[tr][dd], 0.0};
-          l.list2 = ls.bCh[tr][dd];
-          h.bwd[dd].push_back(l);
-        }
       }
+      const int H = (int)ls.bRecH[tr].size();
+      h.bwd.assign(H, {});
+      h.bwdNeed = ls.bNeed[tr];
+      for (int lv = 0; lv < H; ++lv)
+        if (ls.bRecH[tr][lv].count || ls.bChH[tr][lv].count) {
+          Launch l{kBwdMix, tr, ls.bRecH[tr][lv], 0.0};
+          l.list2 = ls.bChH[tr][lv];
+          h.bwd[lv].push_back(l);
+        }
     }
     d.staged.counter = Launch{kCounter, 0, ListRef{}, 0.0};
     d.plan = d.staged.flat();
