@@ -265,28 +265,54 @@ bool BatchServer::epoch() {
   std::vector<int> due;
   for (int slot : slots)
     if (F.iterations(slot) >= nextCheck_.at(slot)) due.push_back(slot);
-  const std::vector<double> br0 = F.walkValues(due, 0, kModeBR);
-  const std::vector<double> br1 = F.walkValues(due, 1, kModeBR);
+  // Exploitability of each due spot: an f32 best-response walk screens
+  // first; a spot whose f32 value is within kScreen of its target (or that
+  // has reached max_iterations) is walked again in FP64, and only the FP64
+  // value retires it. The f32 value of the others only places their next
+  // check. (f32 rounding moves the value by ~1e-6 of the pot, far inside
+  // the factor.)
+  constexpr double kScreen = 1.5;
+  std::vector<double> expl(due.size(), 0.0), target(due.size(), 0.0);
+  std::vector<char> exact(due.size(), 0);
+  {
+    const std::vector<double> s0 = F.walkValuesF32(due, 0, kModeBR);
+    const std::vector<double> s1 = F.walkValuesF32(due, 1, kModeBR);
+    std::vector<int> close;
+    std::vector<size_t> closeAt;
+    for (size_t i = 0; i < due.size(); ++i) {
+      const int slot = due[i];
+      expl[i] = (s0[i] + s1[i] - (double)F.spot(slot).tree.spot.pot) / 2.0;
+      {
+        std::lock_guard<std::mutex> lock(m_);
+        target[i] = reqs_.at(slotTicket_.at(slot)).target;
+      }
+      if ((target[i] > 0.0 && expl[i] <= kScreen * target[i]) ||
+          F.iterations(slot) >= cfg_.maxIterations) {
+        close.push_back(slot);
+        closeAt.push_back(i);
+      }
+    }
+    const std::vector<double> br0 = F.walkValues(close, 0, kModeBR);
+    const std::vector<double> br1 = F.walkValues(close, 1, kModeBR);
+    for (size_t k = 0; k < close.size(); ++k) {
+      const size_t i = closeAt[k];
+      expl[i] = (br0[k] + br1[k] - (double)F.spot(close[k]).tree.spot.pot) / 2.0;
+      exact[i] = 1;
+    }
+  }
   std::vector<int> done;
   std::vector<double> doneExpl;
   for (size_t i = 0; i < due.size(); ++i) {
     const int slot = due[i];
-    const CompiledSpot& cs = F.spot(slot);
-    const double expl = (br0[i] + br1[i] - (double)cs.tree.spot.pot) / 2.0;
-    double target;
-    {
-      std::lock_guard<std::mutex> lock(m_);
-      target = reqs_.at(slotTicket_.at(slot)).target;
-    }
     const int t = F.iterations(slot);
-    if ((target > 0.0 && expl <= target) || t >= cfg_.maxIterations) {
+    if (exact[i] && ((target[i] > 0.0 && expl[i] <= target[i]) || t >= cfg_.maxIterations)) {
       done.push_back(slot);
-      doneExpl.push_back(expl);
+      doneExpl.push_back(expl[i]);
       continue;
     }
     int step = cfg_.checkEvery;
-    if (!cfg_.fixedChecks && target > 0.0 && expl > 0.0) {
-      const double want = (double)t * std::sqrt(expl / target) - (double)t;
+    if (!cfg_.fixedChecks && target[i] > 0.0 && expl[i] > 0.0) {
+      const double want = (double)t * std::sqrt(expl[i] / target[i]) - (double)t;
       const int s = (int)std::ceil(std::max(want, 1.0) / kCheckStep) * kCheckStep;
       step = std::min(cfg_.checkEvery, std::max(kCheckStep, s));
     }

@@ -209,7 +209,8 @@ struct RootInfo {
 
 // Root value of each listed spot: sum_j w[j] * cfv[j] in a fixed order
 // (one CTA per spot, strided partial sums, then a tree reduction).
-__global__ void __launch_bounds__(128) rootValueK(const double* __restrict__ cfv,
+template <typename T>
+__global__ void __launch_bounds__(128) rootValueK(const T* __restrict__ cfv,
                                                   const double* __restrict__ w,
                                                   const RootInfo* __restrict__ info,
                                                   double* __restrict__ out) {
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(128) rootValueK(const double* __restrict__ cfv
   const RootInfo r = info[blockIdx.x];
   double acc = 0.0;
   for (int j = threadIdx.x; j < r.n; j += blockDim.x)
-    acc += w[r.wOff + j] * cfv[(size_t)r.cfvQ * 4 + j];
+    acc += w[r.wOff + j] * (double)cfv[(size_t)r.cfvQ * 4 + j];
   part[threadIdx.x] = acc;
   __syncthreads();
   for (int s = 64; s > 0; s >>= 1) {
@@ -922,6 +923,17 @@ double Forest::lastIterateMs() {
 }
 
 std::vector<double> Forest::walkValues(const std::vector<int>& slots, int tr, int mode) {
+  return walk<double>(slots, tr, mode);
+}
+
+// The same walk with f32 rows: the iteration's own reach and value rows
+// serve as its scratch (every iteration rewrites them before reading).
+std::vector<double> Forest::walkValuesF32(const std::vector<int>& slots, int tr, int mode) {
+  return walk<float>(slots, tr, mode);
+}
+
+template <typename T>
+std::vector<double> Forest::walk(const std::vector<int>& slots, int tr, int mode) {
   Dev& d = *d_;
   std::vector<double> out(slots.size(), 0.0);
   if (slots.empty()) return out;
@@ -931,21 +943,23 @@ std::vector<double> Forest::walkValues(const std::vector<int>& slots, int tr, in
     GB_CK(cudaMemcpyAsync(d.wTasks, ls.all.data(), ls.all.size() * sizeof(int),
                           cudaMemcpyHostToDevice, d.stream));
   const int maxN = d.maxN(slots);
-  const size_t smem = bwdScratchBytes<double>(maxN);
-  raiseSmemLimit((const void*)bwdLevelK<double>, smem);
+  const size_t smem = bwdScratchBytes<T>(maxN);
+  raiseSmemLimit((const void*)bwdLevelK<T>, smem);
   const DevTree tree = d.tree();
-  const DevRows<double> rows = d.rows<double>(aReachD0, aReachD1, aCfvD);
+  const bool f64 = sizeof(T) == 8;
+  const DevRows<T> rows = f64 ? d.rows<T>(aReachD0, aReachD1, aCfvD)
+                              : d.rows<T>(aReachF0, aReachF1, aCfvF);
   const int D = (int)ls.fwd[tr].size();
   for (int dd = 0; dd < D; ++dd) {
     const ListRef a = ls.fwd[tr][dd];
     if (a.count)
-      fwdLevelK<double><<<gridOf(a.count), kThreads, 0, d.stream>>>(tree, rows, d.wTasks + a.off,
-                                                                   a.count, tr, 1);
+      fwdLevelK<T><<<gridOf(a.count), kThreads, 0, d.stream>>>(tree, rows, d.wTasks + a.off,
+                                                              a.count, tr, 1);
   }
   for (int dd = D - 1; dd >= 0; --dd) {
     const ListRef b = ls.bwd[tr][dd];
     if (b.count)
-      bwdLevelK<double><<<gridOf(b.count), kThreads, smem, d.stream>>>(
+      bwdLevelK<T><<<gridOf(b.count), kThreads, smem, d.stream>>>(
           tree, rows, d.wTasks + b.off, b.count, tr, mode, maxN);
   }
   std::vector<RootInfo> info(slots.size());
@@ -960,9 +974,9 @@ std::vector<double> Forest::walkValues(const std::vector<int>& slots, int tr, in
   ensureBuf(d.vals, d.valsCap, info.size());
   GB_CK(cudaMemcpyAsync(d.info, info.data(), info.size() * sizeof(RootInfo),
                         cudaMemcpyHostToDevice, d.stream));
-  rootValueK<<<(unsigned)info.size(), 128, 0, d.stream>>>(
-      static_cast<const double*>(d.arr[aCfvD]), static_cast<const double*>(d.arr[aW]), d.info,
-      d.vals);
+  rootValueK<T><<<(unsigned)info.size(), 128, 0, d.stream>>>(
+      static_cast<const T*>(d.arr[f64 ? aCfvD : aCfvF]), static_cast<const double*>(d.arr[aW]),
+      d.info, d.vals);
   GB_CK(cudaGetLastError());
   GB_CK(cudaMemcpyAsync(out.data(), d.vals, out.size() * sizeof(double), cudaMemcpyDeviceToHost,
                         d.stream));

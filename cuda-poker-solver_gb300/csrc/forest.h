@@ -66,6 +66,9 @@ class Forest {
   // One FP64 walk (kModeEV or kModeBR) of traverser tr over `slots`;
   // returns each spot's root value divided by its pair mass (chips).
   std::vector<double> walkValues(const std::vector<int>& slots, int tr, int mode);
+  // The same values from an f32 walk (a screen: rounding of the f32 rows,
+  // about 1e-6 of the values).
+  std::vector<double> walkValuesF32(const std::vector<int>& slots, int tr, int mode);
   // Cumulative strategy rows of each spot's root decide node (na x n,
   // dense; empty where the root is not a decision), copied in one batch.
   std::vector<std::vector<float>> rootRows(const std::vector<int>& slots);
@@ -80,6 +83,8 @@ class Forest {
 
  private:
   std::unique_ptr<Dev> d_;
+  template <typename T>
+  std::vector<double> walk(const std::vector<int>& slots, int tr, int mode);
 };
 
 }  // namespace gb
