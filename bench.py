@@ -551,8 +551,13 @@ def main():
                 "avg_launch_us": 1000.0 * pms / launches, "peak_source": peak_kind,
                 "iteration_gbs": (sum(v[2] for v in prof.values()) / min(args.steps, 20)) *
                                  (value / world) / 1e9,
-                "profile": {k: {"launches": v[0], "ms": v[1], "algo_bytes": v[2]}
-                            for k, v in prof.items()}}
+                "profile": {k: {"launches": v[0], "ms": v[1], "algo_bytes": v[2],
+                                "achieved_gbs": (v[2] / v[0]) / (v[1] / v[0] / 1000.0) / 1e9
+                                if v[0] and v[1] > 0 else None,
+                                "frac": (v[2] / v[1] * 1000.0 / 1e9) / peak if v[1] > 0 else None}
+                            for k, v in prof.items()},
+                "iteration_frac": None}
+    roofline["iteration_frac"] = roofline["iteration_gbs"] / peak
     batched = None
     if args.batch_spots > 0:
         spots = wl.batched(args.batch_spots)

@@ -200,10 +200,11 @@ def test_served_requests_overlap_and_match(mixed):
     spots, (res, _, _) = mixed
     b = pps.Batch(check_every=CHECK, max_iterations=1024)
     b.start()
-    tickets = []
-    for sp in spots:
-        tickets.append(_submit(b, sp))
-        time.sleep(0.01)
+    # Submitted while the serving thread runs, back to back: they are
+    # compiled on host threads and admitted as they become ready, so several
+    # share the device (a spacing between requests would let fast spots
+    # finish alone).
+    tickets = [_submit(b, sp) for sp in spots]
     got = [b.wait(t, timeout=300) for t in tickets]
     info = b.info()
     b.stop()
