@@ -70,7 +70,7 @@ struct Engine::Dev {
   std::vector<ListRef> bCh[2], fCh[2];       // its chance word lists
   std::vector<ListRef> bRec[2], fRec[2];     // its decide record lists (into recTasks)
   std::vector<ListRef> bRecH[2], bChH[2];    // backward per level (the staged plan)
-  int4* groups = nullptr;
+  GroupRec* groups = nullptr;
   uint32_t* recs = nullptr;
   uint32_t* recTasks = nullptr;
   float* stratLo = nullptr;  // low words of the strategy rows (compensated sums)
@@ -193,7 +193,7 @@ Engine::Engine(const Tree& t, HostLayout&& layout)
   d.recTasks = upload(d, recTasks, B, h2d_);
   d.tasks = upload(d, all, B, h2d_);
   d.hostTasks = all;
-  d.groups = reinterpret_cast<int4*>(upload(d, L_.groups, B, h2d_));
+  d.groups = reinterpret_cast<GroupRec*>(upload(d, L_.groupRecs, B, h2d_));
 
   d.maxN = L_.maxN;
   d.smemF = bwdScratchBytes<float>(d.maxN);

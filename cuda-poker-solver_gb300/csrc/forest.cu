@@ -61,7 +61,7 @@ const ArrayDef kArray[kArrays] = {
     {rReg, 16},               {rReg, 16},                 {rCfv, 16},
     {rCfv, 32},               {rReach0, 16},              {rReach0, 32},
     {rReach1, 16},            {rReach1, 32},              {rW, 8},
-    {rGroup, sizeof(TermGroup)}, {rRec, sizeof(uint32_t)}};
+    {rGroup, 2 * sizeof(GroupRec)}, {rRec, sizeof(uint32_t)}};
 
 size_t roundUp(size_t n, size_t g) { return (n + g - 1) / g * g; }
 
@@ -569,10 +569,25 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   put(aU16, off[rU16], L.poolU16.data(), L.poolU16.size() * 2);
   put(aI16, off[rI16], L.poolI16.data(), L.poolI16.size() * 2);
   put(aSd, off[rSd], L.poolSd.data(), L.poolSd.size() * sizeof(ShowdownInfo));
-  for (TermGroup& g : L.groups)
-    for (int& u : g.node)
-      if (u >= 0) u += (int)off[rNode];
-  put(aGroups, off[rGroup], L.groups.data(), L.groups.size() * sizeof(TermGroup));
+  // Group records (two per group, one per traverser): table offsets into
+  // the pools, the nodes' rows.
+  for (size_t k = 0; k < L.groupRecs.size(); ++k) {
+    GroupRec& g = L.groupRecs[k];
+    const int tr = (int)(k & 1);
+    g.tabOff += (int)off[rU16];
+    if (g.kind == kTaskShowdown) {
+      g.infoOff += (int)off[rSd];
+    } else {
+      g.infoOff += (int)off[rU8];
+      g.sameOff += (int)off[rI16];
+    }
+    for (int j = 0; j < 4; ++j)
+      if ((g.mask >> j) & 1) {
+        g.reachQ[j] += (uint32_t)off[tr ? rReach1 : rReach0];
+        g.cfvQ[j] += (uint32_t)off[rCfv];
+      }
+  }
+  put(aGroups, off[rGroup], L.groupRecs.data(), L.groupRecs.size() * sizeof(GroupRec));
   // Decide records: row offsets into the pools, the spot's counter slot.
   for (int tr = 0; tr < 2; ++tr)
     for (int fwd = 0; fwd < 2; ++fwd) {
@@ -695,6 +710,7 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   L.poolSd = {};
   L.states = {};
   L.groups = {};
+  L.groupRecs = {};
   L.recPool = {};
   d.used += s->bytes;
   rec.spot = std::move(s);
@@ -882,7 +898,7 @@ void Forest::iterate(int n) {
     }
     const PlanArgs args{d.tree(), d.rows<float>(aReachF0, aReachF1, aCfvF), d.tasks, d.counter,
                         (int)d.counterCap, maxN, bwdScratchBytes<float>(maxN),
-                        static_cast<const int4*>(d.arr[aGroups]), smemSd, smemFd,
+                        static_cast<const GroupRec*>(d.arr[aGroups]), smemSd, smemFd,
                         static_cast<const uint32_t*>(d.arr[aRecs]), d.recTasks, shape};
     GB_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
     issueStaged(d.staged, d.br, d.sev,

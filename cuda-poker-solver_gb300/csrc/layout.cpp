@@ -550,6 +550,38 @@ HostLayout buildLayout(const Tree& t) {
     if (job < 2) taskLists(job);
     else termGroups();
   });
+  // Group records: what each traverser's group kernels read of the nodes,
+  // their state and their rows (layout.h GroupRec).
+  L.groupRecs.assign(L.groups.size() * 2, GroupRec{});
+  for (size_t gi = 0; gi < L.groups.size(); ++gi) {
+    const TermGroup& g = L.groups[gi];
+    const int kind = t.nodes[g.node[0]].kind == kShowdown ? kTaskShowdown : kTaskFold;
+    const StateDev& st = L.states[L.nodes[g.node[0]].state];
+    for (int tr = 0; tr < 2; ++tr) {
+      GroupRec& r = L.groupRecs[gi * 2 + tr];
+      const int opp = 1 - tr;
+      r.no = st.n[opp];
+      r.nt = st.n[tr];
+      r.kind = kind;
+      if (kind == kTaskShowdown) {
+        r.tabOff = st.sdOff[tr];
+        r.infoOff = st.sdInfoOff[tr];
+        r.sameOff = -1;
+      } else {
+        r.tabOff = st.csrOff[opp];
+        r.infoOff = st.cardsOff[tr];
+        r.sameOff = st.sameOff[tr];
+      }
+      for (int k = 0; k < 4; ++k) {
+        const int u = g.node[k];
+        if (u < 0) continue;
+        r.mask |= 1 << k;
+        r.reachQ[k] = L.rows[u].reachQ[tr];
+        r.cfvQ[k] = L.rows[u].cfvQ;
+        for (int j = 0; j < 4; ++j) r.val[k][j] = L.termVal[((size_t)u * 2 + tr) * 4 + j];
+      }
+    }
+  }
   // Forward levels (see layout.h): level of a forward-working node = one
   // more than its nearest forward-working ancestor's (0 without one); the
   // nodes are in DFS pre-order, so parents come first.
@@ -763,6 +795,7 @@ uint64_t layoutDigest(const HostLayout& L) {
     f.vecs(L.innerTasks[tr]);
   }
   f.vec(L.groups);
+  f.vec(L.groupRecs);
   f.vecs(L.sdGroupTasks);
   f.vecs(L.fdGroupTasks);
   f.vec(L.recPool);

@@ -93,6 +93,25 @@ struct alignas(16) TermGroup {
   int node[4];
 };
 
+// A terminal group as one traverser's kernels read it: the state's list
+// sizes and table offsets, the four nodes' rows and payoffs, so that a group
+// CTA reaches its tables and rows one dependent load after its task word
+// (instead of group -> node -> state -> tables and node -> row -> data).
+// Records are stored per group and traverser, at 2 group + tr.
+struct alignas(16) GroupRec {
+  int no, nt;          // opponent / traverser list sizes
+  int tabOff;          // u16 pool: showdown sdOff[tr]; fold csrOff[opp]
+  int infoOff;         // showdown: sdInfoOff[tr] (showdown pool); fold: cardsOff[tr] (u8 pool)
+  int sameOff;         // fold: sameOff[tr] (i16 pool); showdown: -1
+  int mask;            // bit k: node slot k holds a node
+  int kind;            // kTaskShowdown or kTaskFold
+  int pad;
+  uint32_t reachQ[4];  // opponent reach row of each node, in tr's layout (quads)
+  uint32_t cfvQ[4];    // value rows (quads)
+  float val[4][4];     // payoffs per node: showdown (win, tie, lose, 0), fold (v, 0, 0, 0)
+};
+static_assert(sizeof(GroupRec) == 128, "group records are one 128-byte line");
+
 struct HostLayout {
   std::vector<NodeDev> nodes;
   std::vector<RowDev> rows;
@@ -116,6 +135,7 @@ struct HostLayout {
   // (node field = index into `groups`; the same for both traversers) and
   // the chance + decide tasks per traverser and depth.
   std::vector<TermGroup> groups;
+  std::vector<GroupRec> groupRecs;  // per group and traverser, at 2 group + tr
   std::vector<std::vector<int>> sdGroupTasks, fdGroupTasks;
   std::vector<std::vector<int>> innerTasks[2];
   // Decide records (decide.cuh) of the default iteration: the pool, per

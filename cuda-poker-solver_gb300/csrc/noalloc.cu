@@ -220,7 +220,7 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
                oStates = A.take(bytesOf(L.states)), oU8 = A.take(bytesOf(L.poolU8)),
                oU16 = A.take(bytesOf(L.poolU16)), oI16 = A.take(bytesOf(L.poolI16)),
                oSd = A.take(bytesOf(L.poolSd)), oTasks = A.take(bytesOf(tasks)),
-               oGroups = A.take(bytesOf(L.groups)),
+               oGroups = A.take(bytesOf(L.groupRecs)),
                oMap = A.take(bytesOf(rowMap)), oReg = A.take(L.regQuads * 16),
                oStr = A.take(L.regQuads * 16), oCfv = A.take(L.cfvQuads * 16),
                oReach0 = A.take(L.reachQuads[0] * 16), oReach1 = A.take(L.reachQuads[1] * 16),
@@ -248,7 +248,7 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
   put(oI16, L.poolI16);
   put(oSd, L.poolSd);
   put(oTasks, tasks);
-  put(oGroups, L.groups);
+  put(oGroups, L.groupRecs);
   put(oMap, rowMap);
   put(oCoef, coef);
   put(oReach0, rootReach[0]);
@@ -292,7 +292,7 @@ int64_t noallocSolve(const gpu::PostflopSpot& spot, const pf::BetConfig& cfg, fl
   rows.cfv = reinterpret_cast<float*>(base + oCfv);
   const int* dTasks = reinterpret_cast<const int*>(base + oTasks);
 
-  const int4* groups = reinterpret_cast<const int4*>(base + oGroups);
+  const GroupRec* groups = reinterpret_cast<const GroupRec*>(base + oGroups);
   const size_t smemSd = sdGroupSmem(L.maxN), smemFd = fdGroupSmem(L.maxN);
   raiseGroupSmem(L.maxN);
   auto grid = [](int count) { return (unsigned)std::min(count, 1 << 20); };

@@ -67,7 +67,7 @@ struct PlanArgs {
   int spots;    // counters advanced per iteration
   int maxN;     // largest combo list (shared scratch layout)
   size_t smem;  // bwdScratchBytes<float>(maxN)
-  const int4* groups;     // terminal groups (TermGroup)
+  const GroupRec* groups;  // terminal group records (2 group + traverser)
   size_t smemSd, smemFd;  // sdGroupSmem / fdGroupSmem(maxN)
   const uint32_t* recs;      // decide record pool
   const uint32_t* recTasks;  // record offsets (the record and chance lists index these)

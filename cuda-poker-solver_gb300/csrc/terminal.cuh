@@ -72,6 +72,38 @@ __device__ __forceinline__ float comp4(float4 v, int g) {
   return g == 0 ? v.x : g == 1 ? v.y : g == 2 ? v.z : v.w;
 }
 
+// The group record as the kernels read it: every thread loads the header
+// (list sizes, table offsets) and the reach rows, which the staging needs,
+// in one round trip after the task word; threads 0-7 copy the whole record
+// to shared memory on the way, and what is read after the first barrier
+// (value rows, payoffs, the showdown table offset) comes from that copy
+// instead of occupying registers through the table builds.
+struct GroupHead {
+  int no, nt, tabOff, infoOff, sameOff, mask;
+  uint4 reachQ;
+};
+static __device__ __forceinline__ GroupHead loadGroupHead(const GroupRec* g, GroupRec* copy) {
+  const uint4* w = reinterpret_cast<const uint4*>(g);
+  const uint4 h0 = w[0], h1 = w[1];
+  GroupHead h;
+  h.no = (int)h0.x;
+  h.nt = (int)h0.y;
+  h.tabOff = (int)h0.z;
+  h.infoOff = (int)h0.w;
+  h.sameOff = (int)h1.x;
+  h.mask = (int)h1.y;
+  h.reachQ = w[2];
+  if (threadIdx.x < sizeof(GroupRec) / 16)
+    reinterpret_cast<uint4*>(copy)[threadIdx.x] = w[threadIdx.x];
+  return h;
+}
+static __device__ __forceinline__ uint4 cfvQOf(const GroupRec* c) {
+  return *reinterpret_cast<const uint4*>(c->cfvQ);
+}
+static __device__ __forceinline__ float4 valOf(const GroupRec* c, int k) {
+  return *reinterpret_cast<const float4*>(c->val[k]);
+}
+
 // ---- shared-memory layout of a group task (maxN: largest list) ----
 // The sorted prefix gives each thread kSpan consecutive positions, so one
 // pass of kTermThreads threads covers every list (kSpan * 256 >= 1327), and
@@ -95,22 +127,25 @@ constexpr int kGroupBlocks = kTermThreads / 32 + 1;  // warp blocks + the total
 // the staged (transposed, unsorted) reach rows, then the sorted prefixes.
 __host__ __device__ inline size_t sdGroupSmem(int maxN) {
   return (size_t)groupTabEntries(maxN) * 2 +
-         16 * ((size_t)groupPrefixEntries(maxN) + groupXEntries(maxN) + 3 * kGroupBlocks);
+         16 * ((size_t)groupPrefixEntries(maxN) + groupXEntries(maxN) + 3 * kGroupBlocks) +
+         sizeof(GroupRec);
 }
-// Fold groups: tab | rs4 | cs4[53] | card pairs (u16) | identical-combo slots (i16).
+// Fold groups: tab | rs4 | cs4[53] | card pairs (u16) | identical-combo
+// slots (i16) | group tail.
 __host__ __device__ inline size_t fdGroupSmem(int maxN) {
   return (size_t)groupTabEntries(maxN) * 2 + 16 * ((size_t)groupRowEntries(maxN) + 53) +
-         (size_t)4 * ((maxN + 7) / 8 * 8);
+         (size_t)4 * ((maxN + 7) / 8 * 8) + sizeof(GroupRec);
 }
 
 // Stages the group's opponent reach rows transposed: rs4[pad8(j)] holds
 // entry j of the four rows (0 for an absent node).
-static __device__ __forceinline__ void stageRows4(float4* rs4, const DevTree& t, const DevRows<float>& rows,
-                                           const int (&u)[4], int tr, int no) {
+static __device__ __forceinline__ void stageRows4(float4* rs4, const DevRows<float>& rows,
+                                                  int mask, uint4 reachQ, int tr, int no) {
+  const uint32_t q[4] = {reachQ.x, reachQ.y, reachQ.z, reachQ.w};
   const float* r[4];
 #pragma unroll
   for (int g = 0; g < 4; ++g)
-    r[g] = u[g] >= 0 ? rows.reach[tr] + (size_t)t.rows[u[g]].reachQ[tr] * 4 : nullptr;
+    r[g] = (mask >> g) & 1 ? rows.reach[tr] + (size_t)q[g] * 4 : nullptr;
   for (int q = threadIdx.x; q < quadsOf(no); q += blockDim.x) {
     float4 v[4];
 #pragma unroll
@@ -125,12 +160,14 @@ static __device__ __forceinline__ void stageRows4(float4* rs4, const DevTree& t,
 }
 
 // Value rows of the group's nodes (nullptr for an absent node).
-static __device__ __forceinline__ void outRows4(float* (&out)[4], const DevTree& t,
-                                                const DevRows<float>& rows, const int (&u)[4]) {
+static __device__ __forceinline__ void outRows4(float* (&out)[4], const DevRows<float>& rows,
+                                                int mask, uint4 cfvQ) {
+  const uint32_t q[4] = {cfvQ.x, cfvQ.y, cfvQ.z, cfvQ.w};
 #pragma unroll
-  for (int g = 0; g < 4; ++g)
-    out[g] = u[g] >= 0 ? rows.cfv + (size_t)t.rows[u[g]].cfvQ * 4 : nullptr;
+  for (int g = 0; g < 4; ++g) out[g] = (mask >> g) & 1 ? rows.cfv + (size_t)q[g] * 4 : nullptr;
 }
+
+
 static __device__ __forceinline__ void storeOut4(float* const (&out)[4], int i, float4 c) {
   if (out[0]) out[0][i] = c.x;
   if (out[1]) out[1][i] = c.y;
@@ -138,12 +175,8 @@ static __device__ __forceinline__ void storeOut4(float* const (&out)[4], int i, 
   if (out[3]) out[3][i] = c.w;
 }
 
-static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& rows, const int (&u)[4],
-                              int tr, unsigned char* smem, int maxN) {
-  const NodeDev nd = t.nodes[u[0]];
-  const StateDev& st = t.states[nd.state];
-  const int opp = 1 - tr;
-  const int no = st.n[opp], nt = st.n[tr];
+static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& rows,
+                                     const GroupRec* grec, int tr, unsigned char* smem, int maxN) {
   uint16_t* tab = reinterpret_cast<uint16_t*>(smem);
   float4* P4 = reinterpret_cast<float4*>(smem + (size_t)groupTabEntries(maxN) * 2);
   float4* rs4 = P4;  // staged rows until the prefixes replace them
@@ -151,14 +184,19 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   float4* W4 = X4 + groupXEntries(maxN);
   float* BH = reinterpret_cast<float*>(W4 + kGroupBlocks);  // [warp block][4]
   float* BL = BH + 4 * kGroupBlocks;
+  GroupRec* rc = reinterpret_cast<GroupRec*>(W4 + 3 * kGroupBlocks);
+  {
+    const GroupHead gh = loadGroupHead(grec, rc);
+    stageTab(tab, t.poolU16 + gh.tabOff, 3 * gh.no + 53);
+    stageRows4(rs4, rows, gh.mask, gh.reachQ, tr, gh.no);
+  }
+  __syncthreads();
+  // From here on the record's words come from the shared copy.
+  const int no = rc->no, nt = rc->nt;
   const uint16_t* ord = tab;
   const uint16_t* seg = ord + no;
   const uint16_t* segSlot = seg + 53;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-
-  stageTab(tab, t.poolU16 + st.sdOff[tr], 3 * no + 53);
-  stageRows4(rs4, t, rows, u, tr, no);
-  __syncthreads();
 
   // Card segments, four cards per warp (8 lanes x 8 entries per card):
   // X4[pad8(seg[c] + c + k)] = reach of the card's first k entries, k = 0..len.
@@ -237,26 +275,17 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
 
   const float4* BH4 = reinterpret_cast<const float4*>(BH);
   const float4* BL4 = reinterpret_cast<const float4*>(BL);
-  float4 win4 = zero4(), tie4 = zero4(), lose4 = zero4();
-  {
-    float w[4] = {0.f, 0.f, 0.f, 0.f}, ti[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-    for (int g = 0; g < 4; ++g)
-      if (u[g] >= 0) {
-        const float* tv = t.termVal + ((size_t)u[g] * 2 + tr) * 4;
-        w[g] = tv[0];
-        ti[g] = tv[1];
-        lo[g] = tv[2];
-      }
-    win4 = make_float4(w[0], w[1], w[2], w[3]);
-    tie4 = make_float4(ti[0], ti[1], ti[2], ti[3]);
-    lose4 = make_float4(lo[0], lo[1], lo[2], lo[3]);
-  }
-  const ShowdownInfo* info = t.poolSd + st.sdInfoOff[tr];
+  // Payoffs of the four nodes (zero for an absent node: the record's
+  // padding slots hold zeros).
+  const float4 v0 = valOf(rc, 0), v1 = valOf(rc, 1), v2 = valOf(rc, 2), v3 = valOf(rc, 3);
+  const float4 win4 = make_float4(v0.x, v1.x, v2.x, v3.x);
+  const float4 tie4 = make_float4(v0.y, v1.y, v2.y, v3.y);
+  const float4 lose4 = make_float4(v0.z, v1.z, v2.z, v3.z);
+  const ShowdownInfo* info = t.poolSd + rc->infoOff;
   const int bn = no >> kSpanShift;
   const float4 TH = BH4[bn], TL = BL4[bn], Pno = P4[pad8(no)];
   float* out[4];
-  outRows4(out, t, rows, u);
+  outRows4(out, rows, rc->mask, cfvQOf(rc));
   const int nt4 = quadsOf(nt) * 4;
 #pragma unroll 2
   for (int i = threadIdx.x; i < nt4; i += blockDim.x) {
@@ -291,24 +320,23 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   }
 }
 
-static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, const int (&u)[4], int tr,
-                          unsigned char* smem, int maxN) {
-  const NodeDev nd = t.nodes[u[0]];
-  const StateDev& st = t.states[nd.state];
-  const int opp = 1 - tr;
-  const int no = st.n[opp], nt = st.n[tr];
+static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, const GroupRec* grec,
+                                 int tr, unsigned char* smem, int maxN) {
   uint16_t* csr = reinterpret_cast<uint16_t*>(smem);
   float4* rs4 = reinterpret_cast<float4*>(smem + (size_t)groupTabEntries(maxN) * 2);
   float4* cs4 = rs4 + groupRowEntries(maxN);  // [52] card sums, [52] total
   uint16_t* cardsS = reinterpret_cast<uint16_t*>(cs4 + 53);
   int16_t* sameS = reinterpret_cast<int16_t*>(cardsS + (maxN + 7) / 8 * 8);
+  GroupRec* rc = reinterpret_cast<GroupRec*>(sameS + (maxN + 7) / 8 * 8);
+  const GroupHead gh = loadGroupHead(grec, rc);
+  const int no = gh.no, nt = gh.nt;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 
-  stageTab(csr, t.poolU16 + st.csrOff[opp], 53 + 2 * no);
-  stageRows4(rs4, t, rows, u, tr, no);
+  stageTab(csr, t.poolU16 + gh.tabOff, 53 + 2 * no);
+  stageRows4(rs4, rows, gh.mask, gh.reachQ, tr, no);
   {  // the traverser's card pairs and identical-combo slots
-    const uint16_t* cards = reinterpret_cast<const uint16_t*>(t.poolU8 + st.cardsOff[tr]);
-    const int16_t* same = t.poolI16 + st.sameOff[tr];
+    const uint16_t* cards = reinterpret_cast<const uint16_t*>(t.poolU8 + gh.infoOff);
+    const int16_t* same = t.poolI16 + gh.sameOff;
     for (int i = threadIdx.x; i < nt; i += blockDim.x) {
       cardsS[i] = cards[i];
       sameS[i] = same[i];
@@ -341,12 +369,9 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
   }
   __syncthreads();
   const float4 tot = cs4[52];
-  float v[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-  for (int g = 0; g < 4; ++g)
-    if (u[g] >= 0) v[g] = t.termVal[((size_t)u[g] * 2 + tr) * 4];
+  const float4 pay = make_float4(rc->val[0][0], rc->val[1][0], rc->val[2][0], rc->val[3][0]);
   float* out[4];
-  outRows4(out, t, rows, u);
+  outRows4(out, rows, rc->mask, cfvQOf(rc));
   const int nt4 = quadsOf(nt) * 4;
 #pragma unroll 2
   for (int i = threadIdx.x; i < nt4; i += blockDim.x) {
@@ -358,7 +383,7 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
     float4 w = tot - cs4[cp & 0xff] - cs4[cp >> 8];
     if (sm >= 0) w += rs4[pad8(sm)];
     w = max0(w);
-    storeOut4(out, i, mul4(w, make_float4(v[0], v[1], v[2], v[3])));
+    storeOut4(out, i, mul4(w, pay));
   }
 }
 
@@ -384,26 +409,22 @@ constexpr int fdMinBlocks(int kT) { return (kT == kTermThreads ? 6 : 5) * kTermT
 
 template <int kT>
 static __global__ void __launch_bounds__(kT, sdMinBlocks(kT))
-sdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
+sdGroupK(DevTree t, DevRows<float> rows, const GroupRec* __restrict__ groups,
          const int* __restrict__ tasks, int count, int tr, int maxN) {
   extern __shared__ __align__(16) unsigned char smem[];
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
-    const int4 g = groups[(unsigned)tasks[i] >> 8];
-    const int u[4] = {g.x, g.y, g.z, g.w};
-    showdownGroup(t, rows, u, tr, smem, maxN);
+    showdownGroup(t, rows, groups + 2 * ((unsigned)tasks[i] >> 8) + tr, tr, smem, maxN);
     __syncthreads();  // the next task reuses the shared memory
   }
 }
 
 template <int kT>
 static __global__ void __launch_bounds__(kT, fdMinBlocks(kT))
-fdGroupK(DevTree t, DevRows<float> rows, const int4* __restrict__ groups,
+fdGroupK(DevTree t, DevRows<float> rows, const GroupRec* __restrict__ groups,
          const int* __restrict__ tasks, int count, int tr, int maxN) {
   extern __shared__ __align__(16) unsigned char smem[];
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
-    const int4 g = groups[(unsigned)tasks[i] >> 8];
-    const int u[4] = {g.x, g.y, g.z, g.w};
-    foldGroup(t, rows, u, tr, smem, maxN);
+    foldGroup(t, rows, groups + 2 * ((unsigned)tasks[i] >> 8) + tr, tr, smem, maxN);
     __syncthreads();
   }
 }
@@ -434,7 +455,7 @@ constexpr int kFusedMaxN = kSpan * kThreads - 1;  // widest list of a 128-thread
 static __global__ void __launch_bounds__(kThreads, 6)
 bwdLevelFusedK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
                const uint32_t* __restrict__ recTasks, int nRec, const uint32_t* __restrict__ chance,
-               int nCh, const int4* __restrict__ groups, const int* __restrict__ sd, int nSd,
+               int nCh, const GroupRec* __restrict__ groups, const int* __restrict__ sd, int nSd,
                const int* __restrict__ fd, int nFd, int tr, int maxN, int termWait) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = (int)threadIdx.x & 31;
@@ -463,15 +484,14 @@ bwdLevelFusedK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs
       __syncthreads();  // the next task reuses the shared memory
     } else {
       const bool show = i < e3;
-      const int4 g = groups[(unsigned)(show ? sd[i - e2] : fd[i - e3]) >> 8];
-      const int u[4] = {g.x, g.y, g.z, g.w};
+      const GroupRec* g = groups + 2 * ((unsigned)(show ? sd[i - e2] : fd[i - e3]) >> 8) + tr;
       if (groupsWait) {
         pdlWait();
         waited = true;
       }
       pdlTrigger();
-      if (show) showdownGroup(t, rows, u, tr, smem, maxN);
-      else foldGroup(t, rows, u, tr, smem, maxN);
+      if (show) showdownGroup(t, rows, g, tr, smem, maxN);
+      else foldGroup(t, rows, g, tr, smem, maxN);
       __syncthreads();
       continue;
     }
@@ -487,7 +507,7 @@ void raiseSmemLimit(const void* kernel, size_t bytes);
 
 // Launches one level's showdown (fold) groups with the CTA size of maxN.
 static inline void launchSdGroups(unsigned grid, size_t smem, cudaStream_t s, const DevTree& t,
-                                  const DevRows<float>& rows, const int4* groups,
+                                  const DevRows<float>& rows, const GroupRec* groups,
                                   const int* tasks, int count, int tr, int maxN) {
   switch (termThreadsFor(maxN)) {
     case 64: sdGroupK<64><<<grid, 64, smem, s>>>(t, rows, groups, tasks, count, tr, maxN); break;
@@ -498,7 +518,7 @@ static inline void launchSdGroups(unsigned grid, size_t smem, cudaStream_t s, co
   }
 }
 static inline void launchFdGroups(unsigned grid, size_t smem, cudaStream_t s, const DevTree& t,
-                                  const DevRows<float>& rows, const int4* groups,
+                                  const DevRows<float>& rows, const GroupRec* groups,
                                   const int* tasks, int count, int tr, int maxN) {
   switch (termThreadsFor(maxN)) {
     case 64: fdGroupK<64><<<grid, 64, smem, s>>>(t, rows, groups, tasks, count, tr, maxN); break;
