@@ -9,8 +9,9 @@
 // nodes. The per-node formulas are those of showdownNode / foldNode
 // (kernels.cuh; the reference's cuda/gpu_cfr.cu:355-406 and 433-454):
 //   showdown: win / tie / lose masses from an exclusive prefix of the
-//     strength-sorted opponent reach (blocks of 128 positions, block
-//     totals accumulated compensated, as (hi, lo) pairs), minus the
+//     strength-sorted opponent reach (warp blocks of 256 positions, block
+//     totals accumulated compensated, as (hi, lo) pairs, the lo word
+//     folded into the block's position prefixes), minus the
 //     opponents holding either card (per-card segment prefixes X read at
 //     precomputed counts), plus the identical combo once in the tie band;
 //   fold: (total - card sums of both cards + identical combo) x payoff,
@@ -123,11 +124,12 @@ __host__ __device__ inline int groupXEntries(int maxN) { return pad8(2 * maxN + 
 __host__ __device__ inline int groupRowEntries(int maxN) { return pad8(4 * ((maxN + 3) / 4)) + 1; }
 constexpr int kGroupBlocks = kTermThreads / 32 + 1;  // warp blocks + the total
 
-// Showdown groups: tab | P4 | X4 | W4 | WH | WL. The P4 region first holds
-// the staged (transposed, unsorted) reach rows, then the sorted prefixes.
+// Showdown groups: tab | P4 | X4 | W4 | BH | record copy. The P4 region
+// first holds the staged (transposed, unsorted) reach rows, then the sorted
+// prefixes.
 __host__ __device__ inline size_t sdGroupSmem(int maxN) {
   return (size_t)groupTabEntries(maxN) * 2 +
-         16 * ((size_t)groupPrefixEntries(maxN) + groupXEntries(maxN) + 3 * kGroupBlocks) +
+         16 * ((size_t)groupPrefixEntries(maxN) + groupXEntries(maxN) + 2 * kGroupBlocks) +
          sizeof(GroupRec);
 }
 // Fold groups: tab | rs4 | cs4[53] | card pairs (u16) | identical-combo
@@ -182,9 +184,8 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   float4* rs4 = P4;  // staged rows until the prefixes replace them
   float4* X4 = P4 + groupPrefixEntries(maxN);
   float4* W4 = X4 + groupXEntries(maxN);
-  float* BH = reinterpret_cast<float*>(W4 + kGroupBlocks);  // [warp block][4]
-  float* BL = BH + 4 * kGroupBlocks;
-  GroupRec* rc = reinterpret_cast<GroupRec*>(W4 + 3 * kGroupBlocks);
+  float4* BH4 = W4 + kGroupBlocks;  // per warp block: the hi word of its offset
+  GroupRec* rc = reinterpret_cast<GroupRec*>(W4 + 2 * kGroupBlocks);
   {
     const GroupHead gh = loadGroupHead(grec, rc);
     stageTab(tab, t.poolU16 + gh.tabOff, 3 * gh.no + 53);
@@ -257,24 +258,26 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
     if (lane == 31) W4[warp] = incl;
   }
   __syncthreads();
-  if (mine)
-#pragma unroll
-    for (int j = 0; j < kSpan; ++j) P4[pad8(k0 + j)] = ex + pre[j];
-  // Compensated exclusive prefix of the warp-block totals, one thread per
-  // node.
-  if (threadIdx.x < 4) {
-    const int g = threadIdx.x;
-    float hi = 0.f, lo = 0.f;
-    for (int b = 0; b < nbw; ++b) {
-      BH[4 * b + g] = hi;
-      BL[4 * b + g] = lo;
-      addComp(hi, lo, comp4(W4[b], g));
+  // Compensated exclusive prefix of the warp-block totals: every thread
+  // of a block computes its own block's (hi, lo) offset, in the same order
+  // as every other, and stores its positions as Q = lo + P (the low word
+  // folded into the block-local prefix); the block's hi goes to BH.
+  if (mine) {
+    float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int b = 0; b < warp; ++b) {
+      const float4 w = W4[b];
+      addComp(hi[0], lo[0], w.x);
+      addComp(hi[1], lo[1], w.y);
+      addComp(hi[2], lo[2], w.z);
+      addComp(hi[3], lo[3], w.w);
     }
+    const float4 bl = make_float4(lo[0], lo[1], lo[2], lo[3]);
+#pragma unroll
+    for (int j = 0; j < kSpan; ++j) P4[pad8(k0 + j)] = bl + (ex + pre[j]);
+    if (lane == 0) BH4[warp] = make_float4(hi[0], hi[1], hi[2], hi[3]);
   }
   __syncthreads();
 
-  const float4* BH4 = reinterpret_cast<const float4*>(BH);
-  const float4* BL4 = reinterpret_cast<const float4*>(BL);
   // Payoffs of the four nodes (zero for an absent node: the record's
   // padding slots hold zeros).
   const float4 v0 = valOf(rc, 0), v1 = valOf(rc, 1), v2 = valOf(rc, 2), v3 = valOf(rc, 3);
@@ -283,7 +286,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   const float4 lose4 = make_float4(v0.z, v1.z, v2.z, v3.z);
   const ShowdownInfo* info = t.poolSd + rc->infoOff;
   const int bn = no >> kSpanShift;
-  const float4 TH = BH4[bn], TL = BL4[bn], Pno = P4[pad8(no)];
+  const float4 TH = BH4[bn], QT = P4[pad8(no)];
   float* out[4];
   outRows4(out, rows, rc->mask, cfvQOf(rc));
   const int nt4 = quadsOf(nt) * 4;
@@ -307,11 +310,11 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
     float4 sameR = zero4();
     if (s1 > 0) sameR = X4[pad8(a1 + s1)] - X4[pad8(a1 + s1 - 1)];
     const int bl = le >> kSpanShift, bt = te >> kSpanShift;
-    const float4 bhl = BH4[bl], bll = BL4[bl], bht = BH4[bt], blt = BL4[bt];
-    const float4 ple = P4[pad8(le)], pte = P4[pad8(te)];
-    const float4 below = bhl + (bll + ple);
-    const float4 band = (bht - bhl) + (blt - bll) + (pte - ple);
-    const float4 above = (TH - bht) + (TL - blt) + (Pno - pte);
+    const float4 bhl = BH4[bl], bht = BH4[bt];
+    const float4 qle = P4[pad8(le)], qte = P4[pad8(te)];
+    const float4 below = bhl + qle;
+    const float4 band = (bht - bhl) + (qte - qle);
+    const float4 above = (TH - bht) + (QT - qte);
     const float4 lm = max0(below - x1le - x2le);
     const float4 tm = max0(band - (x1te - x1le) - (x2te - x2le) + sameR);
     const float4 gm = max0(above - (x1end - x1te) - (x2end - x2te));
