@@ -362,6 +362,7 @@ __device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, in
   const uint16_t* seg = ord + no;
   const uint16_t* segSlot = seg + 53;
   const ShowdownInfo* info = t.poolSd + st.sdInfoOff[tr];
+  const int16_t* sameTab = t.poolI16 + st.sameOff[tr];  // identical combo's opponent slot
   const RowDev ru = t.rows[u];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 
@@ -459,13 +460,14 @@ __device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, in
       out[i] = T(0);
       continue;
     }
+    // The entry holds the group kernels' padded indices (layout.h); this
+    // kernel's arrays are unpadded.
     const ShowdownInfo f = fs[j];
-    const int le = f.x & 0xffff, te = f.x >> 16;
-    const int len1 = f.y & 0xff, len2 = (f.y >> 8) & 0xff;
-    const int a1 = f.w & 0xfff, a2 = (f.w >> 16) & 0xfff;
-    const T x1le = ws.X[a1 + ((f.y >> 16) & 0xff)], x1te = ws.X[a1 + (f.y >> 24)];
-    const T x2le = ws.X[a2 + (f.z & 0xff)], x2te = ws.X[a2 + ((f.z >> 8) & 0xff)];
-    const int same = (int)(f.z >> 16) - 1;
+    const int le = unpad8((int)(f.w & 0x7ff)), te = unpad8((int)((f.w >> 11) & 0x7ff));
+    const T x1le = ws.X[unpad8((int)(f.x & 0xfff))], x1te = ws.X[unpad8((int)((f.x >> 12) & 0xfff))];
+    const T x1end = ws.X[unpad8((int)(f.y & 0xfff))], x2le = ws.X[unpad8((int)((f.y >> 12) & 0xfff))];
+    const T x2te = ws.X[unpad8((int)(f.z & 0xfff))], x2end = ws.X[unpad8((int)((f.z >> 12) & 0xfff))];
+    const int same = sameTab[i];
     const T sameR = same >= 0 ? ws.rs[same] : T(0);
     const int bl = le >> 5, bt = te >> 5;
     T below, band, above;
@@ -481,7 +483,7 @@ __device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, in
     }
     T lm = below - x1le - x2le;
     T tm = band - (x1te - x1le) - (x2te - x2le) + sameR;
-    T gm = above - (ws.X[a1 + len1] - x1te) - (ws.X[a2 + len2] - x2te);
+    T gm = above - (x1end - x1te) - (x2end - x2te);
     lm = lm > T(0) ? lm : T(0);
     tm = tm > T(0) ? tm : T(0);
     gm = gm > T(0) ? gm : T(0);

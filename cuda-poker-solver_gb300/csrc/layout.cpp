@@ -158,17 +158,29 @@ void buildStateParts(const Tree& t, int s, StateParts& P) {
         const auto& v = posOfCard[c1];
         ks1 = (int)(std::lower_bound(v.begin(), v.end(), posOfSlot[same]) - v.begin()) + 1;
       }
+      // Segment prefix runs: card c's run starts at seg[c] + c (one more
+      // entry than the segment); the kernels address entry k of the
+      // concatenated runs at pad8(k).
       const int a1 = segStart[c1] + c1, a2 = segStart[c2] + c2;
-      if (a1 >= 4096 || a2 >= 4096 || ks1 >= 64)
+      const int x1le = pad8(a1 + below(c1, le)), x1te = pad8(a1 + below(c1, te));
+      const int x1end = pad8(a1 + len1);
+      const int x2le = pad8(a2 + below(c2, le)), x2te = pad8(a2 + below(c2, te));
+      const int x2end = pad8(a2 + len2);
+      // The identical combo: the step of card c1's run at its entry (prefix
+      // after it minus prefix before it); without one, two in-range
+      // entries that the kernels read and discard.
+      const int sHi = ks1 > 0 ? pad8(a1 + ks1) : 2;
+      const int sStep = ks1 > 0 ? sHi - pad8(a1 + ks1 - 1) : 1;
+      const int pLe = pad8(le), pTe = pad8(te);
+      if (x1end >= 4096 || x2end >= 4096 || sHi >= 4096 || pTe >= 2048 || (te >> 8) >= 8)
         throw Error{PPS_GB_E_FORMAT, "showdown table entry out of range"};
       ShowdownInfo info;
-      info.x = (uint32_t)le | ((uint32_t)te << 16);
-      info.y = (uint32_t)len1 | ((uint32_t)len2 << 8) | ((uint32_t)below(c1, le) << 16) |
-               ((uint32_t)below(c1, te) << 24);
-      info.z = (uint32_t)below(c2, le) | ((uint32_t)below(c2, te) << 8) |
-               ((uint32_t)(same + 1) << 16);
-      info.w = (uint32_t)a1 | ((uint32_t)(ks1 & 15) << 12) | ((uint32_t)a2 << 16) |
-               ((uint32_t)(ks1 >> 4) << 28);
+      info.x = (uint32_t)x1le | ((uint32_t)x1te << 12) | ((uint32_t)(sHi & 0xff) << 24);
+      info.y = (uint32_t)x1end | ((uint32_t)x2le << 12) | ((uint32_t)(sHi >> 8) << 24);
+      info.z = (uint32_t)x2te | ((uint32_t)x2end << 12);
+      info.w = (uint32_t)pLe | ((uint32_t)pTe << 11) | ((uint32_t)(le >> 8) << 22) |
+               ((uint32_t)(te >> 8) << 25) | ((uint32_t)(sStep - 1) << 28) |
+               ((uint32_t)(ks1 > 0) << 29);
       P.info[tr].push_back(info);
     }
   }

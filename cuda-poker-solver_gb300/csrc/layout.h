@@ -74,15 +74,32 @@ struct alignas(16) StateDev {
                     // per traverser slot (see showdownInfo)
 };
 
-// Showdown entry of one traverser combo (cards c1, c2): x = le | te << 16
-// (opponents strictly weaker / weaker-or-equal, in sorted positions);
-// y = len1 | len2 << 8 | k1le << 16 | k1te << 24; z = k2le | k2te << 8 |
-// (same+1) << 16; w = a1 | (s1 & 15) << 12 | a2 << 16 | (s1 >> 4) << 28.
-// lenX is the length of card cX's segment, kXle / kXte count its entries
-// below le / te, aX = seg[cX] + cX (< 4096) is where its prefix run starts
-// in the kernels' segment scan, `same` is the opponent slot of the
-// identical combo (-1: none) and s1 its entry in card c1's segment plus one
-// (0: none).
+#ifdef __CUDACC__
+#define PPS_HD __host__ __device__
+#else
+#define PPS_HD
+#endif
+// Padded float4 arrays of the terminal kernels: entry k lives at pad8(k),
+// one padding entry after every eight, so that eight threads writing eight
+// consecutive entries each hit eight different bank groups. unpad8 inverts
+// it on the entries pad8 produces.
+PPS_HD inline int pad8(int k) { return k + (k >> 3); }
+PPS_HD inline int unpad8(int p) { return p - p / 9; }
+
+// Showdown entry of one traverser combo (cards c1, c2), as shared-memory
+// indices of the kernels' padded arrays. The opponents strictly weaker /
+// weaker-or-equal end at sorted positions le / te; card cX's prefix run
+// (one entry more than its segment of the strength order) starts at entry
+// aX = seg[cX] + cX of the concatenated runs, and kXle / kXte count its
+// entries below le / te. Fields:
+//   x = pad8(a1 + k1le) | pad8(a1 + k1te) << 12 | (sHi & 0xff) << 24
+//   y = pad8(a1 + len1) | pad8(a2 + k2le) << 12 | (sHi >> 8) << 24
+//   z = pad8(a2 + k2te) | pad8(a2 + len2) << 12
+//   w = pad8(le) | pad8(te) << 11 | (le >> 8) << 22 | (te >> 8) << 25 |
+//       (step - 1) << 28 | hasSame << 29
+// The identical combo's reach is the step of card c1's run at its entry:
+// run[sHi] - run[sHi - step] (step 1, or 2 across a padding entry), where
+// hasSame is set; otherwise sHi = 2, step 1, read and discarded.
 struct alignas(16) ShowdownInfo {
   uint32_t x, y, z, w;
 };

@@ -112,13 +112,13 @@ static __device__ __forceinline__ float4 valOf(const GroupRec* c, int k) {
 // positions form one compensation block.
 constexpr int kSpan = 8;
 constexpr int kSpanShift = 8;  // log2(32 * kSpan): position -> warp block
+static_assert(kSpanShift == 8, "showdown entries carry position >> 8 as the warp block (layout.h)");
 __host__ __device__ inline int groupTabEntries(int maxN) { return (3 * maxN + 53 + 7) / 8 * 8; }
 // The float4 arrays below are padded with one entry after every 8 (entry k
 // lives at pad8(k)): a thread's 8 consecutive positions, and the 8 lanes
 // of a card segment, then fall in 8 different bank groups when they write
 // at stride 8, instead of 8-way conflicts on one bank group (ncu counted
 // conflicts as 62% of the showdown kernel's shared-memory wavefronts).
-__host__ __device__ __forceinline__ int pad8(int k) { return k + (k >> 3); }
 __host__ __device__ inline int groupPrefixEntries(int maxN) { return pad8(maxN + kSpan) + 1; }
 __host__ __device__ inline int groupXEntries(int maxN) { return pad8(2 * maxN + 52) + 1; }
 __host__ __device__ inline int groupRowEntries(int maxN) { return pad8(4 * ((maxN + 3) / 4)) + 1; }
@@ -296,22 +296,20 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
       storeOut4(out, i, zero4());
       continue;
     }
+    // The entry holds the shared-memory indices themselves (layout.h).
     const ShowdownInfo f = info[i];
-    const int le = f.x & 0xffff, te = f.x >> 16;
-    const int len1 = f.y & 0xff, len2 = (f.y >> 8) & 0xff;
-    const int a1 = f.w & 0xfff, a2 = (f.w >> 16) & 0xfff;
-    const int s1 = ((f.w >> 12) & 15) | ((f.w >> 28) << 4);
-    const float4 x1le = X4[pad8(a1 + ((f.y >> 16) & 0xff))], x1te = X4[pad8(a1 + (f.y >> 24))];
-    const float4 x2le = X4[pad8(a2 + (f.z & 0xff))], x2te = X4[pad8(a2 + ((f.z >> 8) & 0xff))];
-    const float4 x1end = X4[pad8(a1 + len1)], x2end = X4[pad8(a2 + len2)];
+    const float4 x1le = X4[f.x & 0xfff], x1te = X4[(f.x >> 12) & 0xfff];
+    const float4 x1end = X4[f.y & 0xfff], x2le = X4[(f.y >> 12) & 0xfff];
+    const float4 x2te = X4[f.z & 0xfff], x2end = X4[(f.z >> 12) & 0xfff];
     // The identical combo's reach: its step in card c1's segment prefix
     // (exact up to the rounding of that prefix, a few units in the last
     // place of a sum of at most 51 entries).
-    float4 sameR = zero4();
-    if (s1 > 0) sameR = X4[pad8(a1 + s1)] - X4[pad8(a1 + s1 - 1)];
-    const int bl = le >> kSpanShift, bt = te >> kSpanShift;
-    const float4 bhl = BH4[bl], bht = BH4[bt];
-    const float4 qle = P4[pad8(le)], qte = P4[pad8(te)];
+    const int sHi = (int)((f.x >> 24) | ((f.y >> 16) & 0xf00));
+    const int sLo = sHi - 1 - (int)((f.w >> 28) & 1);
+    float4 sameR = X4[sHi] - X4[sLo];
+    if (!((f.w >> 29) & 1)) sameR = zero4();
+    const float4 bhl = BH4[(f.w >> 22) & 7], bht = BH4[(f.w >> 25) & 7];
+    const float4 qle = P4[f.w & 0x7ff], qte = P4[(f.w >> 11) & 0x7ff];
     const float4 below = bhl + qle;
     const float4 band = (bht - bhl) + (qte - qle);
     const float4 above = (TH - bht) + (QT - qte);
