@@ -18,9 +18,16 @@ namespace gb {
 namespace {
 
 // Tables that kernels stage into shared memory start on a 16-byte boundary
-// (8 entries) so they can be copied with 16-byte vector loads.
+// so they can be copied with 16-byte vector loads (and a copy that rounds
+// the table up to whole 16-byte chunks stays inside the pool).
 void alignU16(std::vector<uint16_t>& pool) {
   while (pool.size() % 8) pool.push_back(0);
+}
+void alignI16(std::vector<int16_t>& pool) {
+  while (pool.size() % 8) pool.push_back(0);
+}
+void alignU8(std::vector<uint8_t>& pool) {
+  while (pool.size() % 16) pool.push_back(0);
 }
 
 int appendU16(std::vector<uint16_t>& pool, const std::vector<int>& v) {
@@ -387,10 +394,10 @@ HostLayout buildLayout(const Tree& t) {
   size_t nU8 = 0, nU16 = 0, nI16 = 0, nSd = 0;
   for (const StateParts& P : parts)
     for (int p = 0; p < 2; ++p) {
-      nU8 += P.cards[p].size();
+      nU8 += P.cards[p].size() + 16;
       nU16 += P.starts[p].size() + P.entries[p].size() + P.up[p].size() + P.ord[p].size() +
               P.segStart[p].size() + P.segSlot[p].size() + 16;  // + alignment
-      nI16 += P.same[p].size() + P.down[p].size();
+      nI16 += P.same[p].size() + P.down[p].size() + 8;
       nSd += P.info[p].size();
     }
   L.poolU8.reserve(L.poolU8.size() + nU8);
@@ -406,11 +413,13 @@ HostLayout buildLayout(const Tree& t) {
       const int n = (int)st.list[p].size();
       sd.n[p] = n;
       L.maxN = std::max(L.maxN, n);
+      alignU8(L.poolU8);
       sd.cardsOff[p] = (int)L.poolU8.size();
       L.poolU8.insert(L.poolU8.end(), P.cards[p].begin(), P.cards[p].end());
       alignU16(L.poolU16);
       sd.csrOff[p] = appendU16(L.poolU16, P.starts[p]);
       appendU16(L.poolU16, P.entries[p]);
+      alignI16(L.poolI16);
       sd.sameOff[p] = appendI16(L.poolI16, P.same[p]);
       sd.upOff[p] = sd.downOff[p] = -1;
       if (st.parent >= 0) {
@@ -757,6 +766,8 @@ HostLayout buildLayout(const Tree& t) {
   buildBackwardLevels(t, L, bwdRecFirst, chanceRecsOf);
   if (N >= (1 << 24)) throw Error{PPS_GB_E_MEMORY, "tree too large for 24-bit task node ids"};
   alignU16(L.poolU16);
+  alignI16(L.poolI16);
+  alignU8(L.poolU8);
   return L;
 }
 

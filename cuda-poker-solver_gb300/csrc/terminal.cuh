@@ -148,17 +148,34 @@ static __device__ __forceinline__ void stageRows4(float4* rs4, const DevRows<flo
 #pragma unroll
   for (int g = 0; g < 4; ++g)
     r[g] = (mask >> g) & 1 ? rows.reach[tr] + (size_t)q[g] * 4 : nullptr;
+  // Read-only loads: the compiler may issue a thread's next quad before
+  // the shared-memory stores of this one.
   for (int q = threadIdx.x; q < quadsOf(no); q += blockDim.x) {
     float4 v[4];
 #pragma unroll
     for (int g = 0; g < 4; ++g)
-      v[g] = r[g] ? *reinterpret_cast<const float4*>(r[g] + 4 * q) : zero4();
+      v[g] = r[g] ? __ldg(reinterpret_cast<const float4*>(r[g] + 4 * q)) : zero4();
     float4* d = rs4 + pad8(4 * q);  // the quad's 4 entries share one pad block
     d[0] = make_float4(v[0].x, v[1].x, v[2].x, v[3].x);
     d[1] = make_float4(v[0].y, v[1].y, v[2].y, v[3].y);
     d[2] = make_float4(v[0].z, v[1].z, v[2].z, v[3].z);
     d[3] = make_float4(v[0].w, v[1].w, v[2].w, v[3].w);
   }
+}
+
+// Starts asynchronous copies (cp.async, 16 bytes each) of a 16-byte aligned
+// table of n16 chunks into shared memory; they land while the thread loads
+// the reach rows, and stageDone waits for them.
+static __device__ __forceinline__ void stageChunksAsync(void* dst, const void* src, int n16) {
+  for (int k = threadIdx.x; k < n16; k += blockDim.x) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(reinterpret_cast<uint4*>(dst) + k);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s),
+                 "l"(reinterpret_cast<const uint4*>(src) + k)
+                 : "memory");
+  }
+}
+static __device__ __forceinline__ void stageDone() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
 // Value rows of the group's nodes (nullptr for an absent node).
@@ -188,8 +205,9 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   GroupRec* rc = reinterpret_cast<GroupRec*>(W4 + 2 * kGroupBlocks);
   {
     const GroupHead gh = loadGroupHead(grec, rc);
-    stageTab(tab, t.poolU16 + gh.tabOff, 3 * gh.no + 53);
+    stageChunksAsync(tab, t.poolU16 + gh.tabOff, (3 * gh.no + 53 + 7) / 8);
     stageRows4(rs4, rows, gh.mask, gh.reachQ, tr, gh.no);
+    stageDone();
   }
   __syncthreads();
   // From here on the record's words come from the shared copy.
@@ -333,16 +351,13 @@ static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, c
   const int no = gh.no, nt = gh.nt;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 
-  stageTab(csr, t.poolU16 + gh.tabOff, 53 + 2 * no);
+  // The opponent's card lists, the traverser's card pairs (u16 each) and
+  // identical-combo slots: 16-byte aligned tables copied in whole chunks.
+  stageChunksAsync(csr, t.poolU16 + gh.tabOff, (53 + 2 * no + 7) / 8);
+  stageChunksAsync(cardsS, t.poolU8 + gh.infoOff, (nt + 7) / 8);
+  stageChunksAsync(sameS, t.poolI16 + gh.sameOff, (nt + 7) / 8);
   stageRows4(rs4, rows, gh.mask, gh.reachQ, tr, no);
-  {  // the traverser's card pairs and identical-combo slots
-    const uint16_t* cards = reinterpret_cast<const uint16_t*>(t.poolU8 + gh.infoOff);
-    const int16_t* same = t.poolI16 + gh.sameOff;
-    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-      cardsS[i] = cards[i];
-      sameS[i] = same[i];
-    }
-  }
+  stageDone();
   __syncthreads();
   // Card sums, four cards per warp (8 lanes x 8 entries, then a fixed
   // xor tree over the 8 lanes).
