@@ -254,6 +254,51 @@ __device__ __forceinline__ void ld4s(const float4* p, float (&x)[4]) {
   x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
 }
 
+// recordFoldedChildren through the record's child stage C, which is free at
+// that point: per folded-in child, the lane's quads of up to kAsyncNa of its
+// children are copied with cp.async (all in flight at once, no registers
+// held) and summed from C in the children's order, so a child costs one
+// memory round trip per kAsyncNa grandchildren instead of one per
+// grandchild. Entry j of the lane lives at C[j * stride + slot]; each
+// thread reads back only its own entries. The sums are bitwise those of
+// recordFoldedChildren.
+__device__ __forceinline__ void recordFoldedChildrenStaged(const DevRows<float>& rows,
+                                                           const DecRec& r, int lane, float4* C,
+                                                           int stride, int slot) {
+  if (!r.pre) return;
+  const int nq = quadsOf(r.n);
+  const int q = r.chunk * kRecQuads + lane;
+  const uint32_t* p = r.pre;
+  const int P = (int)p[0];
+  ++p;
+  for (int e = 0; e < P; ++e) {
+    const uint32_t row = p[0];
+    const int m = (int)p[1];
+    p += 2;
+    if (q < nq) {
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int b0 = 0; b0 < m; b0 += kAsyncNa) {
+        const int k = m - b0 < kAsyncNa ? m - b0 : kAsyncNa;
+        for (int j = 0; j < k; ++j)
+          cpAsync16(&C[j * stride + slot], rows.cfv + (size_t)p[b0 + j] * 4 + 4 * q);
+        cpAsyncWaitAll();
+        for (int j = 0; j < k; ++j) {
+          float c[4];
+          ld4s(&C[j * stride + slot], c);
+          for (int l = 0; l < 4; ++l) v[l] += c[l];
+        }
+      }
+      for (int l = 0; l < 4; ++l)
+        if (4 * q + l >= r.n) v[l] = 0.f;
+      stq(rows.cfv + (size_t)row * 4 + 4 * q, v);
+    }
+    p += m;
+  }
+  // The rows just written are read next by copies of the async proxy (bulk
+  // and cp.async staging) and by other lanes.
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
 // Backward decide record, staged, first part: the copies of the regret and
 // strategy rows of the traverser's own node (nothing for another node or a
 // record that is not staged). Those rows are written only by the backward
@@ -289,11 +334,11 @@ __device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRo
     decideRecord(t, rows, r, lane);
     return;
   }
-  recordFoldedChildren(rows, r, lane);  // each thread copies back only its own quads
+  const int tid = (int)threadIdx.x;
+  recordFoldedChildrenStaged(rows, r, lane, stage, kThreads, tid);
   const int nq = quadsOf(r.n);
   const int q = r.chunk * kRecQuads + lane;
   if (q >= nq) return;
-  const int tid = (int)threadIdx.x;
   float4* C = stage;
   float4* R = stage + kAsyncNa * kThreads;
   float4* S = R + kAsyncNa * kThreads;
@@ -511,8 +556,11 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
   if (r.own && q0 + lane < nq) prefetchStratLo(t, r, q0 + lane, nq);
   pdlWait();
   if (r.pre) {  // folded-in children: every lane's quads written before lane 0's copies
-    recordFoldedChildren(rows, r, lane);
+    recordFoldedChildrenStaged(rows, r, lane, C, kRecQuads, lane);
     __syncwarp();
+    // The lanes' reads of C (generic proxy) before the child copies into it
+    // (async proxy).
+    if (lane == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   if (lane == 0)
     for (int a = 0; a < na; ++a)
