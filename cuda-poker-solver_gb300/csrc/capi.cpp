@@ -496,6 +496,13 @@ int pps_gb_time_iterations(pps_gb_solver* h, int n, double* ms) {
   });
 }
 
+int pps_gb_probe_bounded_wait(pps_gb_solver* h, int spins) {
+  return guarded([&] {
+    if (spins < 1) throw Error{PPS_GB_E_ARG, "spins must be positive"};
+    core(h).probeBoundedWait(spins);
+  });
+}
+
 int pps_gb_profile(pps_gb_solver* h, int n, int flags, pps_gb_kernel_stat* out, int cap,
                    int* n_out) {
   return guarded([&] {

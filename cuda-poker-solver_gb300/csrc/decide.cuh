@@ -504,8 +504,9 @@ __device__ __forceinline__ void bulkLoad(void* dst, const float* src, uint32_t b
 }
 // True once the barrier's phase `parity` completed; false after kBarSpins
 // polls (each poll may itself wait a little: try_wait has a time limit).
-__device__ __forceinline__ bool barWait(unsigned long long* bar, uint32_t parity) {
-  for (int i = 0; i < kBarSpins; ++i) {
+__device__ __forceinline__ bool barWait(unsigned long long* bar, uint32_t parity,
+                                        int spins = kBarSpins) {
+  for (int i = 0; i < spins; ++i) {
     uint32_t done = 0;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -519,11 +520,27 @@ __device__ __forceinline__ bool barWait(unsigned long long* bar, uint32_t parity
   return false;
 }
 
+// A warp's wait for the copies it issued on its barrier, bounded: true once
+// they landed (every lane agrees). Otherwise it drains - waits for the same
+// copies for up to kDrainRounds more rounds, so that the CTA does not leave
+// with asynchronous writes into its shared memory in flight - sets the
+// device error word (bit 1: the wait ran out; bit 2 as well: the drain ran
+// out too, and the copies may outlive the CTA) and returns false.
+__device__ __forceinline__ bool warpCopiesLanded(unsigned long long* bar, uint32_t parity, int* err,
+                                                 int lane, int spins = kBarSpins) {
+  if (__all_sync(0xffffffffu, barWait(bar, parity, spins))) return true;
+  bool drained = false;
+  for (int k = 0; k < kDrainRounds && !drained; ++k) drained = barWait(bar, parity, spins);
+  if (lane == 0 && err) atomicOr(err, drained ? 1 : 3);
+  return false;
+}
+
 // stage: this warp's segments; bar: this warp's barrier; phase: the
 // barrier's next parity (flipped here).
 __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows<float>& rows,
                                                  const DecRec& r, int lane, float4* stage,
-                                                 unsigned long long* bar, uint32_t& phase) {
+                                                 unsigned long long* bar, uint32_t& phase,
+                                                 bool& broken) {
   const int na = r.na;
   if (na > kAsyncNa) {
     pdlWait();
@@ -539,8 +556,9 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
   float4* S = R + kAsyncNa * kRecQuads;
   float* reg = t.regret + (size_t)r.regQ * 4;
   float* str = t.strat + (size_t)r.regQ * 4;
-  int failed = lane == 0 && t.err ? *reinterpret_cast<volatile int*>(t.err) : 0;
-  if (__shfl_sync(0xffffffffu, failed, 0)) return;  // the same answer for every lane
+  // A warp whose barrier wait gave up on an earlier record issues no more
+  // copies (its barrier may still count that record's); warp-uniform.
+  if (broken) return;
   __syncwarp();  // the lanes' reads of the last record's segments are done
   if (lane == 0) {
     // Earlier reads of the stage (generic proxy) before the copies (async proxy).
@@ -566,18 +584,10 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
     for (int a = 0; a < na; ++a)
       bulkLoad(&C[a * kRecQuads], rows.cfv + ((size_t)r.kid[a] + q0) * 4, segBytes, bar);
   const uint32_t parity = phase;
-  const bool ok = barWait(bar, parity);
   phase ^= 1u;
-  if (!ok) {
-    // Give-up path: the copies are this warp's own and still count on the
-    // barrier. Wait for them once more (bounded again) so that the CTA does
-    // not leave with asynchronous writes into its shared memory in flight;
-    // error bit 1: the wait ran out, bit 2: the drain ran out as well (the
-    // copies may then outlive the CTA; the host discards the launch's
-    // results either way).
-    bool drained = false;
-    for (int k = 0; k < kDrainRounds && !drained; ++k) drained = barWait(bar, parity);
-    if (lane == 0 && t.err) atomicOr(t.err, drained ? 1 : 3);
+  if (!warpCopiesLanded(bar, parity, t.err, lane)) {
+    // The host discards the launch's results.
+    broken = true;
     return;
   }
   const int q = q0 + lane;
@@ -846,6 +856,7 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
   if (lane == 0) barInit(bar);
   __syncwarp();
   uint32_t phase = 0;
+  bool broken = false;
   for (int i = blockIdx.x; i < nCh + nRc; i += gridDim.x) {
     // A CTA that runs more than one task (grids past 2^20 CTAs) must not
     // overwrite shared memory that its warps still read for the last one.
@@ -856,7 +867,7 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       const DecRec r = loadRec(recs, recTasks[k]);
       decideRecordBulk(t, rows, r, lane,  // waits for the previous level itself
                        reinterpret_cast<float4*>(smem) + warp * 3 * kAsyncNa * kRecQuads, bar,
-                       phase);
+                       phase, broken);
     } else {
       const uint4 h = loadChanceHeader(recs, chance[i]);
       chanceRecordTables(t, rows, recs, h, smem);

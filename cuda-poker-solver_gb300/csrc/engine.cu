@@ -582,6 +582,26 @@ void Engine::sync() {
   checkDeviceError();
 }
 
+// One warp expects 16 bytes on its barrier that no copy delivers, and waits
+// with the records' bounded wait and give-up path (warpCopiesLanded).
+static __global__ void boundedWaitProbeK(int* err, int spins) {
+  __shared__ unsigned long long bar;
+  const int lane = (int)threadIdx.x & 31;
+  if (lane == 0) {
+    barInit(&bar);
+    barExpect(&bar, 16);
+  }
+  __syncwarp();
+  warpCopiesLanded(&bar, 0, err, lane, spins);
+}
+
+void Engine::probeBoundedWait(int spins) {
+  boundedWaitProbeK<<<1, 32, 0, d_->stream>>>(d_->tree.err, spins);
+  GB_CK(cudaGetLastError());
+  GB_CK(cudaStreamSynchronize(d_->stream));
+  checkDeviceError();
+}
+
 // A bounded wait in a kernel gave up (its results are not valid).
 void Engine::checkDeviceError() {
   int e = 0;

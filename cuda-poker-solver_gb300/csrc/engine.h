@@ -32,6 +32,10 @@ class Engine {
   void iterate(int n);
   void sync();
   void checkDeviceError();
+  // Diagnostic of the bounded device waits: one warp waits on its barrier
+  // for a copy that is never issued, `spins` polls a round; its give-up
+  // path sets this engine's error word, and checkDeviceError throws.
+  void probeBoundedWait(int spins);
   // Runs one FP64 walk (mode 1 = average-strategy EV, 2 = best response)
   // for traverser tr and waits for it; rows stay readable afterwards.
   void walk(int tr, int mode);

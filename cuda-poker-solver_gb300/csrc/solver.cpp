@@ -171,6 +171,8 @@ void SolverCore::extendSchedule(int n) {
   eng_->setSchedule(tab, (int)t0);
 }
 
+void SolverCore::probeBoundedWait(int spins) { eng_->probeBoundedWait(spins); }
+
 double SolverCore::timeIterations(int n) {
   extendSchedule(n);
   const double ms = eng_->timeIterations(n);

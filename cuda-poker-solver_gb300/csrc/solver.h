@@ -59,6 +59,7 @@ class SolverCore {
   // Benchmark helpers: n more iterations continuing the DCFR schedule
   // (CUDA-event timed / profiled launch by launch).
   double timeIterations(int n);
+  void probeBoundedWait(int spins);
   std::vector<Engine::KernelStat> profile(int n, bool splitKinds);
   // Root value (chips) of one FP64 walk; fills the traverser's root row.
   double walkValue(int tr, int mode, std::vector<double>* rootRow);

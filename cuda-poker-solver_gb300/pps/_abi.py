@@ -140,6 +140,7 @@ _SIGS = {
     "pps_gb_get_launch_shape": (C.c_int, [H, P(LaunchShape)]),
     "pps_gb_time_iterations": (C.c_int, [H, C.c_int, P(C.c_double)]),
     "pps_gb_profile": (C.c_int, [H, C.c_int, C.c_int, P(KernelStat), C.c_int, P(C.c_int)]),
+    "pps_gb_probe_bounded_wait": (C.c_int, [H, C.c_int]),
     "pps_gb_solve_noalloc": (C.c_int, [P(Spot), P(BetConfig), C.c_void_p, C.c_void_p, C.c_int64,
                                        C.c_int, C.c_int, C.c_void_p, P(C.c_int64)]),
     "pps_gb_batch_config_default": (None, [P(BatchConfig)]),

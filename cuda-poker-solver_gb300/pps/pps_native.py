@@ -442,6 +442,11 @@ class Solver:
         check(lib.pps_gb_time_iterations(self._h, int(n), C.byref(ms)))
         return ms.value
 
+    def probe_bounded_wait(self, spins: int = 1024) -> None:
+        """Diagnostic: a warp waits, bounded, for a copy that is never issued;
+        raises the solver's device-wait error (PPS_GB_E_CUDA) afterwards."""
+        check(lib.pps_gb_probe_bounded_wait(self._h, int(spins)))
+
     def profile(self, n: int, split_kinds: bool = False):
         """Per kernel class over n iterations: {name: (launches, ms, bytes)};
         split_kinds reports the backward pass per node kind."""

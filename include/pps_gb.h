@@ -274,6 +274,14 @@ int pps_gb_time_iterations(pps_gb_solver* h, int n, double* ms);
  * and report the kinds separately (the reference's kindMask breakdown). */
 int pps_gb_profile(pps_gb_solver* h, int n, int flags, pps_gb_kernel_stat* out,
                    int cap, int* n_out);
+/* Diagnostic of the bounded device waits (no counterpart in the reference):
+ * on the solver's stream, one warp waits on its shared-memory barrier for a
+ * copy that is never issued, with the same bounded wait and give-up path
+ * as the iteration's bulk-copied records (`spins` polls per round, one
+ * round plus four drain rounds). The give-up sets the solver's device error
+ * word, so the call returns PPS_GB_E_CUDA ("a device wait timed out"); the
+ * solver stays usable. No GPU fault is involved. */
+int pps_gb_probe_bounded_wait(pps_gb_solver* h, int spins);
 
 /* Size in bytes of the static device array behind pps_gb_solve_noalloc. */
 #define PPS_GB_NOALLOC_SCRATCH_BYTES (64ull << 20)

@@ -256,3 +256,22 @@ def test_cli_protocol():
     assert abs(ev0 - 116.649980) < 1e-4
     assert "EXPLOITABILITY" in lines
     assert "iters/s" in out.stderr and "nodes=1305" in out.stderr
+
+
+def test_bounded_wait_gives_up_and_reports():
+    """The device waits are bounded: a warp that waits on its barrier for a
+    copy that is never issued gives up after its polls (the bulk-copied
+    records' wait, then its drain rounds), sets the solver's device error
+    word, and the host raises. No GPU fault is involved, and the solver
+    afterwards solves exactly as a fresh one does."""
+    import time
+    s = fresh()
+    t0 = time.time()
+    with pytest.raises(RuntimeError, match="device wait timed out"):
+        s.probe_bounded_wait(1024)
+    assert time.time() - t0 < 120
+    s.solve(30)
+    f = fresh()
+    f.solve(30)
+    for which in (0, 1):
+        assert np.array_equal(s.read_rows(which), f.read_rows(which))

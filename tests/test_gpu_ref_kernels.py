@@ -92,8 +92,9 @@ def test_solution_matches_reference_kernels(name, iters):
     """After a full solve both strategies pass the solution gates against
     each other: EVs within 0.01 chips, root strategy within 0.10 L-inf
     (range-weighted frequencies of the root actions) and exploitability
-    within a factor 2 (or 0.01 chips where it is ~0, or both within 0.2%
-    of the pot of equilibrium, where rounding sets it). The reference's
+    within a factor 2 (or 0.01 chips where it is ~0, or both within 0.5%
+    of the pot of equilibrium - the batch and serve target - where f32
+    rounding sets it). The reference's
     average strategy is scored by the product's FP64 walks after writing its
     rows in. turn_c3 is the benchmark's own workload (48,255 nodes, 1,000
     iterations), turn_c2_uniform the 6,333-node turn at 500."""
@@ -111,12 +112,13 @@ def test_solution_matches_reference_kernels(name, iters):
     assert abs(mine["ev_oop"] - theirs["ev_oop"]) < 0.01, (mine, theirs)
     assert abs(mine["ev_ip"] - theirs["ev_ip"]) < 0.01, (mine, theirs)
     a, b = mine["exploitability"], theirs["exploitability"]
-    # Where both solutions are within 0.2% of the pot of exact equilibrium
-    # (well inside the 0.5% serving target), their exploitability is set by
-    # f32 rounding, and the ratio is noise: the reference's kernels, whose
-    # fold sums use shared-memory atomics, gave 0.015 and 0.059 chips on
-    # turn_c3 after the same 1,000 iterations in two runs.
-    converged = max(a, b) <= 0.002 * spot.pot
+    # Where both solutions are within 0.5% of the pot of exact equilibrium
+    # (the batch and serve target), their exploitability is set by f32
+    # rounding, and the ratio is noise: the reference's kernels, whose fold
+    # sums use shared-memory atomics (a different order each run), gave
+    # 0.015, 0.059 and 0.249 chips on turn_c3 (pot 100) after the same
+    # 1,000 iterations in three runs. The EVs above are checked either way.
+    converged = max(a, b) <= 0.005 * spot.pot
     assert abs(a - b) < 0.01 or converged or 0.5 <= a / max(b, 1e-9) <= 2.0, (a, b)
     g, ref = np.asarray(s.root_strategy()), np.asarray(scored.root_strategy())
     assert g.shape == ref.shape
