@@ -193,19 +193,31 @@ def accuracy(threads=None):
                      "FP64's; strategy_linf: root frequencies; rows_1_iteration: max |row - "
                      "FP64| / max |FP64| over regret and strategy rows after one iteration; "
                      "f32_restatement: the same errors of a plain f32 restatement of the "
-                     "reference iteration"}
+                     "reference iteration; gpu_per_node_kernels: the product's per-node "
+                     "kernels (engine 1), the same formulas in another f32 order. Where an "
+                     "iteration count leaves the solve far from equilibrium (turn_c3 at 30, "
+                     "exploitability ~5% of pot), f32 rounding flips regret-matching choices "
+                     "at exactly-zero regrets, so every f32 order drifts from FP64 by O(0.1) "
+                     "chips; the spread of the three f32 entries shows that noise"}
     for name, iters in (("river_c1", 1000), ("turn_c2", 200), ("turn_c3", 30)):
         spot = wl.NAMED[name]()
         s = make(spot)
         s.solve(1)
+        # The per-node kernels (engine 1): the same formulas in another f32
+        # evaluation order, for the spread between valid f32 orders.
+        s1 = make(spot)
+        s1.set_engine(1)
+        s1.solve(1)
         o64 = oracle_for(spot, threads, precision=64)
         o32 = oracle_for(spot, threads, precision=32)
         o64.iterate(1)
         o32.iterate(1)
-        rows1 = [max(normwise(x.rows(k) if x is not s else s.read_rows(k), o64.rows(k))
-                     for k in (0, 1)) for x in (s, o32)]
+        rows1 = [max(normwise(x.read_rows(k) if x is not o32 else x.rows(k), o64.rows(k))
+                     for k in (0, 1)) for x in (s, o32, s1)]
         s.solve(iters)
         st = s.stats()
+        s1.solve(iters)
+        st1 = s1.stats()
         o64.iterate(iters - 1)
         o32.iterate(iters - 1)
         e64, e32 = o64.stats(spot.pot), o32.stats(spot.pot)
@@ -221,9 +233,11 @@ def accuracy(threads=None):
         out[name] = {"iterations": iters, "nodes": s.num_nodes,
                      "fp64_ev_oop": e64["ev_oop"], "fp64_exploitability": e64["exploitability"],
                      "gpu": errs(st["ev_oop"], st["exploitability"], s.root_strategy(), rows1[0]),
+                     "gpu_per_node_kernels": errs(st1["ev_oop"], st1["exploitability"],
+                                                  s1.root_strategy(), rows1[2]),
                      "f32_restatement": errs(e32["ev_oop"], e32["exploitability"],
                                              root_freqs(o32.rows(1), na, w0), rows1[1])}
-        del s, o64, o32
+        del s, s1, o64, o32
     return out
 
 
@@ -468,8 +482,10 @@ def main():
                          "(0: the same spots as the batch)")
     ap.add_argument("--served-requests", type=int, default=100,
                     help="requests per arrival rate of the served run (0 skips it)")
-    ap.add_argument("--served-rates", default="50,200,800",
-                    help="Poisson arrival rates (requests/s) of the served run")
+    ap.add_argument("--served-rates", default="4,50,200",
+                    help="Poisson arrival rates (requests/s) of the served run: one "
+                         "below the ~8 solves/s a GB300 sustains on this distribution, "
+                         "two above it")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
