@@ -460,9 +460,9 @@ __device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const De
 // row, and for the traverser's own node of each regret and strategy row)
 // with cp.async.bulk, counted on the warp's mbarrier; the lanes wait on the
 // barrier and compute from shared memory as decideRecordStaged does. The
-// wait is bounded: after kBarSpins polls the warp records an error in the
-// device error word and leaves the record, so a wait can never hang; once
-// the word is set, later records skip the copies and the wait altogether.
+// wait is bounded: after kBarSpins polls the warp drains, records an error
+// in the device error word and leaves the record, so a wait can never hang;
+// that warp's later records (persistent grids) skip their copies.
 // Layout per warp: [row kind][action][32 quads], contiguous segments.
 //
 // The record waits for the previous level itself (griddepcontrol.wait),
