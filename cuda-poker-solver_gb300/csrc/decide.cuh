@@ -125,10 +125,75 @@ __device__ __forceinline__ void prefetchStratLo(const DevTree& t, const DecRec& 
     asm volatile("prefetch.global.L2 [%0];" ::"l"(lo + ((size_t)a * nq + q) * 4));
 }
 
+// Actions of a record staged in shared memory (larger records stream).
+constexpr int kAsyncNa = 4;
+
+__device__ __forceinline__ void cpAsync16(float4* smem, const float* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpAsyncWaitAll() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+__device__ __forceinline__ void ld4s(const float4* p, float (&x)[4]) {
+  const float4 v = *p;
+  x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+
+// recordFoldedChildren through free stage entries of the record: per
+// folded-in child, the lane's quads of up to `slots` of its children are
+// copied with cp.async (all in flight at once, no registers held) and
+// summed from the stage in the children's order, so a child costs one
+// memory round trip per `slots` grandchildren instead of one per
+// grandchild. Entry j of the lane lives at C[j * stride + slot]; each
+// thread reads back only its own entries. The sums are bitwise those of
+// recordFoldedChildren.
+__device__ __forceinline__ void recordFoldedChildrenStaged(const DevRows<float>& rows,
+                                                           const DecRec& r, int lane, float4* C,
+                                                           int stride, int slot, int slots) {
+  if (!r.pre) return;
+  const int nq = quadsOf(r.n);
+  const int q = r.chunk * kRecQuads + lane;
+  const uint32_t* p = r.pre;
+  const int P = (int)p[0];
+  ++p;
+  for (int e = 0; e < P; ++e) {
+    const uint32_t row = p[0];
+    const int m = (int)p[1];
+    p += 2;
+    if (q < nq) {
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int b0 = 0; b0 < m; b0 += slots) {
+        const int k = m - b0 < slots ? m - b0 : slots;
+        for (int j = 0; j < k; ++j)
+          cpAsync16(&C[j * stride + slot], rows.cfv + (size_t)p[b0 + j] * 4 + 4 * q);
+        cpAsyncWaitAll();
+        for (int j = 0; j < k; ++j) {
+          float c[4];
+          ld4s(&C[j * stride + slot], c);
+          for (int l = 0; l < 4; ++l) v[l] += c[l];
+        }
+      }
+      for (int l = 0; l < 4; ++l)
+        if (4 * q + l >= r.n) v[l] = 0.f;
+      stq(rows.cfv + (size_t)row * 4 + 4 * q, v);
+    }
+    p += m;
+  }
+  // The rows just written are read next by copies of the async proxy (bulk
+  // and cp.async staging) and by other lanes.
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
 // Backward decide record (CFR mode, f32 rows), one warp: lane = quad.
+// With a stage (the record's unused shared-memory segments: `slots`
+// entries per lane at stage[j * stride + slot]), its folded-in children are
+// summed through it.
 __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<float>& rows,
-                                             const DecRec& r, int lane) {
-  recordFoldedChildren(rows, r, lane);  // this lane reads back only its own quads
+                                             const DecRec& r, int lane, float4* stage = nullptr,
+                                             int stride = 0, int slot = 0, int slots = 0) {
+  if (stage) recordFoldedChildrenStaged(rows, r, lane, stage, stride, slot, slots);
+  else recordFoldedChildren(rows, r, lane);  // this lane reads back only its own quads
   const int nq = quadsOf(r.n);
   const int q = r.chunk * kRecQuads + lane;
   if (q >= nq) return;
@@ -237,67 +302,10 @@ __device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<
 // use the streaming form.
 // Layout: [row kind][action][thread] float4, conflict-free.
 // ---------------------------------------------------------------------------
-constexpr int kAsyncNa = 4;
 __host__ __device__ constexpr size_t recStageBytes() {
   return (size_t)3 * kAsyncNa * kThreads * sizeof(float4);
 }
 
-__device__ __forceinline__ void cpAsync16(float4* smem, const float* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cpAsyncWaitAll() {
-  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
-}
-__device__ __forceinline__ void ld4s(const float4* p, float (&x)[4]) {
-  const float4 v = *p;
-  x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
-}
-
-// recordFoldedChildren through the record's child stage C, which is free at
-// that point: per folded-in child, the lane's quads of up to kAsyncNa of its
-// children are copied with cp.async (all in flight at once, no registers
-// held) and summed from C in the children's order, so a child costs one
-// memory round trip per kAsyncNa grandchildren instead of one per
-// grandchild. Entry j of the lane lives at C[j * stride + slot]; each
-// thread reads back only its own entries. The sums are bitwise those of
-// recordFoldedChildren.
-__device__ __forceinline__ void recordFoldedChildrenStaged(const DevRows<float>& rows,
-                                                           const DecRec& r, int lane, float4* C,
-                                                           int stride, int slot) {
-  if (!r.pre) return;
-  const int nq = quadsOf(r.n);
-  const int q = r.chunk * kRecQuads + lane;
-  const uint32_t* p = r.pre;
-  const int P = (int)p[0];
-  ++p;
-  for (int e = 0; e < P; ++e) {
-    const uint32_t row = p[0];
-    const int m = (int)p[1];
-    p += 2;
-    if (q < nq) {
-      float v[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int b0 = 0; b0 < m; b0 += kAsyncNa) {
-        const int k = m - b0 < kAsyncNa ? m - b0 : kAsyncNa;
-        for (int j = 0; j < k; ++j)
-          cpAsync16(&C[j * stride + slot], rows.cfv + (size_t)p[b0 + j] * 4 + 4 * q);
-        cpAsyncWaitAll();
-        for (int j = 0; j < k; ++j) {
-          float c[4];
-          ld4s(&C[j * stride + slot], c);
-          for (int l = 0; l < 4; ++l) v[l] += c[l];
-        }
-      }
-      for (int l = 0; l < 4; ++l)
-        if (4 * q + l >= r.n) v[l] = 0.f;
-      stq(rows.cfv + (size_t)row * 4 + 4 * q, v);
-    }
-    p += m;
-  }
-  // The rows just written are read next by copies of the async proxy (bulk
-  // and cp.async staging) and by other lanes.
-  asm volatile("fence.proxy.async.global;" ::: "memory");
-}
 
 // Backward decide record, staged, first part: the copies of the regret and
 // strategy rows of the traverser's own node (nothing for another node or a
@@ -330,12 +338,12 @@ __device__ __forceinline__ void decideRecordOwnRows(const DevTree& t, const DecR
 __device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRows<float>& rows,
                                                    const DecRec& r, int lane, float4* stage) {
   const int na = r.na;
-  if (na > kAsyncNa) {
-    decideRecord(t, rows, r, lane);
+  const int tid = (int)threadIdx.x;
+  if (na > kAsyncNa) {  // streams; its stage entries are free
+    decideRecord(t, rows, r, lane, stage, kThreads, tid, 3 * kAsyncNa);
     return;
   }
-  const int tid = (int)threadIdx.x;
-  recordFoldedChildrenStaged(rows, r, lane, stage, kThreads, tid);
+  recordFoldedChildrenStaged(rows, r, lane, stage, kThreads, tid, kAsyncNa);
   const int nq = quadsOf(r.n);
   const int q = r.chunk * kRecQuads + lane;
   if (q >= nq) return;
@@ -542,9 +550,9 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
                                                  unsigned long long* bar, uint32_t& phase,
                                                  bool& broken) {
   const int na = r.na;
-  if (na > kAsyncNa) {
+  if (na > kAsyncNa) {  // streams; the warp's stage is free
     pdlWait();
-    decideRecord(t, rows, r, lane);
+    decideRecord(t, rows, r, lane, stage, kRecQuads, lane, 3 * kAsyncNa);
     return;
   }
   const int nq = quadsOf(r.n);
@@ -574,7 +582,7 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
   if (r.own && q0 + lane < nq) prefetchStratLo(t, r, q0 + lane, nq);
   pdlWait();
   if (r.pre) {  // folded-in children: every lane's quads written before lane 0's copies
-    recordFoldedChildrenStaged(rows, r, lane, C, kRecQuads, lane);
+    recordFoldedChildrenStaged(rows, r, lane, C, kRecQuads, lane, kAsyncNa);
     __syncwarp();
     // The lanes' reads of C (generic proxy) before the child copies into it
     // (async proxy).

@@ -134,8 +134,11 @@ __host__ __device__ inline size_t sdGroupSmem(int maxN) {
 }
 // Fold groups: tab | rs4 | cs4[53] | card pairs (u16) | identical-combo
 // slots (i16) | group tail.
+// The fold's table (53 segment starts, then the card lists) is shorter than
+// the showdown's.
+__host__ __device__ inline int foldTabEntries(int maxN) { return (2 * maxN + 53 + 7) / 8 * 8; }
 __host__ __device__ inline size_t fdGroupSmem(int maxN) {
-  return (size_t)groupTabEntries(maxN) * 2 + 16 * ((size_t)groupRowEntries(maxN) + 53) +
+  return (size_t)foldTabEntries(maxN) * 2 + 16 * ((size_t)groupRowEntries(maxN) + 53) +
          (size_t)4 * ((maxN + 7) / 8 * 8) + sizeof(GroupRec);
 }
 
@@ -342,7 +345,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
 static __device__ void foldGroup(const DevTree& t, const DevRows<float>& rows, const GroupRec* grec,
                                  int tr, unsigned char* smem, int maxN) {
   uint16_t* csr = reinterpret_cast<uint16_t*>(smem);
-  float4* rs4 = reinterpret_cast<float4*>(smem + (size_t)groupTabEntries(maxN) * 2);
+  float4* rs4 = reinterpret_cast<float4*>(smem + (size_t)foldTabEntries(maxN) * 2);
   float4* cs4 = rs4 + groupRowEntries(maxN);  // [52] card sums, [52] total
   uint16_t* cardsS = reinterpret_cast<uint16_t*>(cs4 + 53);
   int16_t* sameS = reinterpret_cast<int16_t*>(cardsS + (maxN + 7) / 8 * 8);
@@ -417,11 +420,12 @@ __host__ __device__ constexpr int termThreadsFor(int maxN) {
   return maxN + 1 <= kSpan * 64 ? 64 : maxN + 1 <= kSpan * 128 ? 128 : kTermThreads;
 }
 constexpr int sdMinBlocks(int kT) { return 3 * kTermThreads / kT; }
-// Six 256-thread fold CTAs per SM (40 registers): +0.7% and +1.0% over
-// five on the full-range turn spots of 48,255 and 6,333 nodes. The
-// narrower instances stay at the five-CTA register budget, which measured
-// faster on the narrow-range spots.
-constexpr int fdMinBlocks(int kT) { return (kT == kTermThreads ? 6 : 5) * kTermThreads / kT; }
+// Seven 256-thread fold CTAs per SM (32 registers, 29.7 KB of shared memory
+// on the full-range lists): +0.6% on the 48,255-node turn and +0.7% on the
+// 6,333-node one over six (40 registers), +1.0% for six over five before.
+// The narrower instances stay at the five-CTA register budget, which
+// measured faster on the narrow-range spots.
+constexpr int fdMinBlocks(int kT) { return (kT == kTermThreads ? 7 : 5) * kTermThreads / kT; }
 
 template <int kT>
 static __global__ void __launch_bounds__(kT, sdMinBlocks(kT))
