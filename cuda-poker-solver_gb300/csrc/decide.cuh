@@ -49,6 +49,93 @@ __device__ __forceinline__ float rmSigma(float x, float acc, float inv, float un
   return __fmaf_rn(e, inv, q0);
 }
 
+// rmSigma for two lanes: the quotient of both by packed f32x2 instructions
+// (each lane rounded exactly as the scalar form rounds it; x - q0 acc as
+// q0 (-acc) + x, the same single rounding), then each lane's cases.
+__device__ __forceinline__ float2 rmSigma2(float2 x, float2 acc, float2 negAcc, float2 inv,
+                                           float uniform) {
+  const float2 q0 = __fmul2_rn(x, inv);
+  const float2 e = __ffma2_rn(q0, negAcc, x);
+  const float2 q = __ffma2_rn(e, inv, q0);
+  float2 s;
+  s.x = !(acc.x > 0.f) ? uniform : !(x.x > 0.f) ? 0.f : q.x;
+  s.y = !(acc.y > 0.f) ? uniform : !(x.y > 0.f) ? 0.f : q.y;
+  return s;
+}
+
+// One decide record's update from its staged quads (a lane's four combos
+// as two f32x2 pairs): node value, then per action the strategy sums and
+// regrets. R, S, C hold the regret, strategy and child value quads of
+// action a at R[a * stride], ...; the arithmetic and its order are the
+// scalar form's (decideRecord), lane by lane.
+struct RecCoef {
+  float pos, neg, avg, uniform;
+};
+__device__ __forceinline__ void recordUpdatePacked(const float4* R, const float4* S,
+                                                   const float4* C, int stride, int na,
+                                                   const bool (&live)[4], RecCoef k,
+                                                   float* out, float* reg, float* str,
+                                                   float* strLo, int nq, int q) {
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int a = 0; a < na; ++a) {
+    const float4 x = R[a * stride];
+    acc[0] += x.x > 0.f ? x.x : 0.f;
+    acc[1] += x.y > 0.f ? x.y : 0.f;
+    acc[2] += x.z > 0.f ? x.z : 0.f;
+    acc[3] += x.w > 0.f ? x.w : 0.f;
+  }
+  const float2 A0 = make_float2(acc[0], acc[1]), A1 = make_float2(acc[2], acc[3]);
+  const float2 N0 = make_float2(-acc[0], -acc[1]), N1 = make_float2(-acc[2], -acc[3]);
+  const float2 I0 = make_float2(rmInv(acc[0]), rmInv(acc[1]));
+  const float2 I1 = make_float2(rmInv(acc[2]), rmInv(acc[3]));
+  auto sigma = [&](const float4& x, float2& s0, float2& s1) {
+    s0 = rmSigma2(make_float2(x.x, x.y), A0, N0, I0, k.uniform);
+    s1 = rmSigma2(make_float2(x.z, x.w), A1, N1, I1, k.uniform);
+    if (!live[0]) s0.x = 0.f;
+    if (!live[1]) s0.y = 0.f;
+    if (!live[2]) s1.x = 0.f;
+    if (!live[3]) s1.y = 0.f;
+  };
+  float2 V0 = make_float2(0.f, 0.f), V1 = make_float2(0.f, 0.f);
+  for (int a = 0; a < na; ++a) {
+    float2 s0, s1;
+    sigma(R[a * stride], s0, s1);
+    const float4 c = C[a * stride];
+    V0 = __ffma2_rn(s0, make_float2(c.x, c.y), V0);
+    V1 = __ffma2_rn(s1, make_float2(c.z, c.w), V1);
+  }
+  *reinterpret_cast<float4*>(out + 4 * q) = make_float4(V0.x, V0.y, V1.x, V1.y);
+  const float2 NV0 = make_float2(-V0.x, -V0.y), NV1 = make_float2(-V1.x, -V1.y);
+  const float2 avg2 = make_float2(k.avg, k.avg);
+  for (int a = 0; a < na; ++a) {
+    const size_t o = ((size_t)a * nq + q) * 4;
+    const float4 rg = R[a * stride], sg = S[a * stride], c = C[a * stride];
+    float2 s0, s1;
+    sigma(rg, s0, s1);
+    float4 sgo;
+    if (strLo) {
+      float sv[4] = {sg.x, sg.y, sg.z, sg.w}, lo[4];
+      ldq(strLo + o, lo);
+      const float sl[4] = {s0.x, s0.y, s1.x, s1.y};
+      for (int l = 0; l < 4; ++l) stratComp(sv[l], lo[l], k.avg, sl[l]);
+      stq(strLo + o, lo);
+      sgo = make_float4(sv[0], sv[1], sv[2], sv[3]);
+    } else {
+      const float2 g0 = __ffma2_rn(make_float2(sg.x, sg.y), avg2, s0);
+      const float2 g1 = __ffma2_rn(make_float2(sg.z, sg.w), avg2, s1);
+      sgo = make_float4(g0.x, g0.y, g1.x, g1.y);
+    }
+    const float2 d0 = __fadd2_rn(make_float2(c.x, c.y), NV0);
+    const float2 d1 = __fadd2_rn(make_float2(c.z, c.w), NV1);
+    const float2 f0 = make_float2(rg.x >= 0.f ? k.pos : k.neg, rg.y >= 0.f ? k.pos : k.neg);
+    const float2 f1 = make_float2(rg.z >= 0.f ? k.pos : k.neg, rg.w >= 0.f ? k.pos : k.neg);
+    const float2 r0 = __ffma2_rn(make_float2(rg.x, rg.y), f0, d0);
+    const float2 r1 = __ffma2_rn(make_float2(rg.z, rg.w), f1, d1);
+    *reinterpret_cast<float4*>(str + o) = sgo;
+    *reinterpret_cast<float4*>(reg + o) = make_float4(r0.x, r0.y, r1.x, r1.y);
+  }
+}
+
 struct DecRec {
   uint32_t regQ, rowQ;
   int n, na, own, chunk, spot;
@@ -371,41 +458,10 @@ __device__ __forceinline__ void decideRecordStaged(const DevTree& t, const DevRo
   float* reg = t.regret + (size_t)r.regQ * 4;
   float* str = t.strat + (size_t)r.regQ * 4;
   const float* c3 = t.coef + (size_t)t.counter[r.spot] * 3;
-  const float pos = c3[0], neg = c3[1], avg = c3[2];
-  const float uniform = 1.f / (float)na;
-  float val[4] = {0.f, 0.f, 0.f, 0.f}, acc[4] = {0.f, 0.f, 0.f, 0.f};
+  const RecCoef kc{c3[0], c3[1], c3[2], 1.f / (float)na};
   cpAsyncWaitAll();
-  for (int a = 0; a < na; ++a) {
-    float x[4];
-    ld4s(&R[a * kThreads + tid], x);
-    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
-  }
-  float inv[4];
-  for (int l = 0; l < 4; ++l) inv[l] = rmInv(acc[l]);
-  for (int a = 0; a < na; ++a) {
-    float x[4], c[4];
-    ld4s(&R[a * kThreads + tid], x);
-    ld4s(&C[a * kThreads + tid], c);
-    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? rmSigma(x[l], acc[l], inv[l], uniform) : 0.f) * c[l];
-  }
-  stq(out + 4 * q, val);
-  float* strLo = t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr;
-  for (int a = 0; a < na; ++a) {
-    float rg[4], sg[4], c[4], lo[4] = {0.f, 0.f, 0.f, 0.f};
-    const size_t o = ((size_t)a * nq + q) * 4;
-    ld4s(&R[a * kThreads + tid], rg);
-    ld4s(&S[a * kThreads + tid], sg);
-    ld4s(&C[a * kThreads + tid], c);
-    if (strLo) ldq(strLo + o, lo);
-    for (int l = 0; l < 4; ++l) {
-      const float s = live[l] ? rmSigma(rg[l], acc[l], inv[l], uniform) : 0.f;
-      stratUpdate(sg[l], lo[l], avg, s, strLo);
-      rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
-    }
-    stq(str + o, sg);
-    if (strLo) stq(strLo + o, lo);
-    stq(reg + o, rg);
-  }
+  recordUpdatePacked(R + tid, S + tid, C + tid, kThreads, na, live, kc, out, reg, str,
+                     t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr, nq, q);
 }
 
 // Forward decide record, first part: the copies of the node's regret rows
@@ -443,22 +499,33 @@ __device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const De
   cpAsync16(&RR[tid], rows.reach[tr] + (size_t)r.rowQ * 4 + 4 * q);
   if (!regretsIssued) fwdRecordRegrets(t, r, lane, stage);
   const float uniform = 1.f / (float)na;
-  float rr[4], acc[4] = {0.f, 0.f, 0.f, 0.f};
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
   cpAsyncWaitAll();
-  ld4s(&RR[tid], rr);
+  const float4 rr = RR[tid];
   for (int a = 0; a < na; ++a) {
-    float x[4];
-    ld4s(&R[a * kThreads + tid], x);
-    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
+    const float4 x = R[a * kThreads + tid];
+    acc[0] += x.x > 0.f ? x.x : 0.f;
+    acc[1] += x.y > 0.f ? x.y : 0.f;
+    acc[2] += x.z > 0.f ? x.z : 0.f;
+    acc[3] += x.w > 0.f ? x.w : 0.f;
   }
-  float inv[4];
-  for (int l = 0; l < 4; ++l) inv[l] = rmInv(acc[l]);
+  // Two lanes per packed f32x2 instruction (each rounded as the scalar
+  // form rounds it).
+  const float2 A0 = make_float2(acc[0], acc[1]), A1 = make_float2(acc[2], acc[3]);
+  const float2 N0 = make_float2(-acc[0], -acc[1]), N1 = make_float2(-acc[2], -acc[3]);
+  const float2 I0 = make_float2(rmInv(acc[0]), rmInv(acc[1]));
+  const float2 I1 = make_float2(rmInv(acc[2]), rmInv(acc[3]));
+  const float2 rr0 = make_float2(rr.x, rr.y), rr1 = make_float2(rr.z, rr.w);
   for (int a = 0; a < na; ++a) {
-    float x[4], o[4];
-    ld4s(&R[a * kThreads + tid], x);
-    for (int l = 0; l < 4; ++l)
-      o[l] = 4 * q + l < r.n ? rr[l] * rmSigma(x[l], acc[l], inv[l], uniform) : 0.f;
-    stq(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q, o);
+    const float4 x = R[a * kThreads + tid];
+    float2 o0 = __fmul2_rn(rr0, rmSigma2(make_float2(x.x, x.y), A0, N0, I0, uniform));
+    float2 o1 = __fmul2_rn(rr1, rmSigma2(make_float2(x.z, x.w), A1, N1, I1, uniform));
+    if (4 * q + 0 >= r.n) o0.x = 0.f;
+    if (4 * q + 1 >= r.n) o0.y = 0.f;
+    if (4 * q + 2 >= r.n) o1.x = 0.f;
+    if (4 * q + 3 >= r.n) o1.y = 0.f;
+    *reinterpret_cast<float4*>(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q) =
+        make_float4(o0.x, o0.y, o1.x, o1.y);
   }
 }
 
@@ -616,40 +683,9 @@ __device__ __forceinline__ void decideRecordBulk(const DevTree& t, const DevRows
     return;
   }
   const float* c3 = t.coef + (size_t)t.counter[r.spot] * 3;
-  const float pos = c3[0], neg = c3[1], avg = c3[2];
-  const float uniform = 1.f / (float)na;
-  float val[4] = {0.f, 0.f, 0.f, 0.f}, acc[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int a = 0; a < na; ++a) {
-    float x[4];
-    ld4s(&R[a * kRecQuads + lane], x);
-    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
-  }
-  float inv[4];
-  for (int l = 0; l < 4; ++l) inv[l] = rmInv(acc[l]);
-  for (int a = 0; a < na; ++a) {
-    float x[4], c[4];
-    ld4s(&R[a * kRecQuads + lane], x);
-    ld4s(&C[a * kRecQuads + lane], c);
-    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? rmSigma(x[l], acc[l], inv[l], uniform) : 0.f) * c[l];
-  }
-  stq(out + 4 * q, val);
-  float* strLo = t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr;
-  for (int a = 0; a < na; ++a) {
-    float rg[4], sg[4], c[4], lo[4] = {0.f, 0.f, 0.f, 0.f};
-    const size_t o = ((size_t)a * nq + q) * 4;
-    ld4s(&R[a * kRecQuads + lane], rg);
-    ld4s(&S[a * kRecQuads + lane], sg);
-    ld4s(&C[a * kRecQuads + lane], c);
-    if (strLo) ldq(strLo + o, lo);
-    for (int l = 0; l < 4; ++l) {
-      const float s = live[l] ? rmSigma(rg[l], acc[l], inv[l], uniform) : 0.f;
-      stratUpdate(sg[l], lo[l], avg, s, strLo);
-      rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
-    }
-    stq(str + o, sg);
-    if (strLo) stq(strLo + o, lo);
-    stq(reg + o, rg);
-  }
+  const RecCoef kc{c3[0], c3[1], c3[2], 1.f / (float)na};
+  recordUpdatePacked(R + lane, S + lane, C + lane, kRecQuads, na, live, kc, out, reg, str,
+                     t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr, nq, q);
 }
 
 // ---------------------------------------------------------------------------
@@ -745,6 +781,7 @@ __device__ __forceinline__ void chanceRecordSlots(uint4 h, unsigned char* smem) 
 // Backward, last part (after the wait): parent value of one 128-combo
 // chunk = sum over the branches in branch order (cuda/gpu_cfr.cu:542-554),
 // 16 branch loads in flight per thread.
+constexpr int kChanceBatch = 24;
 __device__ __forceinline__ void chanceRecordSum(const DevRows<float>& rows, uint4 h,
                                                 const unsigned char* smem) {
   const int n = (int)(h.y & 0xffff), nb = (int)(h.y >> 16);
@@ -755,15 +792,15 @@ __device__ __forceinline__ void chanceRecordSum(const DevRows<float>& rows, uint
   if (i >= quadsOf(n) * 4) return;
   float v = 0.f;
   if (i < n) {
-    for (int b0 = 0; b0 < nb; b0 += 16) {
-      float x[16];
+    for (int b0 = 0; b0 < nb; b0 += kChanceBatch) {
+      float x[kChanceBatch];
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
+      for (int j = 0; j < kChanceBatch; ++j) {
         const int k = b0 + j < nb ? slot[(b0 + j) * kChanceChunk + threadIdx.x] : -1;
         x[j] = k >= 0 ? rowOf[b0 + j][k] : 0.f;
       }
 #pragma unroll
-      for (int j = 0; j < 16; ++j) v += x[j];
+      for (int j = 0; j < kChanceBatch; ++j) v += x[j];
     }
   }
   out[i] = v;

@@ -131,6 +131,25 @@ def test_solution_matches_oracle(name, iters):
     assert np.max(np.abs(g - r)) <= 0.10
 
 
+@pytest.mark.parametrize("name", ["river_c1", "turn_api", "turn_c2_uniform", "turn_c3"])
+def test_fp64_walks_equal_oracle_on_the_same_rows(name):
+    """The stats walks (FP64 on the device: EV against the average
+    strategy, best responses) evaluate a given strategy exactly: the
+    product's rows after 30 iterations, written into the FP64 oracle, give
+    the same EVs and exploitability there to 1e-9 (observed: 1e-14). This
+    pins the scorer that the solution gates and the batch checks use."""
+    spot = wl.NAMED[name]()
+    s = solver(spot)
+    s.solve(30)
+    mine = s.stats()
+    o = oracle(spot, precision=64)
+    o.set_rows(0, np.asarray(s.read_rows(0), dtype=np.float32))
+    o.set_rows(1, np.asarray(s.read_rows(1), dtype=np.float32))
+    ref = o.stats(spot.pot)
+    for k in ("ev_oop", "ev_ip", "exploitability"):
+        assert abs(mine[k] - ref[k]) <= 1e-9 * max(1.0, abs(ref[k])), (k, mine[k], ref[k])
+
+
 def test_deterministic_rows():
     spot = wl.turn_api()
     a, b = solver(spot), solver(spot)
