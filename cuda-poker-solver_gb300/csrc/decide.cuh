@@ -71,14 +71,16 @@ __device__ __forceinline__ float2 rmSigma2(float2 x, float2 acc, float2 negAcc, 
 struct RecCoef {
   float pos, neg, avg, uniform;
 };
-__device__ __forceinline__ void recordUpdatePacked(const float4* R, const float4* S,
-                                                   const float4* C, int stride, int na,
-                                                   const bool (&live)[4], RecCoef k,
-                                                   float* out, float* reg, float* str,
-                                                   float* strLo, int nq, int q) {
+// RQ(a), SQ(a), CQ(a): the lane's regret, strategy and child value quads of
+// action a (shared-memory stage or global rows).
+template <typename RQ, typename SQ, typename CQ>
+__device__ __forceinline__ void recordUpdatePackedBy(RQ Rq, SQ Sq, CQ Cq, int na,
+                                                     const bool (&live)[4], RecCoef k,
+                                                     float* out, float* reg, float* str,
+                                                     float* strLo, int nq, int q) {
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   for (int a = 0; a < na; ++a) {
-    const float4 x = R[a * stride];
+    const float4 x = Rq(a);
     acc[0] += x.x > 0.f ? x.x : 0.f;
     acc[1] += x.y > 0.f ? x.y : 0.f;
     acc[2] += x.z > 0.f ? x.z : 0.f;
@@ -99,8 +101,8 @@ __device__ __forceinline__ void recordUpdatePacked(const float4* R, const float4
   float2 V0 = make_float2(0.f, 0.f), V1 = make_float2(0.f, 0.f);
   for (int a = 0; a < na; ++a) {
     float2 s0, s1;
-    sigma(R[a * stride], s0, s1);
-    const float4 c = C[a * stride];
+    sigma(Rq(a), s0, s1);
+    const float4 c = Cq(a);
     V0 = __ffma2_rn(s0, make_float2(c.x, c.y), V0);
     V1 = __ffma2_rn(s1, make_float2(c.z, c.w), V1);
   }
@@ -109,7 +111,7 @@ __device__ __forceinline__ void recordUpdatePacked(const float4* R, const float4
   const float2 avg2 = make_float2(k.avg, k.avg);
   for (int a = 0; a < na; ++a) {
     const size_t o = ((size_t)a * nq + q) * 4;
-    const float4 rg = R[a * stride], sg = S[a * stride], c = C[a * stride];
+    const float4 rg = Rq(a), sg = Sq(a), c = Cq(a);
     float2 s0, s1;
     sigma(rg, s0, s1);
     float4 sgo;
@@ -134,6 +136,18 @@ __device__ __forceinline__ void recordUpdatePacked(const float4* R, const float4
     *reinterpret_cast<float4*>(str + o) = sgo;
     *reinterpret_cast<float4*>(reg + o) = make_float4(r0.x, r0.y, r1.x, r1.y);
   }
+}
+
+// The update from the record's shared-memory stage: entry a of the lane at
+// R[a * stride], S[a * stride], C[a * stride].
+__device__ __forceinline__ void recordUpdatePacked(const float4* R, const float4* S,
+                                                   const float4* C, int stride, int na,
+                                                   const bool (&live)[4], RecCoef k,
+                                                   float* out, float* reg, float* str,
+                                                   float* strLo, int nq, int q) {
+  recordUpdatePackedBy([&](int a) { return R[a * stride]; }, [&](int a) { return S[a * stride]; },
+                       [&](int a) { return C[a * stride]; }, na, live, k, out, reg, str, strLo,
+                       nq, q);
 }
 
 struct DecRec {
@@ -196,13 +210,6 @@ __device__ __forceinline__ void recordFoldedChildren(const DevRows<float>& rows,
   asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 
-// One entry of the cumulative-strategy update: compensated (stratComp)
-// where the tree carries low words, else the plain f32 form.
-__device__ __forceinline__ void stratUpdate(float& sg, float& lo, float avg, float sigma,
-                                            const float* strLo) {
-  if (strLo) stratComp(sg, lo, avg, sigma);
-  else sg = sg * avg + sigma;
-}
 // Asks for the low words of a record's strategy rows ahead of the update
 // (an L2 hint, no data): they are read only there, by plain loads.
 __device__ __forceinline__ void prefetchStratLo(const DevTree& t, const DecRec& r, int q, int nq) {
@@ -305,7 +312,6 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
   const float* c3 = t.coef + (size_t)t.counter[r.spot] * 3;
   const float pos = c3[0], neg = c3[1], avg = c3[2];
   const float uniform = 1.f / (float)na;
-  float val[4] = {0.f, 0.f, 0.f, 0.f}, acc[4] = {0.f, 0.f, 0.f, 0.f};
   // The children's value rows and the strategy rows are needed only after
   // the regret pass: start fetching them into L2 now (a hint, no data).
   for (int a = 0; a < na; ++a) {
@@ -314,39 +320,16 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
   }
   prefetchStratLo(t, r, q, nq);
   // Streaming form: a row is reloaded (a cache hit) instead of held in
-  // registers, which keeps the kernel at 40 registers and 48 warps per SM;
-  // the launches are bound by memory latency, not by instruction count.
-  for (int a = 0; a < na; ++a) {
-    float x[4];
-    ldq(reg + ((size_t)a * nq + q) * 4, x);
-    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
-  }
-  float inv[4];
-  for (int l = 0; l < 4; ++l) inv[l] = rmInv(acc[l]);
-  for (int a = 0; a < na; ++a) {
-    float x[4], c[4];
-    ldq(reg + ((size_t)a * nq + q) * 4, x);
-    ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, c);
-    for (int l = 0; l < 4; ++l) val[l] += (live[l] ? rmSigma(x[l], acc[l], inv[l], uniform) : 0.f) * c[l];
-  }
-  stq(out + 4 * q, val);
-  float* strLo = t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr;
-  for (int a = 0; a < na; ++a) {
-    float rg[4], sg[4], c[4], lo[4] = {0.f, 0.f, 0.f, 0.f};
-    const size_t o = ((size_t)a * nq + q) * 4;
-    ldq(reg + o, rg);
-    ldq(str + o, sg);
-    if (strLo) ldq(strLo + o, lo);
-    ldq(rows.cfv + (size_t)r.kid[a] * 4 + 4 * q, c);
-    for (int l = 0; l < 4; ++l) {
-      const float s = live[l] ? rmSigma(rg[l], acc[l], inv[l], uniform) : 0.f;
-      stratUpdate(sg[l], lo[l], avg, s, strLo);
-      rg[l] = rg[l] * (rg[l] >= 0.f ? pos : neg) + (c[l] - val[l]);
-    }
-    stq(str + o, sg);
-    if (strLo) stq(strLo + o, lo);
-    stq(reg + o, rg);
-  }
+  // registers; the launches are bound by memory latency, not by
+  // instruction count. The arithmetic is the staged records' (packed).
+  const uint32_t* kid = r.kid;
+  const float* cfv = rows.cfv;
+  const RecCoef kc{pos, neg, avg, uniform};
+  recordUpdatePackedBy(
+      [&](int a) { return *reinterpret_cast<const float4*>(reg + ((size_t)a * nq + q) * 4); },
+      [&](int a) { return *reinterpret_cast<const float4*>(str + ((size_t)a * nq + q) * 4); },
+      [&](int a) { return *reinterpret_cast<const float4*>(cfv + (size_t)kid[a] * 4 + 4 * q); },
+      na, live, kc, out, reg, str, t.stratLo ? t.stratLo + (size_t)r.regQ * 4 : nullptr, nq, q);
 }
 
 // Forward decide record (opponent node, CFR mode): child reach = reach x
