@@ -334,6 +334,39 @@ __device__ __forceinline__ void decideRecord(const DevTree& t, const DevRows<flo
 
 // Forward decide record (opponent node, CFR mode): child reach = reach x
 // sigma_a from the regrets (regret matching+).
+// Forward record arithmetic (the staged and streaming forms): child reach
+// = reach x sigma_a, two lanes per packed f32x2 instruction (each rounded
+// as the scalar form rounds it). RQ(a): the lane's regret quad of action a.
+template <typename RQ>
+__device__ __forceinline__ void fwdRecordPackedBy(RQ Rq, float4 rr, int na, const DecRec& r,
+                                                  int tr, const DevRows<float>& rows, int q) {
+  const float uniform = 1.f / (float)na;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int a = 0; a < na; ++a) {
+    const float4 x = Rq(a);
+    acc[0] += x.x > 0.f ? x.x : 0.f;
+    acc[1] += x.y > 0.f ? x.y : 0.f;
+    acc[2] += x.z > 0.f ? x.z : 0.f;
+    acc[3] += x.w > 0.f ? x.w : 0.f;
+  }
+  const float2 A0 = make_float2(acc[0], acc[1]), A1 = make_float2(acc[2], acc[3]);
+  const float2 N0 = make_float2(-acc[0], -acc[1]), N1 = make_float2(-acc[2], -acc[3]);
+  const float2 I0 = make_float2(rmInv(acc[0]), rmInv(acc[1]));
+  const float2 I1 = make_float2(rmInv(acc[2]), rmInv(acc[3]));
+  const float2 rr0 = make_float2(rr.x, rr.y), rr1 = make_float2(rr.z, rr.w);
+  for (int a = 0; a < na; ++a) {
+    const float4 x = Rq(a);
+    float2 o0 = __fmul2_rn(rr0, rmSigma2(make_float2(x.x, x.y), A0, N0, I0, uniform));
+    float2 o1 = __fmul2_rn(rr1, rmSigma2(make_float2(x.z, x.w), A1, N1, I1, uniform));
+    if (4 * q + 0 >= r.n) o0.x = 0.f;
+    if (4 * q + 1 >= r.n) o0.y = 0.f;
+    if (4 * q + 2 >= r.n) o1.x = 0.f;
+    if (4 * q + 3 >= r.n) o1.y = 0.f;
+    *reinterpret_cast<float4*>(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q) =
+        make_float4(o0.x, o0.y, o1.x, o1.y);
+  }
+}
+
 __device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<float>& rows,
                                                 int tr, const DecRec& r, int lane) {
   const int nq = quadsOf(r.n);
@@ -341,23 +374,14 @@ __device__ __forceinline__ void fwdDecideRecord(const DevTree& t, const DevRows<
   if (q >= nq) return;
   const int na = r.na;
   const float* src = t.regret + (size_t)r.regQ * 4;
-  const float uniform = 1.f / (float)na;
-  float rr[4], acc[4] = {0.f, 0.f, 0.f, 0.f};
-  ldq(rows.reach[tr] + (size_t)r.rowQ * 4 + 4 * q, rr);
-  for (int a = 0; a < na; ++a) {
-    float x[4];
-    ldq(src + ((size_t)a * nq + q) * 4, x);
-    for (int l = 0; l < 4; ++l) acc[l] += sigmaMass(x[l], 0);
-  }
-  float inv[4];
-  for (int l = 0; l < 4; ++l) inv[l] = rmInv(acc[l]);
-  for (int a = 0; a < na; ++a) {
-    float x[4], o[4];
-    ldq(src + ((size_t)a * nq + q) * 4, x);
-    for (int l = 0; l < 4; ++l)
-      o[l] = 4 * q + l < r.n ? rr[l] * rmSigma(x[l], acc[l], inv[l], uniform) : 0.f;
-    stq(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q, o);
-  }
+  // Every action's regret quad requested at once (L1 hints), then read in
+  // the regret-matching order.
+  for (int a = 0; a < na; ++a)
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(src + ((size_t)a * nq + q) * 4));
+  const float4 rr = *reinterpret_cast<const float4*>(rows.reach[tr] + (size_t)r.rowQ * 4 + 4 * q);
+  fwdRecordPackedBy(
+      [&](int a) { return *reinterpret_cast<const float4*>(src + ((size_t)a * nq + q) * 4); }, rr,
+      na, r, tr, rows, q);
 }
 
 // ---------------------------------------------------------------------------
@@ -481,35 +505,8 @@ __device__ __forceinline__ void fwdDecideRecordStaged(const DevTree& t, const De
   float4* R = stage + kThreads;           // [action][thread]
   cpAsync16(&RR[tid], rows.reach[tr] + (size_t)r.rowQ * 4 + 4 * q);
   if (!regretsIssued) fwdRecordRegrets(t, r, lane, stage);
-  const float uniform = 1.f / (float)na;
-  float acc[4] = {0.f, 0.f, 0.f, 0.f};
   cpAsyncWaitAll();
-  const float4 rr = RR[tid];
-  for (int a = 0; a < na; ++a) {
-    const float4 x = R[a * kThreads + tid];
-    acc[0] += x.x > 0.f ? x.x : 0.f;
-    acc[1] += x.y > 0.f ? x.y : 0.f;
-    acc[2] += x.z > 0.f ? x.z : 0.f;
-    acc[3] += x.w > 0.f ? x.w : 0.f;
-  }
-  // Two lanes per packed f32x2 instruction (each rounded as the scalar
-  // form rounds it).
-  const float2 A0 = make_float2(acc[0], acc[1]), A1 = make_float2(acc[2], acc[3]);
-  const float2 N0 = make_float2(-acc[0], -acc[1]), N1 = make_float2(-acc[2], -acc[3]);
-  const float2 I0 = make_float2(rmInv(acc[0]), rmInv(acc[1]));
-  const float2 I1 = make_float2(rmInv(acc[2]), rmInv(acc[3]));
-  const float2 rr0 = make_float2(rr.x, rr.y), rr1 = make_float2(rr.z, rr.w);
-  for (int a = 0; a < na; ++a) {
-    const float4 x = R[a * kThreads + tid];
-    float2 o0 = __fmul2_rn(rr0, rmSigma2(make_float2(x.x, x.y), A0, N0, I0, uniform));
-    float2 o1 = __fmul2_rn(rr1, rmSigma2(make_float2(x.z, x.w), A1, N1, I1, uniform));
-    if (4 * q + 0 >= r.n) o0.x = 0.f;
-    if (4 * q + 1 >= r.n) o0.y = 0.f;
-    if (4 * q + 2 >= r.n) o1.x = 0.f;
-    if (4 * q + 3 >= r.n) o1.y = 0.f;
-    *reinterpret_cast<float4*>(rows.reach[tr] + (size_t)r.kid[a] * 4 + 4 * q) =
-        make_float4(o0.x, o0.y, o1.x, o1.y);
-  }
+  fwdRecordPackedBy([&](int a) { return R[a * kThreads + tid]; }, RR[tid], na, r, tr, rows, q);
 }
 
 // ---------------------------------------------------------------------------
