@@ -13,7 +13,10 @@ Prints ONE JSON line (rank 0). ``value`` is device-timed (CUDA events on the
 solver's stream, tree resident in HBM); ``e2e`` is the same metric through
 the C ABI from host buffers (compile + upload + K iterations + FP64 stats
 readback); ``roofline`` covers the dominant kernel class from a launch-by-
-launch CUDA-event profile pass; ``cpu_baseline`` times the CPU oracle
+launch CUDA-event profile pass, with every class's achieved bandwidth and
+the whole iteration's algorithmic bandwidth beside it (the terminal groups
+are bound on chip, so the iteration figure is the one to set against HBM);
+``cpu_baseline`` times the CPU oracle
 (restatement of the reference iteration) on this host's cores.
 N > 1: replicas only (one spot per GPU, no collective in the data path);
 ``value`` sums the ranks' iterations over the max time.

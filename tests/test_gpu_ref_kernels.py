@@ -89,48 +89,49 @@ def test_at_least_as_accurate_as_reference_kernels(name, iters):
                                         ("turn_c2_uniform", 100), ("turn_c2_uniform", 500),
                                         ("turn_w52", 1000), ("turn_c3", 1000)])
 def test_solution_matches_reference_kernels(name, iters):
-    """After a full solve both strategies pass the solution gates against
-    each other: EVs within 0.01 chips, root strategy within 0.10 L-inf
-    (range-weighted frequencies of the root actions) and exploitability
-    within a factor 2 (or 0.01 chips where it is ~0, or both within 0.5%
-    of the pot of equilibrium - the batch and serve target - where f32
-    rounding sets it). The reference's average strategy is scored by the
-    product's FP64 walks after writing its rows in (those walks equal the
-    oracle's FP64 evaluation of the same rows to 1e-12: test_gpu_parity).
-    Its fold kernel sums with shared-memory atomics, so two of its runs of
-    the same iterations differ: it is solved twice. Where its runs are far
-    from exact equilibrium the EVs cannot agree to 0.01 chips: a profile
-    with exploitability e has each player's EV within 2e of the game value,
-    so two profiles' EVs may differ by 2(e_a + e_b); the gate then allows
-    e_a + e_b, half of that. On turn_c3 (pot 100) the reference's runs
-    gave exploitabilities of 0.015 to 0.31 chips and root EVs 47.394 to
-    47.402; the product's 0.093 and 47.413. turn_c3 is the benchmark's own
-    workload (48,255 nodes, 1,000 iterations), turn_c2_uniform the
-    6,333-node turn at 500."""
+    """After a full solve the product's strategy passes the solution gates
+    against the reference kernels': EVs within 0.01 chips, root strategy
+    within 0.10 L-inf (range-weighted frequencies of the root actions),
+    exploitability no worse than twice the reference's (or within 0.01
+    chips where it is ~0, or both within 0.5% of the pot - the batch and
+    serve target - where f32 rounding sets it). The reference's average
+    strategy is scored by the product's FP64 walks after writing its rows
+    in (those walks equal the oracle's FP64 evaluation of the same rows to
+    1e-12: test_gpu_parity).
+
+    The reference's kernels are not deterministic (their fold sums use
+    shared-memory atomics), and on turn_c3 their runs are erratic: four
+    runs in one process gave exploitabilities of 0.062, 0.139, 0.747 and
+    0.041 chips (pot 100) and root EVs of 47.414, 47.412, 47.373 and
+    47.415, against the product's 0.093 and 47.413 on every run. So the
+    reference is solved three times and the gates compare with its best
+    run (lowest exploitability). Where a run is far from equilibrium the
+    EVs cannot agree to 0.01 chips: a profile with exploitability e holds
+    each player's EV within 2e of the game value, so the EV gate is 0.01
+    chips or e_a + e_b (half of 2(e_a + e_b)), whichever is larger.
+    turn_c3 is the benchmark's own workload (48,255 nodes, 1,000
+    iterations), turn_c2_uniform the 6,333-node turn at 500."""
     spot = wl.NAMED[name]()
-    theirs_runs = []
-    for _ in range(2):
+    runs = []
+    for _ in range(3):
         r = reference(spot)
         r.solve(iters)
         scored = solver(spot)
         scored.solve(0)
         scored.write_rows(1, r.rows(1))
-        theirs_runs.append(scored.stats())
+        runs.append((scored.stats(), np.asarray(scored.root_strategy())))
         r.close()
+    theirs, ref = min(runs, key=lambda x: x[0]["exploitability"])
     s = solver(spot)
     s.solve(iters)
     mine = s.stats()
-    a = mine["exploitability"]
-    for side in ("ev_oop", "ev_ip"):
-        d, b = min((abs(mine[side] - t[side]), t["exploitability"]) for t in theirs_runs)
-        assert d < max(0.01, a + b), (side, mine, theirs_runs)
-    theirs = theirs_runs[0]
     a, b = mine["exploitability"], theirs["exploitability"]
-    # Where both solutions are within 0.5% of the pot of exact equilibrium
-    # (the batch and serve target), their exploitability is set by f32
-    # rounding, and the ratio is noise (the reference's own runs above).
+    for side in ("ev_oop", "ev_ip"):
+        assert abs(mine[side] - theirs[side]) < max(0.01, a + b), (side, mine, runs)
+    # Where both solutions are within 0.5% of the pot of exact equilibrium,
+    # their exploitability is set by f32 rounding, and the ratio is noise.
     converged = max(a, b) <= 0.005 * spot.pot
-    assert abs(a - b) < 0.01 or converged or 0.5 <= a / max(b, 1e-9) <= 2.0, (a, b)
-    g, ref = np.asarray(s.root_strategy()), np.asarray(scored.root_strategy())
+    assert abs(a - b) < 0.01 or converged or a <= 2.0 * b, (a, b, runs)
+    g = np.asarray(s.root_strategy())
     assert g.shape == ref.shape
     assert float(np.max(np.abs(g - ref))) <= 0.10, (g, ref)
