@@ -498,7 +498,9 @@ int pps_gb_time_iterations(pps_gb_solver* h, int n, double* ms) {
 
 int pps_gb_probe_bounded_wait(pps_gb_solver* h, int spins) {
   return guarded([&] {
-    if (spins < 1) throw Error{PPS_GB_E_ARG, "spins must be positive"};
+    // At most the records' own bound (65,536 polls a round), so that the
+    // probe ends as quickly as their give-up path does.
+    if (spins < 1 || spins > (1 << 16)) throw Error{PPS_GB_E_ARG, "spins must be in [1, 65536]"};
     core(h).probeBoundedWait(spins);
   });
 }

@@ -278,7 +278,8 @@ int pps_gb_profile(pps_gb_solver* h, int n, int flags, pps_gb_kernel_stat* out,
  * on the solver's stream, one warp waits on its shared-memory barrier for a
  * copy that is never issued, with the same bounded wait and give-up path
  * as the iteration's bulk-copied records (`spins` polls per round, one
- * round plus four drain rounds). The give-up sets the solver's device error
+ * round plus four drain rounds; 1 <= spins <= 65536, the records' own
+ * bound, else PPS_GB_E_ARG). The give-up sets the solver's device error
  * word, so the call returns PPS_GB_E_CUDA ("a device wait timed out"); the
  * solver stays usable. No GPU fault is involved. */
 int pps_gb_probe_bounded_wait(pps_gb_solver* h, int spins);
