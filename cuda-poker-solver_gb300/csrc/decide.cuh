@@ -63,16 +63,17 @@ __device__ __forceinline__ float2 rmSigma2(float2 x, float2 acc, float2 negAcc, 
   return s;
 }
 
-// One decide record's update from its staged quads (a lane's four combos
-// as two f32x2 pairs): node value, then per action the strategy sums and
-// regrets. R, S, C hold the regret, strategy and child value quads of
-// action a at R[a * stride], ...; the arithmetic and its order are the
-// scalar form's (decideRecord), lane by lane.
+// DCFR coefficients of the iteration and the uniform strategy of the node.
 struct RecCoef {
   float pos, neg, avg, uniform;
 };
-// RQ(a), SQ(a), CQ(a): the lane's regret, strategy and child value quads of
-// action a (shared-memory stage or global rows).
+// One traverser decide record's update, a lane's four combos as two f32x2
+// pairs: regret matching, the node value, then per action the strategy sums
+// and the regrets. The arithmetic and its order per combo are those of the
+// per-node form (kernels.cuh decideChunk; the reference's
+// cuda/gpu_cfr.cu:479-523), each lane rounded as a scalar would be. RQ(a),
+// SQ(a), CQ(a) give the lane's regret, strategy and child value quads of
+// action a (a shared-memory stage or the global rows).
 template <typename RQ, typename SQ, typename CQ>
 __device__ __forceinline__ void recordUpdatePackedBy(RQ Rq, SQ Sq, CQ Cq, int na,
                                                      const bool (&live)[4], RecCoef k,
