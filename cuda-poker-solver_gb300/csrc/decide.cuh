@@ -69,9 +69,9 @@ struct RecCoef {
 };
 // One traverser decide record's update, a lane's four combos as two f32x2
 // pairs: regret matching, the node value, then per action the strategy sums
-// and the regrets. The arithmetic and its order per combo are those of the
-// per-node form (kernels.cuh decideChunk; the reference's
-// cuda/gpu_cfr.cu:479-523), each lane rounded as a scalar would be. RQ(a),
+// and the regrets, by the formulas of the per-node form (kernels.cuh
+// decideChunk; the reference's cuda/gpu_cfr.cu:479-523), each lane rounded
+// as the scalar operation would round it. RQ(a),
 // SQ(a), CQ(a) give the lane's regret, strategy and child value quads of
 // action a (a shared-memory stage or the global rows).
 template <typename RQ, typename SQ, typename CQ>
