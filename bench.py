@@ -577,6 +577,17 @@ def main():
                             for k, v in prof.items()},
                 "iteration_frac": None}
     roofline["iteration_frac"] = roofline["iteration_gbs"] / peak
+    # The terminal classes (showdown, fold groups) are bound on chip - the
+    # showdown groups by the shared-memory pipe - and move few bytes for
+    # their time; the decide levels are the HBM-bound classes.
+    onchip = {"bwd_showdown": "shared-memory pipe", "bwd_fold": "load latency"}
+    hbm = {k: v["frac"] for k, v in roofline["profile"].items()
+           if k in ("bwd_interior", "fwd_level") and v["frac"] is not None}
+    roofline["note"] = (
+        "dominant class %s%s; HBM-bound classes: %s; whole iteration %.3f of peak"
+        % (name, " (bound on chip: %s, see profiles/turn_c3_top_kernels_ncu.md)" % onchip[name]
+           if name in onchip else "",
+           ", ".join("%s %.3f" % kv for kv in sorted(hbm.items())), roofline["iteration_frac"]))
     batched = None
     if args.batch_spots > 0:
         spots = wl.batched(args.batch_spots)
