@@ -445,24 +445,26 @@ __device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, in
   const int bn = no >> 5;
   // Four combos per thread per round: their table entries are loaded first
   // so the loads overlap.
-  for (int i0 = threadIdx.x; i0 < nt4; i0 += 4 * blockDim.x) {
+  for (int k0 = threadIdx.x; k0 < nt4; k0 += 4 * blockDim.x) {
     ShowdownInfo fs[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const int i = i0 + j * blockDim.x;
-      if (i < nt) fs[j] = info[i];
+      const int k = k0 + j * blockDim.x;
+      if (k < nt) fs[j] = info[k];
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-    const int i = i0 + j * blockDim.x;
-    if (i >= nt4) break;
-    if (i >= nt) {
-      out[i] = T(0);
+    const int k = k0 + j * blockDim.x;
+    if (k >= nt4) break;
+    if (k >= nt) {
+      out[k] = T(0);
       continue;
     }
-    // The entry holds the group kernels' padded indices (layout.h); this
-    // kernel's arrays are unpadded.
+    // The entry holds the group kernels' padded indices and its combo's
+    // offset in its 32-entry window (layout.h); this kernel's arrays are
+    // unpadded.
     const ShowdownInfo f = fs[j];
+    const int i = (k & ~31) | (int)((f.z >> 24) & 31);
     const int le = unpad8((int)(f.w & 0x7ff)), te = unpad8((int)((f.w >> 11) & 0x7ff));
     const T x1le = ws.X[unpad8((int)(f.x & 0xfff))], x1te = ws.X[unpad8((int)((f.x >> 12) & 0xfff))];
     const T x1end = ws.X[unpad8((int)(f.y & 0xfff))], x2le = ws.X[unpad8((int)((f.y >> 12) & 0xfff))];

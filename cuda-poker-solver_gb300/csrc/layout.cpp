@@ -57,6 +57,71 @@ struct StateParts {
   std::vector<ShowdownInfo> info[2];
 };
 
+// Reorders one traverser's showdown entries within each 32-entry window (the
+// combos one warp evaluates together). A float4 gather from shared memory is
+// served a quarter warp (eight lanes) at a time, and lanes whose indices
+// fall in one 16-byte bank group (index mod 8) at different addresses are
+// served one after another: list order puts about two such collisions in
+// every quarter warp and gather. The window's entries are dealt to its
+// quarter warps greedily (each slot takes the remaining entry that adds the
+// fewest collisions over the loop's ten gathers, the lowest index on ties),
+// and z bits 24-28 record each entry's offset in list order.
+void spreadShowdownBanks(std::vector<ShowdownInfo>& info) {
+  constexpr int kG = 10;
+  const int n = (int)info.size();
+  for (int w0 = 0; w0 < n; w0 += 32) {
+    const int m = std::min(32, n - w0);
+    int A[32][kG];
+    for (int k = 0; k < m; ++k) {
+      const ShowdownInfo& f = info[w0 + k];
+      const int sHi = (int)((f.x >> 24) | ((f.y >> 16) & 0xf00));
+      const int v[kG] = {(int)(f.x & 0xfff), (int)((f.x >> 12) & 0xfff), (int)(f.y & 0xfff),
+                         (int)((f.y >> 12) & 0xfff), (int)(f.z & 0xfff), (int)((f.z >> 12) & 0xfff),
+                         sHi, sHi - 1 - (int)((f.w >> 28) & 1), (int)(f.w & 0x7ff),
+                         (int)((f.w >> 11) & 0x7ff)};
+      std::copy(v, v + kG, A[k]);
+    }
+    bool used[32] = {};
+    ShowdownInfo out[32];
+    int pos = 0;
+    for (int q0 = 0; q0 < m; q0 += 8) {
+      // Per gather: the quarter warp's distinct indices and, per bank group,
+      // how many of them it holds.
+      int addr[kG][8], na[kG] = {}, cnt[kG][8] = {}, top[kG] = {};
+      for (int s = 0; s < std::min(8, m - q0); ++s) {
+        int best = -1, bestCost = 1 << 30;
+        for (int k = 0; k < m; ++k) {
+          if (used[k]) continue;
+          int cost = 0;
+          for (int g = 0; g < kG; ++g) {
+            const int a = A[k][g];
+            bool dup = false;
+            for (int j = 0; j < na[g]; ++j) dup |= addr[g][j] == a;
+            if (!dup && cnt[g][a & 7] + 1 > top[g]) ++cost;
+          }
+          if (cost < bestCost) {
+            bestCost = cost;
+            best = k;
+          }
+        }
+        used[best] = true;
+        for (int g = 0; g < kG; ++g) {
+          const int a = A[best][g];
+          bool dup = false;
+          for (int j = 0; j < na[g]; ++j) dup |= addr[g][j] == a;
+          if (dup) continue;
+          addr[g][na[g]++] = a;
+          top[g] = std::max(top[g], ++cnt[g][a & 7]);
+        }
+        out[pos] = info[w0 + best];
+        out[pos].z |= (uint32_t)best << 24;
+        ++pos;
+      }
+    }
+    std::copy(out, out + m, info.begin() + w0);
+  }
+}
+
 void buildStateParts(const Tree& t, int s, StateParts& P) {
   const BoardState& st = t.states[s];
   for (int p = 0; p < 2; ++p) {
@@ -190,6 +255,7 @@ void buildStateParts(const Tree& t, int s, StateParts& P) {
                ((uint32_t)(ks1 > 0) << 29);
       P.info[tr].push_back(info);
     }
+    spreadShowdownBanks(P.info[tr]);
   }
 }
 

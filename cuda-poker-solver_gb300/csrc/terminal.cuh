@@ -312,13 +312,15 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   outRows4(out, rows, rc->mask, cfvQOf(rc));
   const int nt4 = quadsOf(nt) * 4;
 #pragma unroll 2
-  for (int i = threadIdx.x; i < nt4; i += blockDim.x) {
-    if (i >= nt) {
-      storeOut4(out, i, zero4());
+  for (int k = threadIdx.x; k < nt4; k += blockDim.x) {
+    if (k >= nt) {
+      storeOut4(out, k, zero4());
       continue;
     }
-    // The entry holds the shared-memory indices themselves (layout.h).
-    const ShowdownInfo f = info[i];
+    // The entry holds the shared-memory indices themselves and its combo's
+    // offset in its warp window (layout.h).
+    const ShowdownInfo f = info[k];
+    const int i = (k & ~31) | (int)((f.z >> 24) & 31);
     const float4 x1le = X4[f.x & 0xfff], x1te = X4[(f.x >> 12) & 0xfff];
     const float4 x1end = X4[f.y & 0xfff], x2le = X4[(f.y >> 12) & 0xfff];
     const float4 x2te = X4[f.z & 0xfff], x2end = X4[(f.z >> 12) & 0xfff];
