@@ -461,10 +461,10 @@ __device__ void showdownNode(const DevTree& t, const DevRows<T>& rows, int u, in
       continue;
     }
     // The entry holds the group kernels' padded indices and its combo's
-    // offset in its 32-entry window (layout.h); this kernel's arrays are
+    // offset in its window (layout.h); this kernel's arrays are
     // unpadded.
     const ShowdownInfo f = fs[j];
-    const int i = (k & ~31) | (int)((f.z >> 24) & 31);
+    const int i = showdownCombo(k, f);
     const int le = unpad8((int)(f.w & 0x7ff)), te = unpad8((int)((f.w >> 11) & 0x7ff));
     const T x1le = ws.X[unpad8((int)(f.x & 0xfff))], x1te = ws.X[unpad8((int)((f.x >> 12) & 0xfff))];
     const T x1end = ws.X[unpad8((int)(f.y & 0xfff))], x2le = ws.X[unpad8((int)((f.y >> 12) & 0xfff))];

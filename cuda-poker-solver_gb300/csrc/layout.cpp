@@ -57,8 +57,8 @@ struct StateParts {
   std::vector<ShowdownInfo> info[2];
 };
 
-// Reorders one traverser's showdown entries within each 32-entry window (the
-// combos one warp evaluates together). A float4 gather from shared memory is
+// Reorders one traverser's showdown entries within each kSdWindow-entry
+// window (the combos one warp evaluates together). A float4 gather from shared memory is
 // served a quarter warp (eight lanes) at a time, and lanes whose indices
 // fall in one 16-byte bank group (index mod 8) at different addresses are
 // served one after another: list order puts about two such collisions in
@@ -69,9 +69,9 @@ struct StateParts {
 void spreadShowdownBanks(std::vector<ShowdownInfo>& info) {
   constexpr int kG = 10;
   const int n = (int)info.size();
-  for (int w0 = 0; w0 < n; w0 += 32) {
-    const int m = std::min(32, n - w0);
-    int A[32][kG];
+  for (int w0 = 0; w0 < n; w0 += kSdWindow) {
+    const int m = std::min(kSdWindow, n - w0);
+    int A[kSdWindow][kG];
     for (int k = 0; k < m; ++k) {
       const ShowdownInfo& f = info[w0 + k];
       const int sHi = (int)((f.x >> 24) | ((f.y >> 16) & 0xf00));
@@ -81,8 +81,8 @@ void spreadShowdownBanks(std::vector<ShowdownInfo>& info) {
                          (int)((f.w >> 11) & 0x7ff)};
       std::copy(v, v + kG, A[k]);
     }
-    bool used[32] = {};
-    ShowdownInfo out[32];
+    bool used[kSdWindow] = {};
+    ShowdownInfo out[kSdWindow];
     int pos = 0;
     for (int q0 = 0; q0 < m; q0 += 8) {
       // Per gather: the quarter warp's distinct indices and, per bank group,

@@ -94,18 +94,23 @@ PPS_HD inline int unpad8(int p) { return p - p / 9; }
 // entries below le / te. Fields:
 //   x = pad8(a1 + k1le) | pad8(a1 + k1te) << 12 | (sHi & 0xff) << 24
 //   y = pad8(a1 + len1) | pad8(a2 + k2le) << 12 | (sHi >> 8) << 24
-//   z = pad8(a2 + k2te) | pad8(a2 + len2) << 12 | (i & 31) << 24
+//   z = pad8(a2 + k2te) | pad8(a2 + len2) << 12 | (i % kSdWindow) << 24
 //   w = pad8(le) | pad8(te) << 11 | (le >> 8) << 22 | (te >> 8) << 25 |
 //       (step - 1) << 28 | hasSame << 29
 // The identical combo's reach is the step of card c1's run at its entry:
 // run[sHi] - run[sHi - step] (step 1, or 2 across a padding entry), where
 // hasSame is set; otherwise sHi = 2, step 1, read and discarded.
-// Entries are reordered within each 32-entry window (one warp's combos) to
-// spread every quarter warp's indices over the shared-memory bank groups:
-// entry k belongs to traverser combo i = (k & ~31) | (z >> 24 & 31).
+// Entries are reordered within each kSdWindow-entry window (one warp's
+// combos) to spread every quarter warp's indices over the shared-memory bank
+// groups: entry k belongs to traverser combo
+// i = (k & ~(kSdWindow - 1)) | (z >> 24 & (kSdWindow - 1)).
+constexpr int kSdWindow = 32;
 struct alignas(16) ShowdownInfo {
   uint32_t x, y, z, w;
 };
+PPS_HD inline int showdownCombo(int k, const ShowdownInfo& f) {
+  return (k & ~(kSdWindow - 1)) | (int)((f.z >> 24) & (kSdWindow - 1));
+}
 
 // Four terminal nodes (showdown or fold) of one depth and one board state,
 // evaluated together (-1: no node).

@@ -320,7 +320,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
     // The entry holds the shared-memory indices themselves and its combo's
     // offset in its warp window (layout.h).
     const ShowdownInfo f = info[k];
-    const int i = (k & ~31) | (int)((f.z >> 24) & 31);
+    const int i = showdownCombo(k, f);
     const float4 x1le = X4[f.x & 0xfff], x1te = X4[(f.x >> 12) & 0xfff];
     const float4 x1end = X4[f.y & 0xfff], x2le = X4[(f.y >> 12) & 0xfff];
     const float4 x2te = X4[f.z & 0xfff], x2end = X4[(f.z >> 12) & 0xfff];
