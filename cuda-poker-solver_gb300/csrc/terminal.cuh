@@ -311,7 +311,7 @@ static __device__ void showdownGroup(const DevTree& t, const DevRows<float>& row
   float* out[4];
   outRows4(out, rows, rc->mask, cfvQOf(rc));
   const int nt4 = quadsOf(nt) * 4;
-#pragma unroll 2
+#pragma unroll 3
   for (int k = threadIdx.x; k < nt4; k += blockDim.x) {
     if (k >= nt) {
       storeOut4(out, k, zero4());
