@@ -47,6 +47,16 @@ V* alloc(size_t count, size_t& bytes) {
   return p;
 }
 
+// First group of a group task list whose groups are consecutive (a layout
+// appends each depth's groups together), else -1.
+int consecutiveGroups(const std::vector<int>& tasks) {
+  if (tasks.empty()) return -1;
+  const int g0 = (int)((unsigned)tasks[0] >> 8);
+  for (size_t i = 0; i < tasks.size(); ++i)
+    if ((int)((unsigned)tasks[i] >> 8) != g0 + (int)i) return -1;
+  return g0;
+}
+
 }  // namespace
 
 struct Engine::Dev {
@@ -308,10 +318,14 @@ void Engine::buildPlans() {
       }
     }
     for (int dd = 0; dd < D; ++dd) {
-      if (d.sdG[dd].count)
+      if (d.sdG[dd].count) {
         h.sd[dd] = {kSdGroup, tr, d.sdG[dd], groupBytes(L_.sdGroupTasks[dd], tr)};
-      if (d.fdG[dd].count)
+        h.sd[dd].groupBase = consecutiveGroups(L_.sdGroupTasks[dd]);
+      }
+      if (d.fdG[dd].count) {
         h.fd[dd] = {kFdGroup, tr, d.fdG[dd], groupBytes(L_.fdGroupTasks[dd], tr)};
+        h.fd[dd].groupBase = consecutiveGroups(L_.fdGroupTasks[dd]);
+      }
     }
     // Backward per level (layout.h): each launch waits for the
     // terminal depths its nodes read.

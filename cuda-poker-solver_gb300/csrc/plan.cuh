@@ -55,6 +55,10 @@ struct Launch {
   bool late = false;      // kFwdMix: late triggers (the fused plan)
   bool early = false;     // kFwdMix: regret copies before the wait (first half-step only)
   bool termWait = false;  // kBwdFused: its terminal groups wait for the previous grid
+  // kSdGroup / kFdGroup: the list's groups are groupBase, groupBase + 1, ...
+  // (one spot's layout): the kernels take a CTA's record from its task
+  // index instead of loading the task word first. -1: read the list.
+  int groupBase = -1;
 };
 
 // What the level launches of a plan read: the tree, the f32 rows, the
@@ -95,12 +99,14 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
                                                  kModeCFR);
       break;
     case kSdGroup:
-      launchSdGroups(cappedGrid(g, a.shape.sdCap), a.smemSd, s, a.tree, a.rows, a.groups, tk,
-                     l.list.count, l.tr, a.maxN);
+      launchSdGroups(cappedGrid(g, a.shape.sdCap), a.smemSd, s, a.tree, a.rows,
+                     l.groupBase >= 0 ? a.groups + 2 * (size_t)l.groupBase : a.groups,
+                     l.groupBase >= 0 ? nullptr : tk, l.list.count, l.tr, a.maxN);
       break;
     case kFdGroup:
-      launchFdGroups(cappedGrid(g, a.shape.fdCap), a.smemFd, s, a.tree, a.rows, a.groups, tk,
-                     l.list.count, l.tr, a.maxN);
+      launchFdGroups(cappedGrid(g, a.shape.fdCap), a.smemFd, s, a.tree, a.rows,
+                     l.groupBase >= 0 ? a.groups + 2 * (size_t)l.groupBase : a.groups,
+                     l.groupBase >= 0 ? nullptr : tk, l.list.count, l.tr, a.maxN);
       break;
     case kBwdFused: {
       cudaLaunchConfig_t cfg = {};

@@ -429,13 +429,20 @@ constexpr int sdMinBlocks(int kT) { return 3 * kTermThreads / kT; }
 // measured faster on the narrow-range spots.
 constexpr int fdMinBlocks(int kT) { return (kT == kTermThreads ? 7 : 5) * kTermThreads / kT; }
 
+// Group record of task i: from the task word's node field, or, for a list
+// of consecutive groups (tasks null, groups at its first), the i-th.
+static __device__ __forceinline__ const GroupRec* groupOf(const GroupRec* groups,
+                                                          const int* tasks, int i, int tr) {
+  return groups + 2 * (tasks ? (unsigned)tasks[i] >> 8 : (unsigned)i) + tr;
+}
+
 template <int kT>
 static __global__ void __launch_bounds__(kT, sdMinBlocks(kT))
 sdGroupK(DevTree t, DevRows<float> rows, const GroupRec* __restrict__ groups,
          const int* __restrict__ tasks, int count, int tr, int maxN) {
   extern __shared__ __align__(16) unsigned char smem[];
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
-    showdownGroup(t, rows, groups + 2 * ((unsigned)tasks[i] >> 8) + tr, tr, smem, maxN);
+    showdownGroup(t, rows, groupOf(groups, tasks, i, tr), tr, smem, maxN);
     __syncthreads();  // the next task reuses the shared memory
   }
 }
@@ -446,7 +453,7 @@ fdGroupK(DevTree t, DevRows<float> rows, const GroupRec* __restrict__ groups,
          const int* __restrict__ tasks, int count, int tr, int maxN) {
   extern __shared__ __align__(16) unsigned char smem[];
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
-    foldGroup(t, rows, groups + 2 * ((unsigned)tasks[i] >> 8) + tr, tr, smem, maxN);
+    foldGroup(t, rows, groupOf(groups, tasks, i, tr), tr, smem, maxN);
     __syncthreads();
   }
 }
