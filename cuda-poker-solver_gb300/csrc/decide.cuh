@@ -825,6 +825,8 @@ __host__ __device__ constexpr size_t bwdStageBytes() {
 // returned (so a grid that has launched implies that the grid two places
 // before it has completed; the fused plan relies on that), instead of at
 // its start.
+// recTasks null: the level's records are recBase + k recStride (16-byte
+// units), at one stride from the first.
 // early: the records ask for their regret rows before the wait. Only for
 // the first half-step of an iteration (traverser 0): the regrets it reads
 // are the other player's, written by the second half-step of an earlier
@@ -834,7 +836,7 @@ __host__ __device__ constexpr size_t bwdStageBytes() {
 static __global__ void __launch_bounds__(kThreads, 10)
 fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
              const uint32_t* __restrict__ recTasks, int nRec, const uint32_t* __restrict__ chance,
-             int nCh, int tr, int late, int early) {
+             int nCh, int tr, int late, int early, uint32_t recBase, uint32_t recStride) {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* stage = reinterpret_cast<float4*>(smem);
   if (!late) pdlTrigger();
@@ -847,7 +849,7 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
     if (i >= nCh) {
       const int k = (i - nCh) * kRecWarps + (int)(threadIdx.x >> 5);
       if (k >= nRec) continue;
-      const DecRec r = loadRec(recs, recTasks[k]);
+      const DecRec r = loadRec(recs, recTasks ? recTasks[k] : recBase + (uint32_t)k * recStride);
       if (early) fwdRecordRegrets(t, r, lane, stage);
       pdlWait();
       waited = true;

@@ -47,6 +47,16 @@ V* alloc(size_t count, size_t& bytes) {
   return p;
 }
 
+// A record list at one stride from its first record: {first, stride}, else
+// {-1, 0} (a layout places each forward level's records so).
+std::pair<long long, uint32_t> strided(const std::vector<uint32_t>& offs) {
+  if (offs.empty()) return {-1, 0};
+  const uint32_t d = offs.size() > 1 ? offs[1] - offs[0] : 0;
+  for (size_t k = 0; k < offs.size(); ++k)
+    if (offs[k] != offs[0] + (uint32_t)k * d) return {-1, 0};
+  return {(long long)offs[0], d};
+}
+
 // First group of a group task list whose groups are consecutive (a layout
 // appends each depth's groups together), else -1.
 int consecutiveGroups(const std::vector<int>& tasks) {
@@ -314,6 +324,9 @@ void Engine::buildPlans() {
         l.list2 = d.fCh[tr][lv];
         l.bytes2 = listBytes(L_.fwdChance[tr][lv], tr, true);
         l.early = tr == 0;  // the first half-step of the iteration
+        const auto st = strided(L_.fwdRecs[tr][lv]);
+        l.recBase = st.first;
+        l.recStride = st.second;
         h.fwd[lv].push_back(l);
       }
     }

@@ -719,9 +719,18 @@ HostLayout buildLayout(const Tree& t) {
   // them, one writes them into the pool sized once.
   auto recWords = [](int na) { return (size_t)(4 + na + 3) / 4 * 4; };
   auto chunksOf = [](int n) { return (int)((quads(n) + kRecQuads - 1) / kRecQuads); };
+  // Forward records lie apart from the backward ones: per traverser and
+  // forward level, in node order, each padded to the level's largest record,
+  // so a level's records sit at one stride from its first (a kernel can
+  // compute a record's offset from its index).
   size_t words = L.recPool.size();
   std::vector<size_t> nBwd[2] = {std::vector<size_t>(D, 0), std::vector<size_t>(D, 0)};
-  std::vector<size_t> nFwd[2] = {std::vector<size_t>(D, 0), std::vector<size_t>(D, 0)};
+  std::vector<std::vector<int>> fwdNodes[2];  // per forward level: its nodes
+  std::vector<size_t> fwdSpan[2];              // per forward level: words a record
+  for (int tr = 0; tr < 2; ++tr) {
+    fwdNodes[tr].assign(F[tr], {});
+    fwdSpan[tr].assign(F[tr], 0);
+  }
   for (int u = 0; u < N; ++u) {
     const Node& nd = t.nodes[u];
     if (nd.kind != kDecide) continue;
@@ -730,17 +739,25 @@ HostLayout buildLayout(const Tree& t) {
       nBwd[tr][nd.depth] += cb;
       words += cb * recWords(nd.na);
       if (nd.player == tr) continue;
-      const int cf = chunksOf(t.n(u, 1 - tr));
-      nFwd[tr][nd.depth] += cf;
-      words += cf * recWords(nd.na);
+      const int lv = fwdLevel[tr][u];
+      fwdNodes[tr][lv].push_back(u);
+      fwdSpan[tr][lv] = std::max(fwdSpan[tr][lv], recWords(nd.na));
     }
   }
+  for (int tr = 0; tr < 2; ++tr)
+    for (int lv = 0; lv < F[tr]; ++lv) {
+      size_t nf = 0;
+      for (int u : fwdNodes[tr][lv]) nf += chunksOf(t.n(u, 1 - tr));
+      L.fwdRecs[tr][lv].reserve(nf);
+      words += nf * fwdSpan[tr][lv];
+    }
   for (int tr = 0; tr < 2; ++tr)
     for (int d = 0; d < D; ++d) L.bwdRecs[tr][d].reserve(nBwd[tr][d]);
   size_t w = L.recPool.size();
   L.recPool.resize(words, 0u);
   std::vector<uint32_t> kids;
-  auto addRecord = [&](uint32_t regQ, uint32_t rowQ, int n, int na, int own, int chunk) {
+  auto addRecord = [&](uint32_t regQ, uint32_t rowQ, int n, int na, int own, int chunk,
+                       size_t span) {
     const uint32_t off = (uint32_t)(w / 4);
     uint32_t* r = L.recPool.data() + w;
     r[0] = regQ;
@@ -748,7 +765,7 @@ HostLayout buildLayout(const Tree& t) {
     r[2] = (uint32_t)n | ((uint32_t)na << 16) | ((uint32_t)own << 24);
     r[3] = (uint32_t)chunk;
     for (int a = 0; a < na; ++a) r[4 + a] = kids[a];
-    w += recWords(na);
+    w += span;
     return off;
   };
   std::vector<uint32_t> bwdRecFirst[2] = {std::vector<uint32_t>(N, 0),
@@ -762,17 +779,22 @@ HostLayout buildLayout(const Tree& t) {
       const int nTr = t.n(u, tr);
       bwdRecFirst[tr][u] = (uint32_t)(w / 4);
       for (int c = 0, cb = chunksOf(nTr); c < cb; ++c)
-        L.bwdRecs[tr][nd.depth].push_back(
-            addRecord(L.nodes[u].regQ, L.rows[u].cfvQ, nTr, nd.na, nd.player == tr, c));
-      if (nd.player == tr) continue;
-      for (int a = 0; a < nd.na; ++a)
-        kids[a] = L.rows[t.children[nd.childBase + a]].reachQ[tr];
-      const int nOpp = t.n(u, 1 - tr);
-      for (int c = 0, cf = chunksOf(nOpp); c < cf; ++c)
-        L.fwdRecs[tr][fwdLevel[tr][u]].push_back(
-            addRecord(L.nodes[u].regQ, L.rows[u].reachQ[tr], nOpp, nd.na, 0, c));
+        L.bwdRecs[tr][nd.depth].push_back(addRecord(L.nodes[u].regQ, L.rows[u].cfvQ, nTr, nd.na,
+                                                    nd.player == tr, c, recWords(nd.na)));
     }
   }
+  for (int tr = 0; tr < 2; ++tr)
+    for (int lv = 0; lv < F[tr]; ++lv)
+      for (int u : fwdNodes[tr][lv]) {
+        const Node& nd = t.nodes[u];
+        kids.resize(nd.na);
+        for (int a = 0; a < nd.na; ++a)
+          kids[a] = L.rows[t.children[nd.childBase + a]].reachQ[tr];
+        const int nOpp = t.n(u, 1 - tr);
+        for (int c = 0, cf = chunksOf(nOpp); c < cf; ++c)
+          L.fwdRecs[tr][lv].push_back(addRecord(L.nodes[u].regQ, L.rows[u].reachQ[tr], nOpp,
+                                                nd.na, 0, c, fwdSpan[tr][lv]));
+      }
   // Chance records: every row and table address a chance task needs, so a
   // CTA reaches its data in two dependent loads.
   //   forward, per branch: [parent reach row, child reach row (quads, the

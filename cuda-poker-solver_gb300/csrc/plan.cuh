@@ -59,6 +59,11 @@ struct Launch {
   // (one spot's layout): the kernels take a CTA's record from its task
   // index instead of loading the task word first. -1: read the list.
   int groupBase = -1;
+  // kFwdMix: the list's records are recBase + k recStride (16-byte units;
+  // one spot's layout), so the kernel computes a record's offset from its
+  // index instead of loading it. -1: read the list.
+  long long recBase = -1;
+  uint32_t recStride = 0;
 };
 
 // What the level launches of a plan read: the tree, the f32 rows, the
@@ -147,8 +152,10 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       const uint32_t* rt = a.recTasks + l.list.off;
       const uint32_t* ch = a.recTasks + l.list2.off;  // chance record offsets
       if (l.kind == kFwdMix)
-        GB_CK(cudaLaunchKernelEx(&cfg, fwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
-                                 ch, l.list2.count, l.tr, l.late ? 1 : 0, l.early ? 1 : 0));
+        GB_CK(cudaLaunchKernelEx(&cfg, fwdLevelMixK, a.tree, a.rows, a.recs,
+                                 l.recBase >= 0 ? nullptr : rt, l.list.count, ch, l.list2.count,
+                                 l.tr, l.late ? 1 : 0, l.early ? 1 : 0,
+                                 (uint32_t)(l.recBase >= 0 ? l.recBase : 0), l.recStride));
       else
         GB_CK(cudaLaunchKernelEx(&cfg, bwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
                                  ch, l.list2.count, l.tr));
