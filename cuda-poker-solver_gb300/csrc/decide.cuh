@@ -825,8 +825,8 @@ __host__ __device__ constexpr size_t bwdStageBytes() {
 // returned (so a grid that has launched implies that the grid two places
 // before it has completed; the fused plan relies on that), instead of at
 // its start.
-// recTasks null: the level's records are recBase + k recStride (16-byte
-// units), at one stride from the first.
+// recTasks (chance) null: the level's records are recBase + k recStride
+// (chBase + i chStride; 16-byte units), at one stride from the first.
 // early: the records ask for their regret rows before the wait. Only for
 // the first half-step of an iteration (traverser 0): the regrets it reads
 // are the other player's, written by the second half-step of an earlier
@@ -836,7 +836,8 @@ __host__ __device__ constexpr size_t bwdStageBytes() {
 static __global__ void __launch_bounds__(kThreads, 10)
 fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
              const uint32_t* __restrict__ recTasks, int nRec, const uint32_t* __restrict__ chance,
-             int nCh, int tr, int late, int early, uint32_t recBase, uint32_t recStride) {
+             int nCh, int tr, int late, int early, uint32_t recBase, uint32_t recStride,
+             uint32_t chBase, uint32_t chStride) {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* stage = reinterpret_cast<float4*>(smem);
   if (!late) pdlTrigger();
@@ -855,7 +856,7 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
       waited = true;
       fwdDecideRecordStaged(t, rows, tr, r, lane, stage, early != 0);
     } else {
-      const uint4 h = loadChanceHeader(recs, chance[i]);
+      const uint4 h = loadChanceHeader(recs, chance ? chance[i] : chBase + (uint32_t)i * chStride);
       const bool st = fwdChanceStaged(h, fwdStageBytes());
       uint16_t* upS = reinterpret_cast<uint16_t*>(smem);
       if (st) fwdChanceSlots(t, h, upS);

@@ -48,7 +48,8 @@ V* alloc(size_t count, size_t& bytes) {
 }
 
 // A record list at one stride from its first record: {first, stride}, else
-// {-1, 0} (a layout places each forward level's records so).
+// {-1, 0} (a layout places each forward level's decide records so, and its
+// chance records one after another).
 std::pair<long long, uint32_t> strided(const std::vector<uint32_t>& offs) {
   if (offs.empty()) return {-1, 0};
   const uint32_t d = offs.size() > 1 ? offs[1] - offs[0] : 0;
@@ -324,9 +325,11 @@ void Engine::buildPlans() {
         l.list2 = d.fCh[tr][lv];
         l.bytes2 = listBytes(L_.fwdChance[tr][lv], tr, true);
         l.early = tr == 0;  // the first half-step of the iteration
-        const auto st = strided(L_.fwdRecs[tr][lv]);
+        const auto st = strided(L_.fwdRecs[tr][lv]), sc = strided(L_.fwdChanceRecs[tr][lv]);
         l.recBase = st.first;
         l.recStride = st.second;
+        l.chBase = sc.first;
+        l.chStride = sc.second;
         h.fwd[lv].push_back(l);
       }
     }

@@ -64,6 +64,8 @@ struct Launch {
   // index instead of loading it. -1: read the list.
   long long recBase = -1;
   uint32_t recStride = 0;
+  long long chBase = -1;  // kFwdMix: the same for the chance records (list2)
+  uint32_t chStride = 0;
 };
 
 // What the level launches of a plan read: the tree, the f32 rows, the
@@ -153,9 +155,11 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
       const uint32_t* ch = a.recTasks + l.list2.off;  // chance record offsets
       if (l.kind == kFwdMix)
         GB_CK(cudaLaunchKernelEx(&cfg, fwdLevelMixK, a.tree, a.rows, a.recs,
-                                 l.recBase >= 0 ? nullptr : rt, l.list.count, ch, l.list2.count,
-                                 l.tr, l.late ? 1 : 0, l.early ? 1 : 0,
-                                 (uint32_t)(l.recBase >= 0 ? l.recBase : 0), l.recStride));
+                                 l.recBase >= 0 ? nullptr : rt, l.list.count,
+                                 l.chBase >= 0 ? nullptr : ch, l.list2.count, l.tr,
+                                 l.late ? 1 : 0, l.early ? 1 : 0,
+                                 (uint32_t)(l.recBase >= 0 ? l.recBase : 0), l.recStride,
+                                 (uint32_t)(l.chBase >= 0 ? l.chBase : 0), l.chStride));
       else
         GB_CK(cudaLaunchKernelEx(&cfg, bwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
                                  ch, l.list2.count, l.tr));
