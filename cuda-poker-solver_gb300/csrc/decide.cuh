@@ -158,6 +158,24 @@ struct DecRec {
   const uint32_t* pre;  // folded-in children (header bit 25), else nullptr
 };
 
+// A level's record offsets as up to four arithmetic runs (records grouped
+// by size class): run j covers the indices [end[j - 1], end[j]) at base[j] +
+// (k - end[j - 1]) stride[j] (16-byte units).
+struct RecRuns {
+  uint32_t end[4], base[4], stride[4];
+};
+// Offset of record k: from the level's offset list, or (list null) from
+// its runs.
+__device__ __forceinline__ uint32_t recOffset(const uint32_t* __restrict__ recTasks,
+                                              const RecRuns& R, int k) {
+  if (recTasks) return recTasks[k];
+  const uint32_t u = (uint32_t)k;
+  if (u < R.end[0]) return R.base[0] + u * R.stride[0];
+  if (u < R.end[1]) return R.base[1] + (u - R.end[0]) * R.stride[1];
+  if (u < R.end[2]) return R.base[2] + (u - R.end[1]) * R.stride[2];
+  return R.base[3] + (u - R.end[2]) * R.stride[3];
+}
+
 __device__ __forceinline__ DecRec loadRec(const uint32_t* __restrict__ recs, uint32_t off16) {
   const uint32_t* r = recs + (size_t)off16 * 4;
   const uint4 h = *reinterpret_cast<const uint4*>(r);
@@ -875,7 +893,7 @@ fwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
 static __global__ void __launch_bounds__(kThreads, 8)
 bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
              const uint32_t* __restrict__ recTasks, int nRec, const uint32_t* __restrict__ chance,
-             int nCh, int tr) {
+             int nCh, int tr, RecRuns runs) {
   extern __shared__ __align__(16) unsigned char smem[];  // bwdStageBytes()
   pdlTrigger();
   const int nRc = recordCtas(nRec), lane = (int)threadIdx.x & 31;
@@ -893,7 +911,7 @@ bwdLevelMixK(DevTree t, DevRows<float> rows, const uint32_t* __restrict__ recs,
     if (i >= nCh) {
       const int k = (i - nCh) * kRecWarps + (int)(threadIdx.x >> 5);
       if (k >= nRec) continue;
-      const DecRec r = loadRec(recs, recTasks[k]);
+      const DecRec r = loadRec(recs, recOffset(recTasks, runs, k));
       decideRecordBulk(t, rows, r, lane,  // waits for the previous level itself
                        reinterpret_cast<float4*>(smem) + warp * 3 * kAsyncNa * kRecQuads, bar,
                        phase, broken);

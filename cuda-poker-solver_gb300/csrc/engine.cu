@@ -58,6 +58,30 @@ std::pair<long long, uint32_t> strided(const std::vector<uint32_t>& offs) {
   return {(long long)offs[0], d};
 }
 
+// A record list as at most four arithmetic runs (a layout groups each
+// backward level's records by size class); false if it needs more.
+bool recRuns(const std::vector<uint32_t>& offs, RecRuns& R) {
+  if (offs.empty()) return false;
+  size_t i = 0;
+  int j = 0;
+  while (i < offs.size()) {
+    if (j == 4) return false;
+    const uint32_t st = i + 1 < offs.size() ? offs[i + 1] - offs[i] : 0;
+    size_t e = i + 1;
+    while (e < offs.size() && offs[e] == offs[i] + (uint32_t)(e - i) * st) ++e;
+    R.base[j] = offs[i];
+    R.stride[j] = st;
+    R.end[j] = (uint32_t)e;
+    ++j;
+    i = e;
+  }
+  for (; j < 4; ++j) {
+    R.base[j] = R.stride[j] = 0;
+    R.end[j] = 0xffffffffu;
+  }
+  return true;
+}
+
 // First group of a group task list whose groups are consecutive (a layout
 // appends each depth's groups together), else -1.
 int consecutiveGroups(const std::vector<int>& tasks) {
@@ -353,6 +377,7 @@ void Engine::buildPlans() {
       Launch l{kBwdMix, tr, d.bRecH[tr][lv], listBytes(L_.bwdTasksH[tr][lv], tr, false)};
       l.list2 = d.bChH[tr][lv];
       l.bytes2 = listBytes(kindOnly(L_.bwdTasksH[tr][lv], kTaskChance), tr, false);
+      l.runsOn = recRuns(L_.bwdRecsH[tr][lv], l.runs);
       h.bwd[lv].push_back(l);
     }
   }

@@ -602,8 +602,9 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
           for (int a = 0; a < na; ++a) r[4 + a] += rowOff;
         }
     }
-  // Records with folded-in children (the backward levels' own records):
-  // the header rows, the child rows and every folded-in row list.
+  // The backward levels' own records: the header rows, the child rows and,
+  // where there are folded-in children (header bit 25), every folded-in row
+  // list.
   for (int tr = 0; tr < 2; ++tr)
     for (uint32_t o : L.presumRecs[tr]) {
       uint32_t* r = &L.recPool[(size_t)o * 4];
@@ -613,6 +614,7 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
       r[1] += cfv;
       r[3] = (r[3] & 0xffffu) | ((uint32_t)slot << 16);
       for (int a = 0; a < na; ++a) r[4 + a] += cfv;
+      if (!((r[2] >> 25) & 1)) continue;
       uint32_t* p = r + 4 + na;
       const int P = (int)*p++;
       for (int e = 0; e < P; ++e) {

@@ -322,8 +322,9 @@ namespace {
 //     by nothing in the iteration).
 // The records of a traverser node with folded-in children are new: [regret
 // row, value row, n | na << 16 | 1 << 24 | 1 << 25, chunk, child rows[na],
-// P, then P times (child value row, m, its m children's value rows)],
-// padded to 16 bytes; other nodes reuse their depth-list records.
+// P, then P times (child value row, m, its m children's value rows)]; other
+// nodes' records are copies of their depth-list records. Each level's
+// records lie together in the pool (by size class, see below).
 void buildBackwardLevels(const Tree& t, HostLayout& L,
                          const std::vector<uint32_t> (&firstRec)[2],
                          const std::vector<std::vector<uint32_t>> (&chanceRecs)[2]) {
@@ -389,6 +390,9 @@ void buildBackwardLevels(const Tree& t, HostLayout& L,
     L.bwdTasksH[tr].assign(H, {});
     L.bwdNeed[tr].assign(H, 0);
     L.presumRecs[tr].clear();
+    // Each level's records, written to the pool after the walk (below):
+    // their words end to end, and where each starts.
+    std::vector<std::vector<uint32_t>> pendWords(H), pendStart(H);
     for (int u = 0; u < N; ++u) {
       if (h[u] < 0) continue;
       const Node& nd = t.nodes[u];
@@ -405,9 +409,14 @@ void buildBackwardLevels(const Tree& t, HostLayout& L,
         L.bwdTasksH[tr][lv].push_back(makeTask(kTaskDecide, c, u));
       bool folds = false;
       for (int a = 0; a < nd.na; ++a) folds |= foldedIn(child(u, a));
-      if (!folds) {  // the depth-list records, unchanged
+      std::vector<uint32_t>& pw = pendWords[lv];
+      if (!folds) {  // copies of the depth-list records
         const uint32_t stride = (uint32_t)(recWords(nd.na) / 4);
-        for (int c = 0; c < nc; ++c) L.bwdRecsH[tr][lv].push_back(firstRec[tr][u] + (uint32_t)c * stride);
+        for (int c = 0; c < nc; ++c) {
+          const size_t at = (size_t)(firstRec[tr][u] + (uint32_t)c * stride) * 4;
+          pendStart[lv].push_back((uint32_t)pw.size());
+          pw.insert(pw.end(), L.recPool.begin() + at, L.recPool.begin() + at + 4 + nd.na);
+        }
         continue;
       }
       for (int a = 0; a < nd.na; ++a) {  // the folded-in children's work (byte model)
@@ -417,29 +426,60 @@ void buildBackwardLevels(const Tree& t, HostLayout& L,
             L.bwdTasksH[tr][lv].push_back(makeTask(kTaskDecide, c, k));
       }
       for (int c = 0; c < nc; ++c) {
-        while (L.recPool.size() % 4) L.recPool.push_back(0);
-        const uint32_t off = (uint32_t)(L.recPool.size() / 4);
-        L.recPool.push_back(L.nodes[u].regQ);
-        L.recPool.push_back(L.rows[u].cfvQ);
-        L.recPool.push_back((uint32_t)n | ((uint32_t)nd.na << 16) | (1u << 24) | (1u << 25));
-        L.recPool.push_back((uint32_t)c);
+        pendStart[lv].push_back((uint32_t)pw.size());
+        pw.push_back(L.nodes[u].regQ);
+        pw.push_back(L.rows[u].cfvQ);
+        pw.push_back((uint32_t)n | ((uint32_t)nd.na << 16) | (1u << 24) | (1u << 25));
+        pw.push_back((uint32_t)c);
         int P = 0;
         for (int a = 0; a < nd.na; ++a) {
-          L.recPool.push_back(L.rows[child(u, a)].cfvQ);
+          pw.push_back(L.rows[child(u, a)].cfvQ);
           P += foldedIn(child(u, a)) ? 1 : 0;
         }
-        L.recPool.push_back((uint32_t)P);
+        pw.push_back((uint32_t)P);
         for (int a = 0; a < nd.na; ++a) {
           const int k = child(u, a);
           if (!foldedIn(k)) continue;
-          L.recPool.push_back(L.rows[k].cfvQ);
-          L.recPool.push_back((uint32_t)t.nodes[k].nChildren);
-          for (int b = 0; b < t.nodes[k].nChildren; ++b)
-            L.recPool.push_back(L.rows[child(k, b)].cfvQ);
+          pw.push_back(L.rows[k].cfvQ);
+          pw.push_back((uint32_t)t.nodes[k].nChildren);
+          for (int b = 0; b < t.nodes[k].nChildren; ++b) pw.push_back(L.rows[child(k, b)].cfvQ);
         }
-        while (L.recPool.size() % 4) L.recPool.push_back(0);
-        L.bwdRecsH[tr][lv].push_back(off);
-        L.presumRecs[tr].push_back(off);
+      }
+    }
+    // A level's records lie together, grouped by size class (16-byte units
+    // rounded up to a power of two, at least two; the largest class first,
+    // so the records with the most work start first and the level's tail is
+    // short), each padded to its class: the level's offsets form a few
+    // arithmetic runs, from which a kernel computes a record's offset
+    // instead of loading it.
+    while (L.recPool.size() % 4) L.recPool.push_back(0);
+    constexpr int kClasses = 16;  // class c: 2 << c units
+    for (int lv = 0; lv < H; ++lv) {
+      const std::vector<uint32_t>& pw = pendWords[lv];
+      std::vector<uint32_t>& ps = pendStart[lv];
+      const size_t nr = ps.size();
+      ps.push_back((uint32_t)pw.size());
+      std::vector<uint8_t> cls(nr);
+      size_t count[kClasses] = {}, words = 0;
+      for (size_t i = 0; i < nr; ++i) {
+        int c = 0;
+        while (c + 1 < kClasses && (size_t)(8u << c) < ps[i + 1] - ps[i]) ++c;
+        cls[i] = (uint8_t)c;
+        ++count[c];
+        words += (size_t)(8u << c);
+      }
+      L.recPool.reserve(L.recPool.size() + words);
+      L.bwdRecsH[tr][lv].reserve(nr);
+      for (int c = kClasses - 1; c >= 0; --c) {
+        if (!count[c]) continue;
+        for (size_t i = 0; i < nr; ++i) {
+          if (cls[i] != c) continue;
+          const uint32_t off = (uint32_t)(L.recPool.size() / 4);
+          L.recPool.insert(L.recPool.end(), pw.begin() + ps[i], pw.begin() + ps[i + 1]);
+          L.recPool.resize((size_t)off * 4 + (8u << c), 0u);
+          L.bwdRecsH[tr][lv].push_back(off);
+          L.presumRecs[tr].push_back(off);
+        }
       }
     }
   }

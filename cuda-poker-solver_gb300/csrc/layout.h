@@ -188,7 +188,8 @@ struct HostLayout {
   // also compute the value rows of its opponent children, so those need no
   // level; decide and chance record offsets, the same work as task words
   // (byte model), per level the depths of the terminal nodes it reads (bit
-  // d), and the records with folded-in children (relocated on their own).
+  // d), and every record of the levels (their own copies, grouped by size
+  // class: relocated on their own).
   std::vector<std::vector<uint32_t>> bwdRecsH[2], bwdChanceRecsH[2];
   std::vector<std::vector<int>> bwdTasksH[2];
   std::vector<uint64_t> bwdNeed[2];

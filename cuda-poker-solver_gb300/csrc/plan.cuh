@@ -66,6 +66,10 @@ struct Launch {
   uint32_t recStride = 0;
   long long chBase = -1;  // kFwdMix: the same for the chance records (list2)
   uint32_t chStride = 0;
+  // kBwdMix: the level's records as arithmetic runs (one spot's layout),
+  // used instead of the list when runsOn.
+  bool runsOn = false;
+  RecRuns runs{};
 };
 
 // What the level launches of a plan read: the tree, the f32 rows, the
@@ -161,8 +165,9 @@ static inline void issueLaunch(const PlanArgs& a, const Launch& l, cudaStream_t 
                                  (uint32_t)(l.recBase >= 0 ? l.recBase : 0), l.recStride,
                                  (uint32_t)(l.chBase >= 0 ? l.chBase : 0), l.chStride));
       else
-        GB_CK(cudaLaunchKernelEx(&cfg, bwdLevelMixK, a.tree, a.rows, a.recs, rt, l.list.count,
-                                 ch, l.list2.count, l.tr));
+        GB_CK(cudaLaunchKernelEx(&cfg, bwdLevelMixK, a.tree, a.rows, a.recs,
+                                 l.runsOn ? nullptr : rt, l.list.count, ch, l.list2.count, l.tr,
+                                 l.runs));
       break;
     }
     case kCounter:
