@@ -606,7 +606,7 @@ int Forest::admit(std::unique_ptr<CompiledSpot>& s, size_t budget) {
   // where there are folded-in children (header bit 25), every folded-in row
   // list.
   for (int tr = 0; tr < 2; ++tr)
-    for (uint32_t o : L.presumRecs[tr]) {
+    for (uint32_t o : L.levelRecs[tr]) {
       uint32_t* r = &L.recPool[(size_t)o * 4];
       const int na = (int)((r[2] >> 16) & 0xff);
       const uint32_t cfv = (uint32_t)off[rCfv];

@@ -389,7 +389,7 @@ void buildBackwardLevels(const Tree& t, HostLayout& L,
     L.bwdChanceRecsH[tr].assign(H, {});
     L.bwdTasksH[tr].assign(H, {});
     L.bwdNeed[tr].assign(H, 0);
-    L.presumRecs[tr].clear();
+    L.levelRecs[tr].clear();
     // Each level's records, written to the pool after the walk (below):
     // their words end to end, and where each starts.
     std::vector<std::vector<uint32_t>> pendWords(H), pendStart(H);
@@ -478,7 +478,7 @@ void buildBackwardLevels(const Tree& t, HostLayout& L,
           L.recPool.insert(L.recPool.end(), pw.begin() + ps[i], pw.begin() + ps[i + 1]);
           L.recPool.resize((size_t)off * 4 + (8u << c), 0u);
           L.bwdRecsH[tr][lv].push_back(off);
-          L.presumRecs[tr].push_back(off);
+          L.levelRecs[tr].push_back(off);
         }
       }
     }
@@ -967,7 +967,7 @@ uint64_t layoutDigest(const HostLayout& L) {
     f.vecs(L.bwdChanceRecsH[tr]);
     f.vecs(L.bwdTasksH[tr]);
     f.vec(L.bwdNeed[tr]);
-    f.vec(L.presumRecs[tr]);
+    f.vec(L.levelRecs[tr]);
   }
   f.bytes(&L.maxN, sizeof L.maxN);
   f.bytes(&L.maxCardSeg, sizeof L.maxCardSeg);

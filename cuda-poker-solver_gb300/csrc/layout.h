@@ -193,7 +193,7 @@ struct HostLayout {
   std::vector<std::vector<uint32_t>> bwdRecsH[2], bwdChanceRecsH[2];
   std::vector<std::vector<int>> bwdTasksH[2];
   std::vector<uint64_t> bwdNeed[2];
-  std::vector<uint32_t> presumRecs[2];
+  std::vector<uint32_t> levelRecs[2];
   int maxN = 0;        // largest list size (either side)
   int maxCardSeg = 0;  // longest card segment of any list
 };
