@@ -335,7 +335,12 @@ void buildBackwardLevels(const Tree& t, HostLayout& L,
   };
   auto chunks = [](int n) { return (int)((quads(n) + kRecQuads - 1) / kRecQuads); };
   auto recWords = [](int na) { return (size_t)(4 + na + 3) / 4 * 4; };
-  for (int tr = 0; tr < 2; ++tr) {
+  // Each level's records: their words end to end, and where each starts.
+  // The traversers' levels are built in parallel (they read the pool and
+  // write only their own lists); their records go into the pool after, in
+  // traverser order.
+  std::vector<std::vector<uint32_t>> pendWordsOf[2], pendStartOf[2];
+  parallelFor(2, [&](int tr) {
     auto opponent = [&](int u) {
       return t.nodes[u].kind == kDecide && t.nodes[u].player != tr;
     };
@@ -390,9 +395,10 @@ void buildBackwardLevels(const Tree& t, HostLayout& L,
     L.bwdTasksH[tr].assign(H, {});
     L.bwdNeed[tr].assign(H, 0);
     L.levelRecs[tr].clear();
-    // Each level's records, written to the pool after the walk (below):
-    // their words end to end, and where each starts.
-    std::vector<std::vector<uint32_t>> pendWords(H), pendStart(H);
+    std::vector<std::vector<uint32_t>>& pendWords = pendWordsOf[tr];
+    std::vector<std::vector<uint32_t>>& pendStart = pendStartOf[tr];
+    pendWords.assign(H, {});
+    pendStart.assign(H, {});
     for (int u = 0; u < N; ++u) {
       if (h[u] < 0) continue;
       const Node& nd = t.nodes[u];
@@ -446,6 +452,9 @@ void buildBackwardLevels(const Tree& t, HostLayout& L,
         }
       }
     }
+  });
+  for (int tr = 0; tr < 2; ++tr) {
+    const int H = (int)pendWordsOf[tr].size();
     // A level's records lie together, grouped by size class (16-byte units
     // rounded up to a power of two, at least two; the largest class first,
     // so the records with the most work start first and the level's tail is
@@ -455,8 +464,8 @@ void buildBackwardLevels(const Tree& t, HostLayout& L,
     while (L.recPool.size() % 4) L.recPool.push_back(0);
     constexpr int kClasses = 16;  // class c: 2 << c units
     for (int lv = 0; lv < H; ++lv) {
-      const std::vector<uint32_t>& pw = pendWords[lv];
-      std::vector<uint32_t>& ps = pendStart[lv];
+      const std::vector<uint32_t>& pw = pendWordsOf[tr][lv];
+      std::vector<uint32_t>& ps = pendStartOf[tr][lv];
       const size_t nr = ps.size();
       ps.push_back((uint32_t)pw.size());
       std::vector<uint8_t> cls(nr);
