@@ -169,6 +169,37 @@ def test_layout_is_pinned_and_deterministic(golden_dir):
         assert got[0] == got[1] == int(hexd, 16), name
 
 
+def test_layouts_built_concurrently_match(golden_dir):
+    """Layouts built from several threads at once (as a batch's compile
+    workers build them; each build also runs its own helper threads) are
+    the pinned bytes."""
+    import threading
+    from pps import workloads as wl
+    from helpers import abi_cfgs
+    with open(os.path.join(golden_dir, "layout_digests.json")) as f:
+        want = json.load(f)["digests"]
+    names = ["turn_w52", "turn_c2_uniform", "flop_small", "turn_api"]
+    got, errors = {}, []
+
+    def work(k):
+        try:
+            for name in names[k % len(names):] + names[:k % len(names)]:
+                sp = wl.NAMED[name]()
+                d = pn.layout_digest(sp.board, sp.oop, sp.ip, sp.pot, sp.stack, abi_cfgs(sp))
+                got.setdefault(name, []).append(d)
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    for name in names:
+        assert got[name] == [int(want[name], 16)] * 4, name
+
+
 def test_cli_argument_errors():
     """gpu_pfflop rejects bad arguments before any device use, with the
     reference CLI's messages and exit status 2 (tools/gpu_pfflop.cu:44-52,
